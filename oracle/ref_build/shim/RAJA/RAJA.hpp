@@ -1,0 +1,10 @@
+// Umbrella stand-in for RAJA/RAJA.hpp. Only Base_Seq code paths are compiled
+// against it (RUN_RAJA_SEQ, RUN_OPENMP and the GPU back ends stay undefined).
+#ifndef ORACLE_SHIM_RAJA_HPP
+#define ORACLE_SHIM_RAJA_HPP
+#include "RAJA/config.hpp"
+#include "RAJA/util/types.hpp"
+#include "RAJA/util/macros.hpp"
+#include "RAJA/util/Timer.hpp"
+#include "RAJA/internal/MemUtils_CPU.hpp"
+#endif

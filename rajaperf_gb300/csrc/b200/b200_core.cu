@@ -1,0 +1,258 @@
+// libb200 core: error state, launch accounting, device properties, tuning
+// resolution and the data-initialisation kernels.
+#include "b200_internal.cuh"
+
+#include <mutex>
+#include <vector>
+
+namespace b200 {
+
+static thread_local std::string g_last_error;
+static std::atomic<int64_t> g_launches{0};
+static std::mutex g_info_mu;
+static std::vector<DeviceInfo> g_info;
+
+void set_error(const char* fmt, ...) {
+  char buf[512];
+  va_list ap;
+  va_start(ap, fmt);
+  std::vsnprintf(buf, sizeof(buf), fmt, ap);
+  va_end(ap);
+  g_last_error = buf;
+}
+
+void clear_error() { g_last_error.clear(); }
+
+int invalid(const char* fmt, ...) {
+  char buf[512];
+  va_list ap;
+  va_start(ap, fmt);
+  std::vsnprintf(buf, sizeof(buf), fmt, ap);
+  va_end(ap);
+  g_last_error = buf;
+  return B200_ERR_INVALID_ARG;
+}
+
+int after_launch(const char* what, int nlaunches) {
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) {
+    set_error("%s: launch failed: %s", what, cudaGetErrorString(e));
+    return B200_ERR_LAUNCH;
+  }
+  g_launches.fetch_add(nlaunches, std::memory_order_relaxed);
+  return B200_OK;
+}
+
+const DeviceInfo& device_info() {
+  int dev = 0;
+  cudaGetDevice(&dev);
+  std::lock_guard<std::mutex> lk(g_info_mu);
+  if (static_cast<int>(g_info.size()) <= dev) g_info.resize(dev + 1);
+  DeviceInfo& d = g_info[dev];
+  if (d.device != dev) {
+    cudaDeviceProp p;
+    if (cudaGetDeviceProperties(&p, dev) == cudaSuccess) {
+      d.sm_count = p.multiProcessorCount;
+      d.cc_major = p.major;
+      d.cc_minor = p.minor;
+      d.global_mem = p.totalGlobalMem;
+      d.l2_bytes = p.l2CacheSize;
+      d.max_smem_optin = static_cast<int>(p.sharedMemPerBlockOptin);
+    } else {
+      cudaGetLastError();
+      d.sm_count = 152;
+    }
+    d.device = dev;
+  }
+  return d;
+}
+
+Shape resolve_1d(const b200_tune* t, int64_t units, int def_block,
+                 int def_items, int def_vec, int64_t max_grid) {
+  Shape s;
+  s.block = (t && t->block_size) ? t->block_size : def_block;
+  s.items = (t && t->items) ? t->items : def_items;
+  s.vec = (t && t->vec) ? t->vec : def_vec;
+  int64_t cap = (t && t->grid_blocks) ? t->grid_blocks : max_grid;
+  int64_t tiles = ceil_div(units > 0 ? units : 1,
+                           static_cast<int64_t>(s.block) * s.items);
+  if (cap > 0 && tiles > cap) tiles = cap;
+  if (tiles > 0x7fffffffLL) tiles = 0x7fffffffLL;
+  s.grid = static_cast<int>(tiles < 1 ? 1 : tiles);
+  return s;
+}
+
+}  // namespace b200
+
+using b200::g_last_error;
+using b200::g_launches;
+using b200::invalid;
+using b200::after_launch;
+using b200::as_stream;
+using b200::device_info;
+using b200::ceil_div;
+using b200::DeviceInfo;
+
+// ---- initialisation kernels -------------------------------------------------
+
+namespace {
+
+__global__ void init_reference_kernel(double* __restrict__ p, int64_t n,
+                                      double factor) {
+  int64_t stride = static_cast<int64_t>(gridDim.x) * blockDim.x;
+  for (int64_t i = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+       i < n; i += stride) {
+    // Same operation order as the host formula; __dmul_rn/__ddiv_rn keep the
+    // compiler from contracting it, so the values are bit-identical.
+    double di = static_cast<double>(i);
+    p[i] = __ddiv_rn(__dmul_rn(factor, __dadd_rn(di, 1.1)),
+                     __dadd_rn(di, 1.12345));
+  }
+}
+
+__global__ void init_reference_signed_kernel(double* __restrict__ p,
+                                             const int8_t* __restrict__ sign,
+                                             int64_t n, double factor) {
+  int64_t stride = static_cast<int64_t>(gridDim.x) * blockDim.x;
+  for (int64_t i = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+       i < n; i += stride) {
+    double di = static_cast<double>(i);
+    double s = sign[i] < 0 ? -1.0 : 1.0;
+    p[i] = __ddiv_rn(__dmul_rn(__dmul_rn(s, factor), __dadd_rn(di, 1.1)),
+                     __dadd_rn(di, 1.12345));
+  }
+}
+
+template <typename T>
+__global__ void init_const_kernel(T* __restrict__ p, int64_t n, T v) {
+  int64_t stride = static_cast<int64_t>(gridDim.x) * blockDim.x;
+  for (int64_t i = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+       i < n; i += stride) {
+    p[i] = v;
+  }
+}
+
+// splitmix64 finaliser over (seed, stream, index): a counter-based generator,
+// so any element can be produced independently on the host or the device.
+__host__ __device__ inline uint64_t mix64(uint64_t z) {
+  z = (z ^ (z >> 30)) * 0xbf58476d1ce4e5b9ULL;
+  z = (z ^ (z >> 27)) * 0x94d049bb133111ebULL;
+  return z ^ (z >> 31);
+}
+
+__device__ inline uint64_t counter_bits(uint64_t seed, uint64_t stream,
+                                        uint64_t i) {
+  uint64_t key = mix64(seed + 0x9e3779b97f4a7c15ULL * (stream + 1));
+  return mix64(key + 0x9e3779b97f4a7c15ULL * (i + 1));
+}
+
+__global__ void init_uniform_kernel(double* __restrict__ p, int64_t n,
+                                    uint64_t seed, uint64_t stream, double lo,
+                                    double width) {
+  int64_t stride = static_cast<int64_t>(gridDim.x) * blockDim.x;
+  for (int64_t i = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+       i < n; i += stride) {
+    double u = static_cast<double>(counter_bits(seed, stream, i) >> 11) *
+               0x1.0p-53;
+    p[i] = __dadd_rn(lo, __dmul_rn(width, u));
+  }
+}
+
+__global__ void init_uniform_i64_kernel(int64_t* __restrict__ p, int64_t n,
+                                        uint64_t seed, uint64_t stream,
+                                        int64_t lo, uint64_t range) {
+  int64_t stride = static_cast<int64_t>(gridDim.x) * blockDim.x;
+  for (int64_t i = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+       i < n; i += stride) {
+    p[i] = lo + static_cast<int64_t>(counter_bits(seed, stream, i) % range);
+  }
+}
+
+int init_grid(int64_t n) {
+  int64_t g = ceil_div(n, 256);
+  int64_t cap = static_cast<int64_t>(device_info().sm_count) * 16;
+  if (g > cap) g = cap;
+  return static_cast<int>(g < 1 ? 1 : g);
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* b200_last_error_string(void) { return g_last_error.c_str(); }
+
+int b200_device_caps(b200_caps* out) {
+  if (!out) return invalid("b200_device_caps: null output");
+  const DeviceInfo& d = device_info();
+  out->device = d.device;
+  out->sm_count = d.sm_count;
+  out->cc_major = d.cc_major;
+  out->cc_minor = d.cc_minor;
+  out->global_mem_bytes = static_cast<int64_t>(d.global_mem);
+  out->l2_bytes = d.l2_bytes;
+  out->max_smem_per_block_optin = d.max_smem_optin;
+  out->reserved = 0;
+  return B200_OK;
+}
+
+int64_t b200_launch_count(void) { return g_launches.load(); }
+
+int b200_init_reference(double* p, int64_t n, double factor,
+                        b200_stream_t stream) {
+  if (n < 0 || (n > 0 && !p)) return invalid("b200_init_reference: bad args");
+  if (n == 0) return B200_OK;
+  init_reference_kernel<<<init_grid(n), 256, 0, as_stream(stream)>>>(p, n,
+                                                                     factor);
+  return after_launch("b200_init_reference");
+}
+
+int b200_init_reference_signed(double* p, const int8_t* sign, int64_t n,
+                               double factor, b200_stream_t stream) {
+  if (n < 0 || (n > 0 && (!p || !sign)))
+    return invalid("b200_init_reference_signed: bad args");
+  if (n == 0) return B200_OK;
+  init_reference_signed_kernel<<<init_grid(n), 256, 0, as_stream(stream)>>>(
+      p, sign, n, factor);
+  return after_launch("b200_init_reference_signed");
+}
+
+int b200_init_const(double* p, int64_t n, double value,
+                    b200_stream_t stream) {
+  if (n < 0 || (n > 0 && !p)) return invalid("b200_init_const: bad args");
+  if (n == 0) return B200_OK;
+  init_const_kernel<double><<<init_grid(n), 256, 0, as_stream(stream)>>>(
+      p, n, value);
+  return after_launch("b200_init_const");
+}
+
+int b200_init_const_i64(int64_t* p, int64_t n, int64_t value,
+                        b200_stream_t stream) {
+  if (n < 0 || (n > 0 && !p)) return invalid("b200_init_const_i64: bad args");
+  if (n == 0) return B200_OK;
+  init_const_kernel<int64_t><<<init_grid(n), 256, 0, as_stream(stream)>>>(
+      p, n, value);
+  return after_launch("b200_init_const_i64");
+}
+
+int b200_init_uniform(double* p, int64_t n, uint64_t seed, uint64_t stream_id,
+                      double lo, double hi, b200_stream_t stream) {
+  if (n < 0 || (n > 0 && !p) || !(hi >= lo))
+    return invalid("b200_init_uniform: bad args");
+  if (n == 0) return B200_OK;
+  init_uniform_kernel<<<init_grid(n), 256, 0, as_stream(stream)>>>(
+      p, n, seed, stream_id, lo, hi - lo);
+  return after_launch("b200_init_uniform");
+}
+
+int b200_init_uniform_i64(int64_t* p, int64_t n, uint64_t seed,
+                          uint64_t stream_id, int64_t lo, int64_t hi,
+                          b200_stream_t stream) {
+  if (n < 0 || (n > 0 && !p) || hi <= lo)
+    return invalid("b200_init_uniform_i64: bad args");
+  if (n == 0) return B200_OK;
+  init_uniform_i64_kernel<<<init_grid(n), 256, 0, as_stream(stream)>>>(
+      p, n, seed, stream_id, lo, static_cast<uint64_t>(hi - lo));
+  return after_launch("b200_init_uniform_i64");
+}
+
+}  // extern "C"

@@ -1,0 +1,185 @@
+#include "KernelBase.hpp"
+
+#include "GraphRepRunner.hpp"
+#include "TuningTable.hpp"
+
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <stdexcept>
+
+namespace rajaperf {
+
+KernelBase::KernelBase(KernelID kid, const RunParams& params)
+    : run_params(params), checksum_scale_factor(1.0), kernel_id(kid),
+      name(getFullKernelName(kid)) {}
+
+KernelBase::~KernelBase() = default;
+
+// Same rule as the suite's KernelBase.cpp:115-125, plus the per-kernel size
+// map (a --size-map entry overrides --size/--sizefact for that kernel).
+Index_type KernelBase::getTargetProblemSize() const {
+  double per_kernel = run_params.getKernelSize(kernel_id);
+  if (per_kernel >= 0.0) return static_cast<Index_type>(per_kernel);
+  if (run_params.getSizeMeaning() == RunParams::Direct)
+    return static_cast<Index_type>(run_params.getSize());
+  return static_cast<Index_type>(default_prob_size * run_params.getSizeFactor());
+}
+
+// KernelBase.cpp:127-136.
+Index_type KernelBase::getRunReps() const {
+  if (run_params.getInputState() == RunParams::CheckRun)
+    return static_cast<Index_type>(run_params.getCheckRunReps());
+  return static_cast<Index_type>(default_reps * run_params.getRepFactor());
+}
+
+void KernelBase::setVariantDefined(VariantID vid) {
+  if (!isVariantAvailable(vid)) return;
+  setGB300TuningDefinitions(vid);
+  size_t nt = getNumVariantTunings(vid);
+  checksum[vid].assign(nt, 0.0L);
+  num_exec[vid].assign(nt, 0);
+  min_time[vid].assign(nt, std::numeric_limits<double>::max());
+  max_time[vid].assign(nt, -std::numeric_limits<double>::max());
+  tot_time[vid].assign(nt, 0.0);
+}
+
+void KernelBase::setGB300TuningDefinitions(VariantID vid) {
+  addVariantTuningName(vid, getDefaultTuningName());
+  addVariantTuningName(vid, "graph");
+  for (const NamedTune& nt : named_tunes) addVariantTuningName(vid, nt.name);
+}
+
+void KernelBase::addTuning(const std::string& tname, const b200_tune& t,
+                           bool graph) {
+  named_tunes.push_back(NamedTune{tname, t, graph});
+}
+
+size_t KernelBase::getVariantTuningIndex(VariantID vid,
+                                         const std::string& tname) const {
+  const auto& names = getVariantTuningNames(vid);
+  for (size_t t = 0; t < names.size(); ++t)
+    if (names[t] == tname) return t;
+  return getUnknownTuningIdx();
+}
+
+b200_tune KernelBase::getTune(size_t tune_idx) const {
+  b200_tune t{};
+  const std::string& tname = getVariantTuningName(Base_GB300, tune_idx);
+  for (const NamedTune& nt : named_tunes)
+    if (nt.name == tname) return nt.tune;
+  TuningTable::instance().lookup(name, actual_prob_size, &t);
+  return t;
+}
+
+bool KernelBase::isGraphTuning(size_t tune_idx) const {
+  const std::string& tname = getVariantTuningName(Base_GB300, tune_idx);
+  if (tname == "graph") return true;
+  for (const NamedTune& nt : named_tunes)
+    if (nt.name == tname) return nt.graph;
+  return false;
+}
+
+void KernelBase::synchronize() {
+  checkCuda(cudaDeviceSynchronize(), "cudaDeviceSynchronize");
+}
+
+void KernelBase::startTimer() {
+  synchronize();
+  timer_start = std::chrono::steady_clock::now();
+}
+
+void KernelBase::stopTimer() {
+  synchronize();
+  auto t1 = std::chrono::steady_clock::now();
+  timer_elapsed += std::chrono::duration<double>(t1 - timer_start).count();
+  recordExecTime();
+}
+
+void KernelBase::recordExecTime() {
+  num_exec[running_variant].at(running_tuning)++;
+  double t = timer_elapsed;
+  min_time[running_variant].at(running_tuning) =
+      std::min(min_time[running_variant].at(running_tuning), t);
+  max_time[running_variant].at(running_tuning) =
+      std::max(max_time[running_variant].at(running_tuning), t);
+  tot_time[running_variant].at(running_tuning) += t;
+}
+
+void KernelBase::execute(VariantID vid, size_t tune_idx) {
+  running_variant = vid;
+  running_tuning = tune_idx;
+  resetTimer();
+  detail::resetDataInitCount();
+  try {
+    setUp(vid, tune_idx);
+    runKernel(vid, tune_idx);
+    updateChecksum(vid, tune_idx);
+  } catch (...) {
+    try { tearDown(vid, tune_idx); } catch (...) {}
+    running_variant = NumVariants;
+    running_tuning = getUnknownTuningIdx();
+    throw;
+  }
+  tearDown(vid, tune_idx);
+  running_variant = NumVariants;
+  running_tuning = getUnknownTuningIdx();
+}
+
+void KernelBase::runKernel(VariantID vid, size_t tune_idx) {
+  if (!hasVariantDefined(vid)) return;
+  runGB300Variant(vid, tune_idx);
+}
+
+void KernelBase::runGB300Variant(VariantID, size_t tune_idx) {
+  prepareRun(tune_idx);
+  runReps(tune_idx, getRunReps(), makeRepBody(tune_idx));
+  finishRun(tune_idx);
+}
+
+void KernelBase::runReps(size_t tune_idx, Index_type reps,
+                         const std::function<void(b200_stream_t)>& rep_body) {
+  if (!isGraphTuning(tune_idx)) {
+    startTimer();
+    for (RepIndex_type irep = 0; irep < reps; ++irep) rep_body(getStream());
+    stopTimer();
+    return;
+  }
+  GraphRepRunner runner;
+  runner.capture(reps, rep_body);
+  startTimer();
+  runner.launch();
+  stopTimer();
+}
+
+void KernelBase::allocAndInitData(Real_ptr& ptr, Size_type len, VariantID vid) {
+  allocData(ptr, len, vid);
+  initDeviceData(run_params, ptr, len);
+}
+
+void KernelBase::allocAndInitDataConst(Real_ptr& ptr, Size_type len,
+                                       Real_type val, VariantID vid) {
+  allocData(ptr, len, vid);
+  initDeviceDataConst(ptr, len, val);
+}
+
+void KernelBase::allocAndInitDataConst(Index_type*& ptr, Size_type len,
+                                       Index_type val, VariantID vid) {
+  allocData(ptr, len, vid);
+  initDeviceDataConst(ptr, len, val);
+}
+
+void KernelBase::allocAndInitDataRandSign(Real_ptr& ptr, Size_type len,
+                                          VariantID vid) {
+  allocData(ptr, len, vid);
+  initDeviceDataRandSign(run_params, ptr, len);
+}
+
+void KernelBase::allocAndInitDataRandValue(Real_ptr& ptr, Size_type len,
+                                           VariantID vid) {
+  allocData(ptr, len, vid);
+  initDeviceDataRandValue(run_params, ptr, len);
+}
+
+}  // namespace rajaperf

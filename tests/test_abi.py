@@ -1,0 +1,33 @@
+"""The C-ABI libraries load and export every function their headers declare
+(no GPU needed: nothing is called)."""
+import ctypes
+
+import pytest
+
+import rajaperf_gb300 as rp
+
+
+def test_libb200_exports_header():
+    names = rp.declared_functions("b200.h")
+    assert "b200_stream_triad" in names
+    lib = rp.b200()
+    missing = [n for n in names if not hasattr(lib, n)]
+    assert not missing, missing
+
+
+def test_host_exports_header():
+    names = rp.declared_functions("rajaperf_gb300.h")
+    assert {"rp_run", "rp_last_error", "rp_graph_batch"} <= set(names)
+    lib = rp.host()
+    missing = [n for n in names if not hasattr(lib, n)]
+    assert not missing, missing
+
+
+def test_python_signatures_cover_header():
+    names = rp.declared_functions("b200.h")
+    assert set(names) <= set(rp.B200_SIGNATURES), set(names) - set(rp.B200_SIGNATURES)
+
+
+def test_tune_struct_layout():
+    assert ctypes.sizeof(rp.Tune) == 12 * 4
+    assert ctypes.sizeof(rp.RpResult) == 64 + 32 + 64 + 5 * 8 + 6 * 8 + 8
