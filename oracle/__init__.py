@@ -15,10 +15,13 @@ from __future__ import annotations
 import ctypes
 import json
 import os
+import platform
 import subprocess
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-LIB_PATH = os.path.join(HERE, "liboracle.so")
+# one library per host architecture, so a copy made on another machine is
+# never loaded by mistake
+LIB_PATH = os.path.join(HERE, f"liboracle.{platform.machine()}.so")
 REF_EXE = os.path.join(HERE, "_ref", "rajaperf_ref")
 REF_SRC_DEFAULT = "/root/reference"
 

@@ -62,7 +62,22 @@ def _run(cmd: list[str]) -> None:
         raise RuntimeError(f"build step failed: {os.path.basename(cmd[-1])}")
 
 
+def _check_arch_stamp() -> None:
+    """Objects and libraries from another host architecture are discarded."""
+    import platform
+    stamp = os.path.join(ROOT, "_build", "ARCH")
+    arch = platform.machine()
+    old = open(stamp).read().strip() if os.path.exists(stamp) else None
+    if old != arch:
+        for d in (OBJ, LIB, BIN):
+            shutil.rmtree(d, ignore_errors=True)
+        os.makedirs(os.path.dirname(stamp), exist_ok=True)
+        with open(stamp, "w") as f:
+            f.write(arch + "\n")
+
+
 def build(verbose: bool = False, jobs: int | None = None) -> dict:
+    _check_arch_stamp()
     home = cuda_home()
     nvcc = os.path.join(home, "bin", "nvcc")
     libdir = _cuda_libdir(home)
