@@ -56,9 +56,11 @@ def load_traffic() -> dict:
 # --------------------------------------------------------------------------
 
 class Case:
-    """One kernel of the workload: device buffers, one rep, bytes per rep."""
+    """One kernel of the workload: device buffers, one rep, and the suite's
+    Bytes/rep and FLOPs/rep for it."""
     name = ""
     launches = 1
+    flops_per_rep = 0
 
     def __init__(self, torch, rp, seed):
         self.torch = torch
@@ -197,8 +199,235 @@ def _stream_cases():
             "Stream_TRIAD": Triad, "Stream_DOT": Dot}
 
 
+def _ddv_mesh(np, rzmax, seed):
+    """ADomain(rzmax, 2) of apps/AppsData.hpp with jittered node positions
+    and the real-zone list (AppsData.cpp:56-151)."""
+    npnl, npnr = 2, 1
+    imin = jmin = npnl
+    imax = jmax = npnl + rzmax - 1
+    jp = imax + 1 - imin + npnl + npnr
+    nnalls = jp * (jmax + 1 - jmin + npnl + npnr)
+    ii, jj = np.meshgrid(np.arange(jp), np.arange(nnalls // jp))
+    rng = np.random.default_rng(seed)
+    x = (ii * 0.2 + 0.2 * rng.uniform(-0.1, 0.1, ii.shape)).ravel()
+    y = (jj * 0.1 + 0.1 * rng.uniform(-0.1, 0.1, jj.shape)).ravel()
+    zi, zj = np.meshgrid(np.arange(imin, imax), np.arange(jmin, jmax))
+    zones = (zi + zj * jp).ravel().astype(np.int64)
+    n_real_nodes = (imax + 1 - imin) * (jmax + 1 - jmin)
+    return x, y, zones, jp, nnalls, n_real_nodes
+
+
+def _bandwidth_cases():
+    import numpy as np
+
+    class Hydro2D(Case):
+        name = "Lcals_HYDRO_2D"
+        launches = 2
+
+        def __init__(self, torch, rp, seed, size):
+            super().__init__(torch, rp, seed)
+            self.jn = self.kn = int(math.sqrt(size) + math.sqrt(2) - 1)
+            n = self.kn * self.jn
+            self.arr = [self.uniform(n) for _ in range(11)]
+            kn, jn = self.kn, self.jn
+            self.bytes_per_rep = (8 * (4 * n + 4 * n + 4 * (kn - 2) * (jn - 2)) +
+                                  8 * 6 * (kn - 2) * (jn - 2))
+            self.flops_per_rep = 44 * (kn - 2) * (jn - 2)
+
+        def inputs(self):
+            return self.arr[2:9]
+
+        def outputs(self):
+            return [self.arr[6], self.arr[7], self.arr[9], self.arr[10]]
+
+        def run(self, s):
+            a = [t.data_ptr() for t in self.arr]
+            return self.L.b200_lcals_hydro_2d(*a, 0.0041, 0.0037, self.kn, self.jn, None, s)
+
+    class Eos(Case):
+        name = "Lcals_EOS"
+
+        def __init__(self, torch, rp, seed, n):
+            super().__init__(torch, rp, seed)
+            self.n = n
+            self.x = self.zeros(n + 7)
+            self.y, self.z, self.u = (self.uniform(n + 7) for _ in range(3))
+            self.bytes_per_rep = 16 * n + 8 * (n + 7) + 8 * n
+            self.flops_per_rep = 16 * n
+
+        def inputs(self):
+            return [self.y, self.z, self.u]
+
+        def outputs(self):
+            return [self.x]
+
+        def run(self, s):
+            return self.L.b200_lcals_eos(self.x.data_ptr(), self.y.data_ptr(), self.z.data_ptr(),
+                                         self.u.data_ptr(), 0.0979, 0.1958, 0.0979, self.n,
+                                         None, s)
+
+    class FirstDiff(Case):
+        name = "Lcals_FIRST_DIFF"
+
+        def __init__(self, torch, rp, seed, n):
+            super().__init__(torch, rp, seed)
+            self.n = n
+            self.x = self.zeros(n + 1)
+            self.y = self.uniform(n + 1)
+            self.bytes_per_rep = 8 * (n + 1) + 8 * n
+            self.flops_per_rep = n
+
+        def inputs(self):
+            return [self.y]
+
+        def outputs(self):
+            return [self.x]
+
+        def run(self, s):
+            return self.L.b200_lcals_first_diff(self.x.data_ptr(), self.y.data_ptr(), self.n,
+                                                None, s)
+
+    class FirstMin(Case):
+        name = "Lcals_FIRST_MIN"
+
+        def __init__(self, torch, rp, seed, n):
+            super().__init__(torch, rp, seed)
+            self.n = n
+            self.x = self.uniform(n)
+            planted = int(np.random.default_rng(seed).integers(0, n))
+            self.x[planted] = -0.5
+            self.loc = self.zeros(1, dtype=torch.int64)
+            self.ws_bytes = self.L.b200_reduce_workspace_bytes(n, None)
+            self.ws = self.zeros(self.ws_bytes, dtype=torch.uint8)
+            self.bytes_per_rep = 8 + 8 + 8 * n + 8 + 8
+            self.flops_per_rep = 0
+
+        def inputs(self):
+            return [self.x]
+
+        def outputs(self):
+            return [self.loc]
+
+        def run(self, s):
+            return self.L.b200_lcals_first_min(self.x.data_ptr(), self.n, 0.5, 0,
+                                               self.loc.data_ptr(), None, self.ws.data_ptr(),
+                                               self.ws_bytes, None, s)
+
+    class DelDotVec2D(Case):
+        name = "Apps_DEL_DOT_VEC_2D"
+
+        def __init__(self, torch, rp, seed, size):
+            super().__init__(torch, rp, seed)
+            rzmax = int(math.sqrt(size) + 1 + math.sqrt(2) - 1)
+            x, y, zones, self.jp, nn, n_real_nodes = _ddv_mesh(np, rzmax, seed)
+            self.x = torch.from_numpy(x).cuda()
+            self.y = torch.from_numpy(y).cuda()
+            self.zones = torch.from_numpy(zones).cuda()
+            self.nz = zones.size
+            self.xdot, self.ydot = self.uniform(nn), self.uniform(nn)
+            self.div = self.zeros(nn)
+            self.bytes_per_rep = 8 * self.nz + 4 * 8 * n_real_nodes + 8 * self.nz
+            self.flops_per_rep = 54 * self.nz
+
+        def inputs(self):
+            return [self.x, self.y, self.xdot, self.ydot, self.zones]
+
+        def outputs(self):
+            return [self.div]
+
+        def run(self, s):
+            return self.L.b200_apps_del_dot_vec_2d(
+                self.x.data_ptr(), self.y.data_ptr(), self.xdot.data_ptr(),
+                self.ydot.data_ptr(), self.div.data_ptr(), self.zones.data_ptr(), self.nz,
+                self.jp, 1e-20, 0.5, None, s)
+
+    class Jacobi2D(Case):
+        name = "Polybench_JACOBI_2D"
+
+        def __init__(self, torch, rp, seed, size, tsteps=50):
+            super().__init__(torch, rp, seed)
+            N = self.N = int(math.sqrt(size) + 2 + math.sqrt(2) - 1)
+            self.tsteps = tsteps
+            self.launches = 2 * tsteps
+            self.A, self.B = self.uniform(N * N), self.uniform(N * N)
+            self.bytes_per_rep = (8 * (N * N - 4) * 2 + 8 * (N - 2) * (N - 2) * 2) * tsteps
+            self.flops_per_rep = tsteps * 10 * (N - 2) * (N - 2)
+
+        def inputs(self):
+            return [self.A, self.B]
+
+        def outputs(self):
+            return [self.A, self.B]
+
+        def run(self, s):
+            return self.L.b200_polybench_jacobi_2d(self.A.data_ptr(), self.B.data_ptr(), self.N,
+                                                   self.tsteps, None, s)
+
+    class Heat3D(Case):
+        name = "Polybench_HEAT_3D"
+
+        def __init__(self, torch, rp, seed, size, tsteps=20):
+            super().__init__(torch, rp, seed)
+            N = self.N = int(round(size ** (1.0 / 3.0)) + 2 + 3 ** (1.0 / 3.0) - 1)
+            self.tsteps = tsteps
+            self.launches = 2 * tsteps
+            self.A, self.B = self.uniform(N ** 3), self.uniform(N ** 3)
+            inner = (N - 2) ** 3
+            self.bytes_per_rep = (8 * (N ** 3 - 12 * (N - 2) - 8) * 2 + 8 * inner * 2) * tsteps
+            self.flops_per_rep = tsteps * 30 * inner
+
+        def inputs(self):
+            return [self.A, self.B]
+
+        def outputs(self):
+            return [self.A, self.B]
+
+        def run(self, s):
+            return self.L.b200_polybench_heat_3d(self.A.data_ptr(), self.B.data_ptr(), self.N,
+                                                 self.tsteps, None, s)
+
+    class ScanI64(Case):
+        name = "Algorithm_SCAN"
+
+        def __init__(self, torch, rp, seed, n):
+            super().__init__(torch, rp, seed)
+            self.n = n
+            self.x = torch.empty(n, dtype=torch.int64, device="cuda")
+            rp.check(self.L.b200_init_uniform_i64(self.x.data_ptr(), n, seed, 0, 0, 100, None))
+            self.y = self.zeros(n, dtype=torch.int64)
+            self.ws_bytes = self.L.b200_scan_workspace_bytes(n)
+            self.ws = self.zeros(self.ws_bytes, dtype=torch.uint8)
+            self.bytes_per_rep = 16 * n
+            self.flops_per_rep = n
+
+        def inputs(self):
+            return [self.x]
+
+        def outputs(self):
+            return [self.y]
+
+        def run(self, s):
+            return self.L.b200_algorithm_scan_i64(self.x.data_ptr(), self.y.data_ptr(), self.n,
+                                                  0, self.ws.data_ptr(), self.ws_bytes, None, s)
+
+    return {"Lcals_HYDRO_2D": Hydro2D, "Lcals_EOS": Eos, "Lcals_FIRST_DIFF": FirstDiff,
+            "Lcals_FIRST_MIN": FirstMin, "Apps_DEL_DOT_VEC_2D": DelDotVec2D,
+            "Polybench_JACOBI_2D": Jacobi2D, "Polybench_HEAT_3D": Heat3D,
+            "Algorithm_SCAN": ScanI64}
+
+
 # workload -> list of (kernel, size, oracle kwargs for the CPU baseline)
 WORKLOADS = {
+    "bandwidth_stencil": {
+        "description": "FP64, uniform [0.5,1.5) from a seed: HYDRO_2D 4096x4096; EOS, "
+                       "FIRST_DIFF, FIRST_MIN (planted minimum) N=2^24; DEL_DOT_VEC_2D "
+                       "4096x4096 mesh jittered by up to 0.1 cell; JACOBI_2D N=4096, 50 "
+                       "tsteps; HEAT_3D 256^3, 20 tsteps; SCAN int64 in [0,100), N=2^26",
+        "kernels": [("Lcals_HYDRO_2D", 4096 * 4096), ("Lcals_EOS", 1 << 24),
+                    ("Lcals_FIRST_DIFF", 1 << 24), ("Lcals_FIRST_MIN", 1 << 24),
+                    ("Apps_DEL_DOT_VEC_2D", 4096 * 4096), ("Polybench_JACOBI_2D", 4094 * 4094),
+                    ("Polybench_HEAT_3D", 254 ** 3), ("Algorithm_SCAN", 1 << 26)],
+    },
     "stream": {
         "description": "Stream COPY/MUL/ADD/TRIAD/DOT, FP64, N=2^27 per array",
         "kernels": [("Stream_COPY", 1 << 27), ("Stream_MUL", 1 << 27),
@@ -206,17 +435,21 @@ WORKLOADS = {
                     ("Stream_DOT", 1 << 27)],
     },
 }
-DEFAULT_WORKLOAD = "stream"
+DEFAULT_WORKLOAD = "bandwidth_stencil"
 
 
-def build_cases(torch, rp, workload, seed):
+def workload_kernels(workload, only=None):
+    ks = WORKLOADS[workload]["kernels"]
+    if only:
+        ks = [(k, n) for k, n in ks if k in only or k.split("_", 1)[1] in only]
+    return ks
+
+
+def build_cases(torch, rp, workload, seed, only=None):
     registry = {}
     registry.update(_stream_cases())
-    cases = []
-    for kname, size in WORKLOADS[workload]["kernels"]:
-        if kname in registry:
-            cases.append(registry[kname](torch, rp, seed, size))
-    return cases
+    registry.update(_bandwidth_cases())
+    return [registry[k](torch, rp, seed, n) for k, n in workload_kernels(workload, only)]
 
 
 # --------------------------------------------------------------------------
@@ -239,7 +472,7 @@ class ClockSampler:
         try:
             self.proc = subprocess.Popen(
                 ["nvidia-smi", "-i", str(self.dev), f"--query-gpu={self.QUERY}",
-                 "--format=csv,noheader,nounits", "-lms", "200"],
+                 "--format=csv,noheader,nounits", "-lms", "100"],
                 stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
         except (OSError, FileNotFoundError):
             self.proc = None
@@ -302,10 +535,11 @@ def run_gpu(args, rank, world):
         dist.init_process_group("nccl")
     peaks = load_peaks()
     traffic = load_traffic()
-    cases = build_cases(torch, rp, args.workload, args.seed + rank)
+    cases = build_cases(torch, rp, args.workload, args.seed + rank, args.kernels)
     stream = torch.cuda.current_stream()
     s = stream.cuda_stream
     flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device="cuda")
+    fp64 = measure_fp64_peak(torch, rp, stream)
 
     def one_step(timed_events=None):
         for i, c in enumerate(cases):
@@ -342,8 +576,11 @@ def run_gpu(args, rank, world):
         ms = [ev[k][i][0].elapsed_time(ev[k][i][1]) for k in range(args.steps)]
         avg_s = sum(ms) / len(ms) / 1e3
         gbs = c.bytes_per_rep / avg_s / 1e9
+        gfs = c.flops_per_rep / avg_s / 1e9
         per_kernel.append({"kernel": c.name, "ms": avg_s * 1e3, "gbs": gbs,
-                           "frac": gbs / peaks["hbm_gbs"], "bytes": c.bytes_per_rep})
+                           "frac": gbs / peaks["hbm_gbs"], "bytes": c.bytes_per_rep,
+                           "gflops": gfs, "fp64_frac": gfs / fp64["gflops"],
+                           "launches": c.launches})
     step_s = sum(p["ms"] for p in per_kernel) / 1e3
     if dist:
         t = torch.tensor([step_s], device="cuda")
@@ -352,20 +589,45 @@ def run_gpu(args, rank, world):
     value = 100.0 * geomean([p["frac"] for p in per_kernel])
 
     # e2e through the C ABI with host buffers
-    e2e = run_e2e(torch, rp, cases, s, stream, args, peaks)
+    e2e = None if args.no_e2e else run_e2e(torch, rp, cases, s, stream, args, peaks)
 
     dom = max(per_kernel, key=lambda p: p["ms"])
     tr = traffic.get(dom["kernel"])
     roofline = {"bound": "hbm", "kernel": dom["kernel"], "achieved": round(dom["gbs"], 1),
                 "peak": peaks["hbm_gbs"], "unit": "GB/s",
                 "frac": round(dom["gbs"] / peaks["hbm_gbs"], 4),
-                "traffic": (tr["bytes_per_launch"] if tr else None),
-                "algorithmic_bytes": dom["bytes"], "peak_source": peaks["source"]}
+                "traffic": (tr["bytes_per_rep"] if tr else None),
+                "algorithmic_bytes": dom["bytes"],
+                "peak_source": f"{peaks['source']} (MEASURED_PEAKS.json copy peak)"
+                               if peaks["source"] == "measured" else "fallback",
+                "fp64": {"achieved_gflops": round(dom["gflops"], 1),
+                         "peak_gflops": round(fp64["gflops"], 1),
+                         "frac": round(dom["fp64_frac"], 4),
+                         "peak_source": "measured in this run (b200_probe_dfma, FMA = 2 flops)"}}
     return {
         "value": value, "step_s": step_s, "per_kernel": per_kernel, "e2e": e2e,
         "roofline": roofline, "clocks": clocks, "launches": launches, "wall_s": wall,
-        "world": world, "dist": dist,
+        "world": world, "dist": dist, "fp64": fp64,
     }
+
+
+def measure_fp64_peak(torch, rp, stream):
+    """FP64 FMA rate of this GPU from the library's probe (best of 3)."""
+    L = rp.b200()
+    out = torch.empty(int(L.b200_probe_dfma_threads()), dtype=torch.float64, device="cuda")
+    import ctypes
+    cnt = ctypes.c_int64(0)
+    best = 0.0
+    for _ in range(4):
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        rp.check(L.b200_probe_dfma(out.data_ptr(), 2048, ctypes.byref(cnt), stream.cuda_stream))
+        e1.record(stream)
+        torch.cuda.synchronize()
+        rate = cnt.value / (e0.elapsed_time(e1) / 1e3)
+        best = max(best, rate)
+    return {"fma_per_s": best, "gflops": 2.0 * best / 1e9}
 
 
 def run_e2e(torch, rp, cases, s, stream, args, peaks):
@@ -410,13 +672,13 @@ def cpu_cores() -> int:
         return os.cpu_count() or 1
 
 
-def run_cpu(workload, seed, threads, peaks):
+def run_cpu(workload, seed, threads, peaks, only=None):
     """The suite's Base_OpenMP loops (oracle restatement), one rep per kernel
     at the workload's full size; returns the metric and per-kernel times."""
     import oracle
     oracle.build()
     fr, per = [], []
-    for kname, size in WORKLOADS[workload]["kernels"]:
+    for kname, size in workload_kernels(workload, only):
         kw = dict(WORKLOAD_ORACLE_ARGS.get(kname, {}))
         r = oracle.run(kname, size=size, reps=1, init="uniform", seed=seed,
                        threads=threads, skip_checksum=True, **kw)
@@ -426,18 +688,25 @@ def run_cpu(workload, seed, threads, peaks):
     return 100.0 * geomean(fr), per
 
 
-WORKLOAD_ORACLE_ARGS = {}
+# oracle arguments of the CPU baseline per kernel (time steps, int64 scan)
+WORKLOAD_ORACLE_ARGS = {"Polybench_JACOBI_2D": {"tsteps": 50},
+                        "Polybench_HEAT_3D": {"tsteps": 20},
+                        "Algorithm_SCAN": {"variant": 1}}
 
 
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--workload", default=DEFAULT_WORKLOAD, choices=sorted(WORKLOADS))
     ap.add_argument("--seed", type=int, default=4793)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true",
+                    help="skip the host-buffer end-to-end leg")
+    ap.add_argument("--kernels", type=lambda s: s.split(","), default=None,
+                    help="comma list: run only these kernels of the workload")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3) if args.impl == "gb300" else args.warmup
     rank = int(os.environ.get("RANK", "0"))
@@ -445,7 +714,7 @@ def main():
     peaks = load_peaks()
     desc = WORKLOADS[args.workload]["description"]
     config = {"workload": args.workload, "description": desc,
-              "kernels": [k for k, _ in WORKLOADS[args.workload]["kernels"]],
+              "kernels": [k for k, _ in workload_kernels(args.workload, args.kernels)],
               "l2": "flushed (256 MiB write) before every kernel",
               "init": f"uniform [0.5,1.5) seed {args.seed}"}
     metric = "geomean % of measured HBM copy peak over kernels (suite Bytes/rep)"
@@ -457,7 +726,7 @@ def main():
         vals, per = [], []
         t0 = time.perf_counter()
         for _ in range(max(1, args.steps)):
-            v, per = run_cpu(args.workload, args.seed, cores, peaks)
+            v, per = run_cpu(args.workload, args.seed, cores, peaks, args.kernels)
             vals.append(v)
         wall = time.perf_counter() - t0
         v = sum(vals) / len(vals)
@@ -491,7 +760,7 @@ def main():
     cpu = None
     if not args.no_cpu_baseline and world == 1:
         cores = cpu_cores()
-        cv, per = run_cpu(args.workload, args.seed, cores, peaks)
+        cv, per = run_cpu(args.workload, args.seed, cores, peaks, args.kernels)
         cpu = {"value": round(cv, 4), "unit": "%", "cores": cores, "kind": "port",
                "sample": "suite Base_OpenMP loops (C restatement), one rep per kernel at "
                          "the workload's full size", "per_kernel": per}
@@ -502,6 +771,7 @@ def main():
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
         "config": config, "e2e": res["e2e"], "roofline": res["roofline"],
         "cpu_baseline": cpu, "clocks": res["clocks"], "gpu_launches": res["launches"],
+        "fp64_peak_gflops": round(res["fp64"]["gflops"], 1),
         "per_kernel": [{k: (round(v, 4) if isinstance(v, float) else v) for k, v in p.items()}
                        for p in res["per_kernel"]],
     }

@@ -86,6 +86,15 @@ int b200_device_caps(b200_caps* out);
 /* Number of kernels this library has launched since it was loaded. */
 int64_t b200_launch_count(void);
 
+/* FP64 pipe probe: launches 8 independent fma chains of `iters` steps in
+ * each of b200_probe_dfma_threads() threads (out must hold that many
+ * doubles) and reports the number of fused multiply-adds issued.  Timing the
+ * launch gives the device's FP64 FMA rate, the roofline of the FP64-bound
+ * kernels.  Not in the reference. */
+int64_t b200_probe_dfma_threads(void);
+int b200_probe_dfma(double* out, int32_t iters, int64_t* fma_count,
+                    b200_stream_t stream);
+
 /* ---- data initialisation (DataUtils.cpp) -------------------------------- */
 
 /* p[i] = factor*(i + 1.1)/(i + 1.12345)  -- common/DataUtils.cpp:504-513. */
@@ -144,6 +153,175 @@ int b200_stream_dot(const double* a, const double* b, int64_t n,
                     double dot_init, double* dot_accum, void* workspace,
                     size_t workspace_bytes, const b200_tune* tune,
                     b200_stream_t stream);
+
+/* ---- Basic (kernels of the batched small-size suite) --------------------- */
+
+/* y[i] += a*x[i]                   -- basic/DAXPY.hpp, DAXPY-Cuda.cpp        */
+int b200_basic_daxpy(double* y, const double* x, double a, int64_t n,
+                     const b200_tune* tune, b200_stream_t stream);
+
+/* out1 = out2 = out3 = -in1 - in2  -- basic/INIT3.hpp, INIT3-Cuda.cpp        */
+int b200_basic_init3(double* out1, double* out2, double* out3, const double* in1,
+                     const double* in2, int64_t n, const b200_tune* tune,
+                     b200_stream_t stream);
+
+/* out1 = in1*in2, out2 = in1+in2, out3 = in1-in2 -- basic/MULADDSUB.hpp      */
+int b200_basic_muladdsub(double* out1, double* out2, double* out3,
+                         const double* in1, const double* in2, int64_t n,
+                         const b200_tune* tune, b200_stream_t stream);
+
+/* ---- LCALS -------------------------------------------------------------- */
+
+/* x[i] = q + y[i]*(r*z[i+10] + t*z[i+11]); z holds >= n+11 values
+ *   -- lcals/HYDRO_1D.hpp:30, HYDRO_1D-Cuda.cpp:26                          */
+int b200_lcals_hydro_1d(double* x, const double* y, const double* z, double q,
+                        double r, double t, int64_t n, const b200_tune* tune,
+                        b200_stream_t stream);
+
+/* One rep of HYDRO_2D on a kn x jn row-major grid (index j + k*jn): BODY1
+ * (za, zb) then BODY2 (zu, zv +=) and BODY3 (zrout, zzout) over the interior
+ *   -- lcals/HYDRO_2D.hpp:66-90, HYDRO_2D-Cuda.cpp:104-140.  Two launches.   */
+int b200_lcals_hydro_2d(double* za, double* zb, const double* zm,
+                        const double* zp, const double* zq, const double* zr,
+                        double* zu, double* zv, const double* zz, double* zrout,
+                        double* zzout, double s, double t, int64_t kn,
+                        int64_t jn, const b200_tune* tune, b200_stream_t stream);
+
+/* x[i] = EOS polynomial; y, z, u hold >= n+7 values
+ *   -- lcals/EOS.hpp:33, EOS-Cuda.cpp:26                                    */
+int b200_lcals_eos(double* x, const double* y, const double* z, const double* u,
+                   double q, double r, double t, int64_t n,
+                   const b200_tune* tune, b200_stream_t stream);
+
+/* x[i] = y[i+1] - y[i]             -- lcals/FIRST_DIFF.hpp:25                */
+int b200_lcals_first_diff(double* x, const double* y, int64_t n,
+                          const b200_tune* tune, b200_stream_t stream);
+
+/* px[i] = 9-term predictor over planes px[i + k*n], k = 2..12 (px has 13n)
+ *   -- lcals/INT_PREDICT.hpp:40, INT_PREDICT-Cuda.cpp:26                    */
+int b200_lcals_int_predict(double* px, double dm22, double dm23, double dm24,
+                           double dm25, double dm26, double dm27, double dm28,
+                           double c0, int64_t n, const b200_tune* tune,
+                           b200_stream_t stream);
+
+/* First-index minimum: *minloc = smallest i with x[i] minimal (strict '<'
+ * scan seeded with (xmin_init, initloc)); *minval (optional) = the minimum.
+ * Workspace from b200_reduce_workspace_bytes.  One launch; exact.
+ *   -- lcals/FIRST_MIN.hpp:29-54, FIRST_MIN-Seq.cpp:34-48                   */
+int b200_lcals_first_min(const double* x, int64_t n, double xmin_init,
+                         int64_t initloc, int64_t* minloc, double* minval,
+                         void* workspace, size_t workspace_bytes,
+                         const b200_tune* tune, b200_stream_t stream);
+
+/* Divided-difference predictor over planes px[i + k*n], k = 4..13 (px has
+ * 14n), in place   -- lcals/DIFF_PREDICT.hpp                               */
+int b200_lcals_diff_predict(double* px, const double* cx, int64_t n,
+                            const b200_tune* tune, b200_stream_t stream);
+
+/* y[i] = u[i]/v[i]; w[i] = x[i]/(exp(y[i]) - 1)  -- lcals/PLANCKIAN.hpp     */
+int b200_lcals_planckian(const double* x, double* y, const double* u,
+                         const double* v, double* w, int64_t n,
+                         const b200_tune* tune, b200_stream_t stream);
+
+/* ---- Apps --------------------------------------------------------------- */
+
+/* BODY1 and BODY2 of PRESSURE fused per element
+ *   -- apps/PRESSURE.hpp:39-46, PRESSURE-Cuda.cpp:26,38                     */
+int b200_apps_pressure(const double* compression, double* bvc, double* p_new,
+                       const double* e_old, const double* vnewc, double cls,
+                       double p_cut, double pmin, double eosvmax, int64_t n,
+                       const b200_tune* tune, b200_stream_t stream);
+
+/* BODY1..BODY6 of ENERGY fused per element
+ *   -- apps/ENERGY.hpp:111-178, ENERGY-Cuda.cpp:26-182                      */
+int b200_apps_energy(double* e_new, const double* e_old, const double* delvc,
+                     const double* p_new, const double* p_old, double* q_new,
+                     const double* q_old, const double* work,
+                     const double* compHalfStep, const double* pHalfStep,
+                     const double* bvc, const double* pbvc, const double* ql_old,
+                     const double* qq_old, const double* vnewc, double rho0,
+                     double e_cut, double emin, double q_cut, int64_t n,
+                     const b200_tune* tune, b200_stream_t stream);
+
+/* Hexahedron volumes for i in [ibegin, iend) from the 8 corners i + {0, 1,
+ * jp, 1+jp, kp, 1+kp, jp+kp, 1+jp+kp}  -- apps/VOL3D.hpp:88-146,
+ * VOL3D-Cuda.cpp:26-75                                                      */
+int b200_apps_vol3d(const double* x, const double* y, const double* z,
+                    double* vol, double vnormq, int64_t jp, int64_t kp,
+                    int64_t ibegin, int64_t iend, const b200_tune* tune,
+                    b200_stream_t stream);
+
+/* Nodal divergence for each real zone i = real_zones[ii], corners i, i+1,
+ * i+1+jp, i+jp  -- apps/DEL_DOT_VEC_2D.hpp:65-90, DEL_DOT_VEC_2D-Cuda.cpp:30-60 */
+int b200_apps_del_dot_vec_2d(const double* x, const double* y,
+                             const double* xdot, const double* ydot,
+                             double* div, const int64_t* real_zones,
+                             int64_t n_real_zones, int64_t jp, double ptiny,
+                             double half, const b200_tune* tune,
+                             b200_stream_t stream);
+
+/* ---- Polybench ---------------------------------------------------------- */
+
+/* tsteps x (B <- 5-point average of A, then A <- of B) on an N x N grid
+ *   -- polybench/POLYBENCH_JACOBI_2D.hpp:38-44, -Cuda.cpp:86-114            */
+int b200_polybench_jacobi_2d(double* A, double* B, int64_t N, int64_t tsteps,
+                             const b200_tune* tune, b200_stream_t stream);
+
+/* tsteps x (B <- 7-point heat update of A, then A <- of B) on N^3
+ *   -- polybench/POLYBENCH_HEAT_3D.hpp:47-82, -Cuda.cpp:97-113              */
+int b200_polybench_heat_3d(double* A, double* B, int64_t N, int64_t tsteps,
+                           const b200_tune* tune, b200_stream_t stream);
+
+/* tsteps of the 2-D FDTD update on nx x ny (fict holds tsteps values)
+ *   -- polybench/POLYBENCH_FDTD_2D.hpp:52-69, -Cuda.cpp:164-190             */
+int b200_polybench_fdtd_2d(double* ex, double* ey, double* hz,
+                           const double* fict, int64_t nx, int64_t ny,
+                           int64_t tsteps, const b200_tune* tune,
+                           b200_stream_t stream);
+
+/* C[i][j] = sum_k (alpha*A[i][k]) * B[k][j], row-major, FP64 (the suite's
+ * GEMM: its beta scaling is overwritten by BODY4)
+ *   -- polybench/POLYBENCH_GEMM.hpp:40-56, -Cuda.cpp:27-59                  */
+int b200_polybench_gemm(const double* A, const double* B, double* C, int64_t ni,
+                        int64_t nj, int64_t nk, double alpha,
+                        const b200_tune* tune, b200_stream_t stream);
+
+/* E = A*B, F = C*D, G = E*F (FP64)
+ *   -- polybench/POLYBENCH_3MM.hpp:61-86, -Cuda.cpp:144-160                 */
+int b200_polybench_3mm(const double* A, const double* B, const double* C,
+                       const double* D, double* E, double* F, double* G,
+                       int64_t ni, int64_t nj, int64_t nk, int64_t nl,
+                       int64_t nm, const b200_tune* tune, b200_stream_t stream);
+
+/* C = alpha*A*B + beta*C, row-major m x k times k x n, native FP64 (the
+ * classic GEMM form the split-precision path is measured against).        */
+int b200_gemm_f64(const double* A, const double* B, double* C, int64_t m,
+                  int64_t n, int64_t k, double alpha, double beta,
+                  const b200_tune* tune, b200_stream_t stream);
+
+/* ---- Algorithm ---------------------------------------------------------- */
+
+/* Workspace for b200_algorithm_scan / _scan_i64 on n elements. */
+size_t b200_scan_workspace_bytes(int64_t n);
+
+/* y[i] = init + sum_{j<i} x[j] (exclusive), single-pass decoupled lookback
+ *   -- algorithm/SCAN.hpp:23-36, SCAN-Cuda.cpp:143-300.  One launch.        */
+int b200_algorithm_scan(const double* x, double* y, int64_t n, double init,
+                        void* workspace, size_t workspace_bytes,
+                        const b200_tune* tune, b200_stream_t stream);
+
+/* The same over int64 values: exact. */
+int b200_algorithm_scan_i64(const int64_t* x, int64_t* y, int64_t n,
+                            int64_t init, void* workspace,
+                            size_t workspace_bytes, const b200_tune* tune,
+                            b200_stream_t stream);
+
+/* *sum = sum_init + sum_i x[i], fixed-shape tree (deterministic)
+ *   -- algorithm/REDUCE_SUM.hpp:25-32, REDUCE_SUM-Seq.cpp:34-48             */
+int b200_algorithm_reduce_sum(const double* x, int64_t n, double sum_init,
+                              double* sum, void* workspace,
+                              size_t workspace_bytes, const b200_tune* tune,
+                              b200_stream_t stream);
 
 #ifdef __cplusplus
 }

@@ -86,6 +86,22 @@ def lib() -> ctypes.CDLL:
         L.oracle_uniform_value.restype = ctypes.c_double
         L.oracle_first_min_planted_index.argtypes = [ctypes.c_uint64, ctypes.c_int64]
         L.oracle_first_min_planted_index.restype = ctypes.c_int64
+        P, I, D = ctypes.c_void_p, ctypes.c_int64, ctypes.c_double
+        for name, args in {
+            "oracle_hydro_2d_rep": [P] * 11 + [D, D, I, I],
+            "oracle_del_dot_vec_2d_rep": [P] * 6 + [I, I, D, D],
+            "oracle_vol3d_rep": [P] * 4 + [D, I, I, I, I],
+            "oracle_energy_rep": [P] * 15 + [D, D, D, D, I],
+            "oracle_jacobi_2d": [P, P, I, I],
+            "oracle_heat_3d": [P, P, I, I],
+            "oracle_fdtd_2d": [P, P, P, P, I, I, I],
+            "oracle_scan_f64": [P, P, I],
+            "oracle_scan_i64": [P, P, I],
+            "oracle_gemm": [P, P, P, I, I, I, D, D],
+        }.items():
+            fn = getattr(L, name)
+            fn.argtypes = args
+            fn.restype = None
         _lib = L
     return _lib
 
@@ -125,3 +141,15 @@ def run_ref(kernel: str, size: int, reps: int) -> dict:
                          capture_output=True, text=True).stdout
     line = [ln for ln in out.splitlines() if ln.startswith("{")][-1]
     return json.loads(line)
+
+
+def call(name: str, *args) -> None:
+    """Calls an oracle building block; numpy arrays are passed by address
+    (they must be contiguous and of the declared element type)."""
+    conv = []
+    for a in args:
+        if hasattr(a, "ctypes"):
+            conv.append(a.ctypes.data)
+        else:
+            conv.append(a)
+    getattr(lib(), name)(*conv)

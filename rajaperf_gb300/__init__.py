@@ -65,32 +65,50 @@ class RpBatchResult(ctypes.Structure):
                 ("launch_time_s", ctypes.c_double), ("graph_time_s", ctypes.c_double)]
 
 
-_P = ctypes.c_void_p
-_I64 = ctypes.c_int64
-_D = ctypes.c_double
-_TP = ctypes.POINTER(Tune)
-
-# argtypes of every libb200 entry point, keyed by name.  Pointers are passed
-# as integers (device addresses), scalars by value.
-B200_SIGNATURES = {
-    "b200_last_error_string": ([], ctypes.c_char_p),
-    "b200_device_caps": ([ctypes.POINTER(Caps)], ctypes.c_int),
-    "b200_launch_count": ([], ctypes.c_int64),
-    "b200_init_reference": ([_P, _I64, _D, _P], ctypes.c_int),
-    "b200_init_reference_signed": ([_P, _P, _I64, _D, _P], ctypes.c_int),
-    "b200_init_const": ([_P, _I64, _D, _P], ctypes.c_int),
-    "b200_init_const_i64": ([_P, _I64, _I64, _P], ctypes.c_int),
-    "b200_init_uniform": ([_P, _I64, ctypes.c_uint64, ctypes.c_uint64, _D, _D, _P],
-                          ctypes.c_int),
-    "b200_init_uniform_i64": ([_P, _I64, ctypes.c_uint64, ctypes.c_uint64, _I64, _I64, _P],
-                              ctypes.c_int),
-    "b200_stream_copy": ([_P, _P, _I64, _TP, _P], ctypes.c_int),
-    "b200_stream_mul": ([_P, _P, _D, _I64, _TP, _P], ctypes.c_int),
-    "b200_stream_add": ([_P, _P, _P, _I64, _TP, _P], ctypes.c_int),
-    "b200_stream_triad": ([_P, _P, _P, _D, _I64, _TP, _P], ctypes.c_int),
-    "b200_reduce_workspace_bytes": ([_I64, _TP], ctypes.c_size_t),
-    "b200_stream_dot": ([_P, _P, _I64, _D, _P, _P, ctypes.c_size_t, _TP, _P], ctypes.c_int),
+_C_TYPES = {
+    "double": ctypes.c_double, "int64_t": ctypes.c_int64, "uint64_t": ctypes.c_uint64,
+    "size_t": ctypes.c_size_t, "int": ctypes.c_int, "int32_t": ctypes.c_int32,
+    "b200_stream_t": ctypes.c_void_p, "void": None,
 }
+
+
+def _ctype(decl: str):
+    """ctypes type of one C parameter/return declaration from b200.h."""
+    d = decl.replace("const ", "").strip()
+    if d.startswith("char*") or d == "char *":
+        return ctypes.c_char_p
+    if "b200_tune*" in d.replace(" ", ""):
+        return ctypes.POINTER(Tune)
+    if "b200_caps*" in d.replace(" ", ""):
+        return ctypes.POINTER(Caps)
+    if "*" in d:
+        return ctypes.c_void_p  # device or host address passed as an integer
+    base = d.split()[0]
+    if base not in _C_TYPES:
+        raise ValueError(f"unmapped C type in b200.h: {decl!r}")
+    return _C_TYPES[base]
+
+
+def parse_signatures(header: str = "b200.h") -> dict:
+    """{name: (argtypes, restype)} for every function declared in a header."""
+    text = open(os.path.join(INCLUDE, header)).read()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    sigs = {}
+    for m in re.finditer(r"([A-Za-z_][\w\s\*]*?)\b((?:b200|rp)_\w+)\s*\(([^;{]*?)\)\s*;",
+                         text, flags=re.S):
+        ret, name, params = m.group(1).strip(), m.group(2), m.group(3).strip()
+        ret = ret.replace("const char*", "char*").replace("const char *", "char*")
+        restype = ctypes.c_char_p if ret.endswith("char*") else _ctype(ret)
+        args = []
+        if params and params != "void":
+            for prm in params.split(","):
+                prm = " ".join(prm.split())
+                # drop the parameter name
+                tname = re.sub(r"\b\w+$", "", prm).strip() if not prm.endswith("*") else prm
+                args.append(_ctype(tname))
+        sigs[name] = (args, restype)
+    return sigs
+
 
 _b200 = None
 _host = None
@@ -110,10 +128,10 @@ def b200() -> ctypes.CDLL:
     if _b200 is None:
         _require(LIBB200)
         lib = ctypes.CDLL(LIBB200)
-        for name, (args, res) in B200_SIGNATURES.items():
+        for name, (args, res) in parse_signatures("b200.h").items():
             fn = getattr(lib, name, None)
             if fn is None:
-                continue
+                raise RuntimeError(f"{LIBB200} does not export {name} (declared in b200.h)")
             fn.argtypes = args
             fn.restype = res
         _b200 = lib

@@ -1,0 +1,306 @@
+// Algorithm group: SCAN (exclusive prefix sum, FP64 and int64) and REDUCE_SUM.
+//
+// SCAN is a single-pass decoupled-lookback scan: every CTA takes the next
+// tile id from a counter (so a CTA only ever waits on tiles already owned by
+// running CTAs), scans its tile in shared memory, publishes the tile
+// aggregate, looks back over its predecessors' aggregates / inclusive
+// prefixes with one warp, then publishes its own inclusive prefix.  Flags
+// carry a launch epoch, so the workspace never needs re-zeroing between calls
+// (and the call can be captured in a CUDA graph): the last CTA to finish
+// resets the tile counter and advances the epoch.  Every wait is bounded; a
+// wait that gives up sets the workspace error word and the call's results are
+// invalid (b200_scan_workspace_error reads it back).
+#include "b200_internal.cuh"
+#include "b200_reduce.cuh"
+
+using namespace b200;
+
+namespace {
+
+constexpr int kScanBlock = 256;
+constexpr int kScanItems = 16;
+constexpr int kScanTile = kScanBlock * kScanItems;
+constexpr long long kSpinLimit = 1LL << 22;
+
+struct ScanHeader {
+  unsigned long long epoch;
+  unsigned int tile_counter;
+  unsigned int done_counter;
+  unsigned int error;
+  unsigned int pad[59];
+};
+static_assert(sizeof(ScanHeader) == 256, "scan header is 256 bytes");
+
+__device__ __forceinline__ int padded(int i) { return i + (i >> 4); }
+
+__device__ __forceinline__ unsigned long long ld_acquire(const unsigned long long* p) {
+  unsigned long long v;
+  asm volatile("ld.acquire.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+  return v;
+}
+
+__device__ __forceinline__ void st_release(unsigned long long* p, unsigned long long v) {
+  asm volatile("st.release.gpu.global.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
+}
+
+template <typename T>
+__device__ __forceinline__ T warp_inclusive_scan(T v) {
+  const int lane = threadIdx.x & 31;
+#pragma unroll
+  for (int off = 1; off < 32; off <<= 1) {
+    T o = __shfl_up_sync(0xffffffffu, v, off);
+    if (lane >= off) v += o;
+  }
+  return v;
+}
+
+template <typename T>
+__global__ void __launch_bounds__(kScanBlock)
+scan_kernel(const T* __restrict__ x, T* __restrict__ y, int64_t n, T init,
+            ScanHeader* __restrict__ hdr, unsigned long long* __restrict__ flags,
+            T* __restrict__ aggs, T* __restrict__ incs) {
+  __shared__ T s_tile[kScanTile + kScanTile / 16];
+  __shared__ T s_warp[kScanBlock / 32];
+  __shared__ T s_excl;
+  __shared__ unsigned int s_tile_id;
+  __shared__ unsigned long long s_epoch;
+  __shared__ bool s_last;
+
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  if (tid == 0) {
+    s_epoch = *reinterpret_cast<volatile unsigned long long*>(&hdr->epoch);
+    s_tile_id = atomicAdd(&hdr->tile_counter, 1u);
+  }
+  __syncthreads();
+  const unsigned int tile = s_tile_id;
+  const unsigned long long epoch = s_epoch;
+  const unsigned long long AGG = epoch * 4 + 1, INC = epoch * 4 + 2;
+  const int64_t base = static_cast<int64_t>(tile) * kScanTile;
+
+  // striped, coalesced load into shared memory
+#pragma unroll
+  for (int u = 0; u < kScanItems; ++u) {
+    int k = u * kScanBlock + tid;
+    int64_t i = base + k;
+    s_tile[padded(k)] = (i < n) ? __ldg(x + i) : T(0);
+  }
+  __syncthreads();
+
+  // each thread scans its IT consecutive items
+  T v[kScanItems];
+  T run = T(0);
+#pragma unroll
+  for (int u = 0; u < kScanItems; ++u) {
+    v[u] = run;  // exclusive within the thread
+    run += s_tile[padded(tid * kScanItems + u)];
+  }
+  // block scan of thread totals
+  T incl = warp_inclusive_scan(run);
+  if (lane == 31) s_warp[warp] = incl;
+  __syncthreads();
+  if (warp == 0) {
+    T w = (lane < kScanBlock / 32) ? s_warp[lane] : T(0);
+    T wi = warp_inclusive_scan(w);
+    if (lane < kScanBlock / 32) s_warp[lane] = wi - w;  // exclusive warp offsets
+  }
+  __syncthreads();
+  const T thread_excl = s_warp[warp] + (incl - run);
+  // The tile aggregate is the last thread's inclusive total.
+  __syncthreads();
+  if (tid == kScanBlock - 1) s_warp[0] = thread_excl + run;
+  __syncthreads();
+  const T agg = s_warp[0];
+
+  // decoupled lookback (warp 0)
+  if (warp == 0) {
+    T exclusive = init;
+    if (tile == 0) {
+      if (lane == 0) {
+        incs[0] = init + agg;
+        __threadfence();
+        st_release(&flags[0], INC);
+      }
+    } else {
+      if (lane == 0) {
+        aggs[tile] = agg;
+        __threadfence();
+        st_release(&flags[tile], AGG);
+      }
+      T acc = T(0);
+      int64_t p_hi = static_cast<int64_t>(tile) - 1;  // nearest unexamined predecessor
+      bool done = false;
+      while (!done) {
+        int64_t p = p_hi - lane;
+        unsigned long long f = INC;  // lanes past tile 0 act as a terminator
+        T val = T(0);
+        if (p >= 0) {
+          long long spins = 0;
+          f = ld_acquire(&flags[p]);
+          while (f < AGG) {
+            if (++spins > kSpinLimit) {
+              atomicExch(&hdr->error, 1u);
+              f = INC;
+              break;
+            }
+            if (spins > 64) __nanosleep(64);
+            f = ld_acquire(&flags[p]);
+          }
+          // L1-bypassing loads: the values were written by other SMs.
+          if (f >= AGG) val = (f == INC) ? __ldcg(incs + p) : __ldcg(aggs + p);
+        }
+        // first lane (nearest predecessor) holding an inclusive prefix
+        unsigned int inc_mask = __ballot_sync(0xffffffffu, f == INC);
+        int stop = inc_mask ? (__ffs(inc_mask) - 1) : 32;
+        if (lane > stop) val = T(0);
+        // fixed lane order: nearest predecessor first
+#pragma unroll
+        for (int off = 16; off > 0; off >>= 1) val += __shfl_down_sync(0xffffffffu, val, off);
+        acc += __shfl_sync(0xffffffffu, val, 0);
+        if (stop < 32) done = true;
+        p_hi -= 32;
+      }
+      exclusive = acc;
+      if (lane == 0) {
+        incs[tile] = exclusive + agg;
+        __threadfence();
+        st_release(&flags[tile], INC);
+      }
+    }
+    if (lane == 0) s_excl = exclusive;
+  }
+  __syncthreads();
+  const T prefix = s_excl + thread_excl;
+#pragma unroll
+  for (int u = 0; u < kScanItems; ++u) s_tile[padded(tid * kScanItems + u)] = prefix + v[u];
+  __syncthreads();
+#pragma unroll
+  for (int u = 0; u < kScanItems; ++u) {
+    int k = u * kScanBlock + tid;
+    int64_t i = base + k;
+    if (i < n) y[i] = s_tile[padded(k)];
+  }
+
+  // the last CTA to finish prepares the workspace for the next call
+  if (tid == 0) {
+    __threadfence();
+    unsigned int prev = atomicAdd(&hdr->done_counter, 1u);
+    s_last = (prev == gridDim.x - 1);
+  }
+  __syncthreads();
+  if (s_last && tid == 0) {
+    hdr->tile_counter = 0u;
+    hdr->done_counter = 0u;
+    __threadfence();
+    *reinterpret_cast<volatile unsigned long long*>(&hdr->epoch) = epoch + 1;
+  }
+}
+
+int64_t scan_tiles(int64_t n) { return ceil_div(n > 0 ? n : 1, kScanTile); }
+
+template <typename T>
+int launch_scan(const char* name, const T* x, T* y, int64_t n, T init, void* ws,
+                size_t ws_bytes, cudaStream_t st) {
+  if (n < 0 || (n > 0 && (!x || !y))) return invalid("%s: bad args", name);
+  if (n == 0) return B200_OK;
+  int64_t tiles = scan_tiles(n);
+  if (tiles > 0x7fffffffLL) return invalid("%s: n too large", name);
+  size_t need = 256 + static_cast<size_t>(tiles) * 24;
+  if (!ws || ws_bytes < need) {
+    set_error("%s: workspace %zu bytes, need %zu", name, ws_bytes, need);
+    return B200_ERR_WORKSPACE;
+  }
+  char* w = static_cast<char*>(ws);
+  ScanHeader* hdr = reinterpret_cast<ScanHeader*>(w);
+  unsigned long long* flags = reinterpret_cast<unsigned long long*>(w + 256);
+  T* aggs = reinterpret_cast<T*>(w + 256 + tiles * 8);
+  T* incs = reinterpret_cast<T*>(w + 256 + tiles * 16);
+  scan_kernel<T><<<static_cast<int>(tiles), kScanBlock, 0, st>>>(x, y, n, init, hdr, flags,
+                                                                 aggs, incs);
+  return after_launch(name);
+}
+
+// ---- REDUCE_SUM -------------------------------------------------------------
+template <int BS, int IT>
+__global__ void __launch_bounds__(BS)
+reduce_sum_kernel(const double* __restrict__ x, int64_t n, double init,
+                  double* __restrict__ out, double* __restrict__ partials,
+                  unsigned int* __restrict__ counter) {
+  __shared__ double smem[BS / 32];
+  __shared__ bool last_flag;
+  double s = 0.0;
+  for (int64_t t0 = static_cast<int64_t>(blockIdx.x) * (BS * IT); t0 < n;
+       t0 += static_cast<int64_t>(gridDim.x) * (BS * IT)) {
+    double v[IT];
+#pragma unroll
+    for (int u = 0; u < IT; ++u) {
+      int64_t i = t0 + u * BS + threadIdx.x;
+      v[u] = (i < n) ? __ldg(x + i) : 0.0;
+    }
+#pragma unroll
+    for (int u = 0; u < IT; ++u) s += v[u];
+  }
+  s = block_sum<BS>(s, smem);
+  if (threadIdx.x == 0) partials[blockIdx.x] = s;
+  if (arrive_last(counter, &last_flag)) {
+    double t = 0.0;
+    for (int i = threadIdx.x; i < static_cast<int>(gridDim.x); i += BS)
+      t += __ldcg(partials + i);
+    t = block_sum<BS>(t, smem);
+    if (threadIdx.x == 0) {
+      *out = init + t;
+      *counter = 0u;
+    }
+  }
+}
+
+}  // namespace
+
+extern "C" {
+
+size_t b200_scan_workspace_bytes(int64_t n) {
+  return 256 + static_cast<size_t>(scan_tiles(n)) * 24;
+}
+
+int b200_algorithm_scan(const double* x, double* y, int64_t n, double init,
+                        void* workspace, size_t workspace_bytes, const b200_tune* tune,
+                        b200_stream_t stream) {
+  (void)tune;
+  return launch_scan<double>("b200_algorithm_scan", x, y, n, init, workspace,
+                             workspace_bytes, as_stream(stream));
+}
+
+int b200_algorithm_scan_i64(const int64_t* x, int64_t* y, int64_t n, int64_t init,
+                            void* workspace, size_t workspace_bytes,
+                            const b200_tune* tune, b200_stream_t stream) {
+  (void)tune;
+  return launch_scan<long long>("b200_algorithm_scan_i64",
+                                reinterpret_cast<const long long*>(x),
+                                reinterpret_cast<long long*>(y), n,
+                                static_cast<long long>(init), workspace, workspace_bytes,
+                                as_stream(stream));
+}
+
+int b200_algorithm_reduce_sum(const double* x, int64_t n, double sum_init, double* sum,
+                              void* workspace, size_t workspace_bytes,
+                              const b200_tune* tune, b200_stream_t stream) {
+  if (n < 0 || (n > 0 && !x) || !sum) return invalid("b200_algorithm_reduce_sum: bad args");
+  int block = (tune && tune->block_size) ? tune->block_size : 256;
+  int items = (tune && tune->items) ? tune->items : 8;
+  if (!valid_block(block))
+    return invalid("b200_algorithm_reduce_sum: bad block size %d", block);
+  int grid = reduce_grid(n, tune, block, items);
+  size_t need = reduce_ws_bytes_for_grid(grid);
+  if (!workspace || workspace_bytes < need) {
+    set_error("b200_algorithm_reduce_sum: workspace %zu bytes, need %zu", workspace_bytes,
+              need);
+    return B200_ERR_WORKSPACE;
+  }
+  unsigned int* counter = static_cast<unsigned int*>(workspace);
+  double* partials = reinterpret_cast<double*>(static_cast<char*>(workspace) + 256);
+  cudaStream_t st = as_stream(stream);
+  B200_DISPATCH_BLOCK(block, BS, B200_DISPATCH_ITEMS(items, IT,
+    reduce_sum_kernel<BS, IT><<<grid, BS, 0, st>>>(x, n, sum_init, sum, partials, counter)));
+  return after_launch("b200_algorithm_reduce_sum");
+}
+
+}  // extern "C"

@@ -1,0 +1,251 @@
+// Apps group: PRESSURE, ENERGY, VOL3D, DEL_DOT_VEC_2D.
+//
+// PRESSURE's two loops and ENERGY's six loops are point-wise in i (each body
+// reads only index i of arrays written by earlier bodies), so each rep is one
+// fused pass that applies the bodies in order per element: the per-point
+// arithmetic is the suite's, and arrays that only carry values between
+// bodies stay in registers.
+#include "b200_internal.cuh"
+#include "b200_map.cuh"
+
+using namespace b200;
+
+namespace {
+
+// apps/PRESSURE.hpp:39-46 (BODY1 then BODY2)
+struct Pressure {
+  const double* __restrict__ compression;
+  double* __restrict__ bvc;
+  double* __restrict__ p_new;
+  const double* __restrict__ e_old;
+  const double* __restrict__ vnewc;
+  double cls, p_cut, pmin, eosvmax;
+  __device__ void operator()(int64_t i) const {
+    const double b = cls * (ld(compression + i) + 1.0);
+    bvc[i] = b;
+    double p = b * ld(e_old + i);
+    if (fabs(p) < p_cut) p = 0.0;
+    if (ld(vnewc + i) >= eosvmax) p = 0.0;
+    if (p < pmin) p = pmin;
+    p_new[i] = p;
+  }
+};
+
+// apps/ENERGY.hpp:111-178 (BODY1..BODY6 in order)
+struct Energy {
+  double* __restrict__ e_new;
+  const double* __restrict__ e_old;
+  const double* __restrict__ delvc;
+  const double* __restrict__ p_new;
+  const double* __restrict__ p_old;
+  double* __restrict__ q_new;
+  const double* __restrict__ q_old;
+  const double* __restrict__ work;
+  const double* __restrict__ compHalfStep;
+  const double* __restrict__ pHalfStep;
+  const double* __restrict__ bvc;
+  const double* __restrict__ pbvc;
+  const double* __restrict__ ql_old;
+  const double* __restrict__ qq_old;
+  const double* __restrict__ vnewc;
+  double rho0, e_cut, emin, q_cut;
+
+  __device__ void operator()(int64_t i) const {
+    const double dv = ld(delvc + i);
+    const double po = ld(p_old + i), qo = ld(q_old + i), wk = ld(work + i);
+    const double ph = ld(pHalfStep + i), pn = ld(p_new + i);
+    // BODY1
+    double e = ld(e_old + i) - 0.5 * dv * (po + qo) + 0.5 * wk;
+    // BODY2
+    double qn;
+    if (dv > 0.0) {
+      qn = 0.0;
+    } else {
+      double vhalf = 1.0 / (1.0 + ld(compHalfStep + i));
+      double ssc = (ld(pbvc + i) * e + vhalf * vhalf * ld(bvc + i) * ph) / rho0;
+      if (ssc <= 0.1111111e-36) ssc = 0.3333333e-18;
+      else ssc = sqrt(ssc);
+      qn = (ssc * ld(ql_old + i) + ld(qq_old + i));
+    }
+    // BODY3
+    e = e + 0.5 * dv * (3.0 * (po + qo) - 4.0 * (ph + qn));
+    // BODY4
+    e += 0.5 * wk;
+    if (fabs(e) < e_cut) e = 0.0;
+    if (e < emin) e = emin;
+    // BODY5
+    double q_tilde;
+    if (dv > 0.0) {
+      q_tilde = 0.;
+    } else {
+      double vn = ld(vnewc + i);
+      double ssc = (ld(pbvc + i) * e + vn * vn * ld(bvc + i) * pn) / rho0;
+      if (ssc <= 0.1111111e-36) ssc = 0.3333333e-18;
+      else ssc = sqrt(ssc);
+      q_tilde = (ssc * ld(ql_old + i) + ld(qq_old + i));
+    }
+    e = e - (7.0 * (po + qo) - 8.0 * (ph + qn) + (pn + q_tilde)) * dv / 6.0;
+    if (fabs(e) < e_cut) e = 0.0;
+    if (e < emin) e = emin;
+    // BODY6
+    if (dv <= 0.0) {
+      double vn = ld(vnewc + i);
+      double ssc = (ld(pbvc + i) * e + vn * vn * ld(bvc + i) * pn) / rho0;
+      if (ssc <= 0.1111111e-36) ssc = 0.3333333e-18;
+      else ssc = sqrt(ssc);
+      qn = (ssc * ld(ql_old + i) + ld(qq_old + i));
+      if (fabs(qn) < q_cut) qn = 0.0;
+    }
+    e_new[i] = e;
+    q_new[i] = qn;
+  }
+};
+
+// apps/VOL3D.hpp:88-146 -- the macro body with its four accumulation blocks
+// (the third repeats the second block's cross products), corner pointers
+// from NDPTRSET (apps/AppsData.hpp: v0=v, v1=v0+1, v2=v0+jp, v3=v1+jp,
+// v4..v7 = v0..v3 + kp).
+struct Vol3D {
+  const double* __restrict__ x;
+  const double* __restrict__ y;
+  const double* __restrict__ z;
+  double* __restrict__ vol;
+  double vnormq;
+  int64_t jp, kp, ibegin;
+  __device__ void operator()(int64_t ii) const {
+    const int64_t i = ibegin + ii;
+    const int64_t o1 = 1, o2 = jp, o3 = 1 + jp, o4 = kp, o5 = 1 + kp, o6 = jp + kp,
+                  o7 = 1 + jp + kp;
+    const double X0 = ld(x + i), X1 = ld(x + i + o1), X2 = ld(x + i + o2), X3 = ld(x + i + o3),
+                 X4 = ld(x + i + o4), X5 = ld(x + i + o5), X6 = ld(x + i + o6),
+                 X7 = ld(x + i + o7);
+    const double Y0 = ld(y + i), Y1 = ld(y + i + o1), Y2 = ld(y + i + o2), Y3 = ld(y + i + o3),
+                 Y4 = ld(y + i + o4), Y5 = ld(y + i + o5), Y6 = ld(y + i + o6),
+                 Y7 = ld(y + i + o7);
+    const double Z0 = ld(z + i), Z1 = ld(z + i + o1), Z2 = ld(z + i + o2), Z3 = ld(z + i + o3),
+                 Z4 = ld(z + i + o4), Z5 = ld(z + i + o5), Z6 = ld(z + i + o6),
+                 Z7 = ld(z + i + o7);
+    double x71 = X7 - X1, x72 = X7 - X2, x74 = X7 - X4;
+    double x30 = X3 - X0, x50 = X5 - X0, x60 = X6 - X0;
+    double y71 = Y7 - Y1, y72 = Y7 - Y2, y74 = Y7 - Y4;
+    double y30 = Y3 - Y0, y50 = Y5 - Y0, y60 = Y6 - Y0;
+    double z71 = Z7 - Z1, z72 = Z7 - Z2, z74 = Z7 - Z4;
+    double z30 = Z3 - Z0, z50 = Z5 - Z0, z60 = Z6 - Z0;
+    double xps = x71 + x60, yps = y71 + y60, zps = z71 + z60;
+    double cyz = y72 * z30 - z72 * y30;
+    double czx = z72 * x30 - x72 * z30;
+    double cxy = x72 * y30 - y72 * x30;
+    double v = xps * cyz + yps * czx + zps * cxy;
+    xps = x72 + x50; yps = y72 + y50; zps = z72 + z50;
+    cyz = y74 * z60 - z74 * y60;
+    czx = z74 * x60 - x74 * z60;
+    cxy = x74 * y60 - y74 * x60;
+    v += xps * cyz + yps * czx + zps * cxy;
+    xps = x74 + x30; yps = y74 + y30; zps = z74 + z30;
+    cyz = y74 * z60 - z74 * y60;
+    czx = z74 * x60 - x74 * z60;
+    cxy = x74 * y60 - y74 * x60;
+    v += xps * cyz + yps * czx + zps * cxy;
+    xps = x74 + x30; yps = y74 + y30; zps = z74 + z30;
+    cyz = y71 * z50 - z71 * y50;
+    czx = z71 * x50 - x71 * z50;
+    cxy = x71 * y50 - y71 * x50;
+    v += xps * cyz + yps * czx + zps * cxy;
+    vol[i] = v * vnormq;
+  }
+};
+
+// apps/DEL_DOT_VEC_2D.hpp:65-90 with corners from NDSET2D (AppsData.hpp:
+// v4=v, v1=v4+1, v2=v1+jp, v3=v4+jp); zone index through real_zones.
+struct DelDotVec2D {
+  const double* __restrict__ x;
+  const double* __restrict__ y;
+  const double* __restrict__ xdot;
+  const double* __restrict__ ydot;
+  double* __restrict__ div;
+  const int64_t* __restrict__ real_zones;
+  int64_t jp;
+  double ptiny, half;
+  __device__ void operator()(int64_t ii) const {
+    const int64_t i = ld(real_zones + ii);
+    const int64_t c1 = i + 1, c2 = i + 1 + jp, c3 = i + jp, c4 = i;
+    const double x1 = ld(x + c1), x2 = ld(x + c2), x3 = ld(x + c3), x4 = ld(x + c4);
+    const double y1 = ld(y + c1), y2 = ld(y + c2), y3 = ld(y + c3), y4 = ld(y + c4);
+    const double fx1 = ld(xdot + c1), fx2 = ld(xdot + c2), fx3 = ld(xdot + c3),
+                 fx4 = ld(xdot + c4);
+    const double fy1 = ld(ydot + c1), fy2 = ld(ydot + c2), fy3 = ld(ydot + c3),
+                 fy4 = ld(ydot + c4);
+    double xi = half * (x1 + x2 - x3 - x4);
+    double xj = half * (x2 + x3 - x4 - x1);
+    double yi = half * (y1 + y2 - y3 - y4);
+    double yj = half * (y2 + y3 - y4 - y1);
+    double fxi = half * (fx1 + fx2 - fx3 - fx4);
+    double fxj = half * (fx2 + fx3 - fx4 - fx1);
+    double fyi = half * (fy1 + fy2 - fy3 - fy4);
+    double fyj = half * (fy2 + fy3 - fy4 - fy1);
+    double rarea = 1.0 / (xi * yj - xj * yi + ptiny);
+    double dfxdx = rarea * (fxi * yj - fxj * yi);
+    double dfydy = rarea * (fyj * xi - fyi * xj);
+    double affine = (fy1 + fy2 + fy3 + fy4) / (y1 + y2 + y3 + y4);
+    div[i] = dfxdx + dfydy + affine;
+  }
+};
+
+}  // namespace
+
+extern "C" {
+
+int b200_apps_pressure(const double* compression, double* bvc, double* p_new,
+                       const double* e_old, const double* vnewc, double cls,
+                       double p_cut, double pmin, double eosvmax, int64_t n,
+                       const b200_tune* tune, b200_stream_t stream) {
+  if (n < 0 || (n > 0 && (!compression || !bvc || !p_new || !e_old || !vnewc)))
+    return invalid("b200_apps_pressure: bad args");
+  return launch_map1d("b200_apps_pressure",
+                      Pressure{compression, bvc, p_new, e_old, vnewc, cls, p_cut, pmin,
+                               eosvmax},
+                      n, tune, as_stream(stream));
+}
+
+int b200_apps_energy(double* e_new, const double* e_old, const double* delvc,
+                     const double* p_new, const double* p_old, double* q_new,
+                     const double* q_old, const double* work,
+                     const double* compHalfStep, const double* pHalfStep,
+                     const double* bvc, const double* pbvc, const double* ql_old,
+                     const double* qq_old, const double* vnewc, double rho0,
+                     double e_cut, double emin, double q_cut, int64_t n,
+                     const b200_tune* tune, b200_stream_t stream) {
+  if (n < 0 || (n > 0 && (!e_new || !e_old || !delvc || !p_new || !p_old || !q_new ||
+                          !q_old || !work || !compHalfStep || !pHalfStep || !bvc ||
+                          !pbvc || !ql_old || !qq_old || !vnewc)))
+    return invalid("b200_apps_energy: bad args");
+  return launch_map1d("b200_apps_energy",
+                      Energy{e_new, e_old, delvc, p_new, p_old, q_new, q_old, work,
+                             compHalfStep, pHalfStep, bvc, pbvc, ql_old, qq_old, vnewc,
+                             rho0, e_cut, emin, q_cut},
+                      n, tune, as_stream(stream));
+}
+
+int b200_apps_vol3d(const double* x, const double* y, const double* z, double* vol,
+                    double vnormq, int64_t jp, int64_t kp, int64_t ibegin,
+                    int64_t iend, const b200_tune* tune, b200_stream_t stream) {
+  if (!x || !y || !z || !vol || ibegin < 0 || iend < ibegin || jp < 0 || kp < 0)
+    return invalid("b200_apps_vol3d: bad args");
+  return launch_map1d("b200_apps_vol3d", Vol3D{x, y, z, vol, vnormq, jp, kp, ibegin},
+                      iend - ibegin, tune, as_stream(stream));
+}
+
+int b200_apps_del_dot_vec_2d(const double* x, const double* y, const double* xdot,
+                             const double* ydot, double* div,
+                             const int64_t* real_zones, int64_t n_real_zones,
+                             int64_t jp, double ptiny, double half,
+                             const b200_tune* tune, b200_stream_t stream) {
+  if (n_real_zones < 0 || jp < 0 ||
+      (n_real_zones > 0 && (!x || !y || !xdot || !ydot || !div || !real_zones)))
+    return invalid("b200_apps_del_dot_vec_2d: bad args");
+  return launch_map1d("b200_apps_del_dot_vec_2d",
+                      DelDotVec2D{x, y, xdot, ydot, div, real_zones, jp, ptiny, half},
+                      n_real_zones, tune, as_stream(stream));
+}
+
+}  // extern "C"

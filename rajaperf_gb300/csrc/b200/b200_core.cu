@@ -256,3 +256,39 @@ int b200_init_uniform_i64(int64_t* p, int64_t n, uint64_t seed,
 }
 
 }  // extern "C"
+
+// ---- FP64 pipe probe ----------------------------------------------------------
+
+namespace {
+
+// Eight independent FMA chains per thread; out[] receives one value per thread
+// so the chains are live.  `out` must hold probe_threads() doubles.
+__global__ void __launch_bounds__(256) dfma_probe_kernel(double* out, double a, double b,
+                                                         int iters) {
+  double x0 = threadIdx.x * 1e-3, x1 = x0 + 1, x2 = x0 + 2, x3 = x0 + 3;
+  double x4 = x0 + 4, x5 = x0 + 5, x6 = x0 + 6, x7 = x0 + 7;
+  for (int i = 0; i < iters; ++i) {
+    x0 = fma(x0, a, b); x1 = fma(x1, a, b); x2 = fma(x2, a, b); x3 = fma(x3, a, b);
+    x4 = fma(x4, a, b); x5 = fma(x5, a, b); x6 = fma(x6, a, b); x7 = fma(x7, a, b);
+  }
+  out[static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x] =
+      x0 + x1 + x2 + x3 + x4 + x5 + x6 + x7;
+}
+
+}  // namespace
+
+extern "C" {
+
+int64_t b200_probe_dfma_threads(void) {
+  return static_cast<int64_t>(device_info().sm_count) * 8 * 256;
+}
+
+int b200_probe_dfma(double* out, int32_t iters, int64_t* fma_count, b200_stream_t stream) {
+  if (!out || iters <= 0 || !fma_count) return invalid("b200_probe_dfma: bad args");
+  int blocks = device_info().sm_count * 8;
+  dfma_probe_kernel<<<blocks, 256, 0, as_stream(stream)>>>(out, 0.999999, 1e-7, iters);
+  *fma_count = static_cast<int64_t>(blocks) * 256 * 8 * iters;
+  return after_launch("b200_probe_dfma");
+}
+
+}  // extern "C"

@@ -1,0 +1,301 @@
+// LCALS group: HYDRO_1D, HYDRO_2D, EOS, FIRST_DIFF, INT_PREDICT, FIRST_MIN,
+// DIFF_PREDICT, PLANCKIAN.  Each functor body is the suite's macro body for
+// one index (citations at each functor); the arithmetic is written in the
+// macro's operation order.
+#include "b200_internal.cuh"
+#include "b200_map.cuh"
+#include "b200_reduce.cuh"
+
+using namespace b200;
+
+namespace {
+
+// lcals/HYDRO_1D.hpp:30
+struct Hydro1D {
+  double* __restrict__ x;
+  const double* __restrict__ y;
+  const double* __restrict__ z;
+  double q, r, t;
+  __device__ void operator()(int64_t i) const {
+    x[i] = q + ld(y + i) * (r * ld(z + i + 10) + t * ld(z + i + 11));
+  }
+};
+
+// lcals/EOS.hpp:33
+struct Eos {
+  double* __restrict__ x;
+  const double* __restrict__ y;
+  const double* __restrict__ z;
+  const double* __restrict__ u;
+  double q, r, t;
+  __device__ void operator()(int64_t i) const {
+    x[i] = ld(u + i) + r * (ld(z + i) + r * ld(y + i)) +
+           t * (ld(u + i + 3) + r * (ld(u + i + 2) + r * ld(u + i + 1)) +
+                t * (ld(u + i + 6) + q * (ld(u + i + 5) + q * ld(u + i + 4))));
+  }
+};
+
+// lcals/FIRST_DIFF.hpp:25
+struct FirstDiff {
+  double* __restrict__ x;
+  const double* __restrict__ y;
+  __device__ void operator()(int64_t i) const { x[i] = ld(y + i + 1) - ld(y + i); }
+};
+
+// lcals/INT_PREDICT.hpp:40 -- px[0..n) is written, planes 2..12 are read.
+struct IntPredict {
+  double* px;
+  int64_t o;
+  double dm22, dm23, dm24, dm25, dm26, dm27, dm28, c0;
+  __device__ void operator()(int64_t i) const {
+    const double* p = px;
+    px[i] = dm28 * ld(p + i + o * 12) + dm27 * ld(p + i + o * 11) +
+            dm26 * ld(p + i + o * 10) + dm25 * ld(p + i + o * 9) +
+            dm24 * ld(p + i + o * 8) + dm23 * ld(p + i + o * 7) +
+            dm22 * ld(p + i + o * 6) +
+            c0 * (ld(p + i + o * 4) + ld(p + i + o * 5)) + ld(p + i + o * 2);
+  }
+};
+
+// lcals/DIFF_PREDICT.hpp -- planes 4..13 of px are updated in place per i.
+struct DiffPredict {
+  double* px;
+  const double* __restrict__ cx;
+  int64_t o;
+  __device__ void operator()(int64_t i) const {
+    double ar, br, cr;
+    ar = ld(cx + i + o * 4);
+    br = ar - px[i + o * 4];
+    px[i + o * 4] = ar;
+    cr = br - px[i + o * 5];
+    px[i + o * 5] = br;
+    ar = cr - px[i + o * 6];
+    px[i + o * 6] = cr;
+    br = ar - px[i + o * 7];
+    px[i + o * 7] = ar;
+    cr = br - px[i + o * 8];
+    px[i + o * 8] = br;
+    ar = cr - px[i + o * 9];
+    px[i + o * 9] = cr;
+    br = ar - px[i + o * 10];
+    px[i + o * 10] = ar;
+    cr = br - px[i + o * 11];
+    px[i + o * 11] = br;
+    px[i + o * 13] = cr - px[i + o * 12];
+    px[i + o * 12] = cr;
+  }
+};
+
+// lcals/PLANCKIAN.hpp
+struct Planckian {
+  const double* __restrict__ x;
+  double* __restrict__ y;
+  const double* __restrict__ u;
+  const double* __restrict__ v;
+  double* __restrict__ w;
+  __device__ void operator()(int64_t i) const {
+    double yi = ld(u + i) / ld(v + i);
+    y[i] = yi;
+    w[i] = ld(x + i) / (exp(yi) - 1.0);
+  }
+};
+
+// ---- HYDRO_2D ---------------------------------------------------------------
+// lcals/HYDRO_2D.hpp:66-90.  Pass 1 (BODY1) writes za, zb on the interior;
+// pass 2 fuses BODY2 and BODY3 (both point-wise given za, zb), so a rep is two
+// launches instead of three and zu/zv are not re-read for BODY3.
+template <int BS>
+__global__ void __launch_bounds__(BS)
+hydro2d_body1(double* __restrict__ za, double* __restrict__ zb,
+              const double* __restrict__ zm, const double* __restrict__ zp,
+              const double* __restrict__ zq, const double* __restrict__ zr,
+              int64_t kn, int64_t jn) {
+  const int64_t j = 1 + static_cast<int64_t>(blockIdx.x) * BS + threadIdx.x;
+  if (j >= jn - 1) return;
+  for (int64_t k = 1 + blockIdx.y; k < kn - 1; k += gridDim.y) {
+    const int64_t c = j + k * jn;
+    za[c] = (ld(zp + c - 1 + jn) + ld(zq + c - 1 + jn) - ld(zp + c - 1) - ld(zq + c - 1)) *
+            (ld(zr + c) + ld(zr + c - 1)) / (ld(zm + c - 1) + ld(zm + c - 1 + jn));
+    zb[c] = (ld(zp + c - 1) + ld(zq + c - 1) - ld(zp + c) - ld(zq + c)) *
+            (ld(zr + c) + ld(zr + c - jn)) / (ld(zm + c) + ld(zm + c - 1));
+  }
+}
+
+template <int BS>
+__global__ void __launch_bounds__(BS)
+hydro2d_body23(const double* __restrict__ za, const double* __restrict__ zb,
+               const double* __restrict__ zr, double* __restrict__ zu,
+               double* __restrict__ zv, const double* __restrict__ zz,
+               double* __restrict__ zrout, double* __restrict__ zzout, double s,
+               double t, int64_t kn, int64_t jn) {
+  const int64_t j = 1 + static_cast<int64_t>(blockIdx.x) * BS + threadIdx.x;
+  if (j >= jn - 1) return;
+  for (int64_t k = 1 + blockIdx.y; k < kn - 1; k += gridDim.y) {
+    const int64_t c = j + k * jn;
+    const double za0 = ld(za + c), za1 = ld(za + c - 1);
+    const double zb0 = ld(zb + c), zb1 = ld(zb + c + jn);
+    const double zz0 = ld(zz + c), zr0 = ld(zr + c);
+    const double u = zu[c] + s * (za0 * (zz0 - ld(zz + c + 1)) - za1 * (zz0 - ld(zz + c - 1)) -
+                                  zb0 * (zz0 - ld(zz + c - jn)) + zb1 * (zz0 - ld(zz + c + jn)));
+    const double v = zv[c] + s * (za0 * (zr0 - ld(zr + c + 1)) - za1 * (zr0 - ld(zr + c - 1)) -
+                                  zb0 * (zr0 - ld(zr + c - jn)) + zb1 * (zr0 - ld(zr + c + jn)));
+    zu[c] = u;
+    zv[c] = v;
+    zrout[c] = zr0 + t * u;
+    zzout[c] = zz0 + t * v;
+  }
+}
+
+// ---- FIRST_MIN --------------------------------------------------------------
+// lcals/FIRST_MIN.hpp:29-54, FIRST_MIN-Seq.cpp:34-48: strict '<' scan, so the
+// result is the smallest index holding the minimum (or initloc when the
+// initial value is not beaten).
+template <int BS, int IT>
+__global__ void __launch_bounds__(BS)
+first_min_kernel(const double* __restrict__ x, int64_t n, double xmin_init,
+                 int64_t initloc, int64_t* __restrict__ minloc_out,
+                 double* __restrict__ minval_out, MinLoc* __restrict__ partials,
+                 unsigned int* __restrict__ counter) {
+  __shared__ MinLoc smem[BS / 32];
+  __shared__ bool last_flag;
+  MinLoc m;
+  m.val = xmin_init;
+  m.loc = initloc;
+  for (int64_t t0 = static_cast<int64_t>(blockIdx.x) * (BS * IT); t0 < n;
+       t0 += static_cast<int64_t>(gridDim.x) * (BS * IT)) {
+    double v[IT];
+#pragma unroll
+    for (int u = 0; u < IT; ++u) {
+      int64_t i = t0 + u * BS + threadIdx.x;
+      v[u] = (i < n) ? __ldg(x + i) : 0.0;
+    }
+#pragma unroll
+    for (int u = 0; u < IT; ++u) {
+      int64_t i = t0 + u * BS + threadIdx.x;
+      if (i < n && v[u] < m.val) { m.val = v[u]; m.loc = i; }
+    }
+  }
+  m = block_minloc<BS>(m, smem);
+  if (threadIdx.x == 0) partials[blockIdx.x] = m;
+  if (arrive_last(counter, &last_flag)) {
+    MinLoc a;
+    a.val = xmin_init;
+    a.loc = initloc;
+    for (int i = threadIdx.x; i < static_cast<int>(gridDim.x); i += BS) {
+      MinLoc p;
+      p.val = __ldcg(&partials[i].val);
+      p.loc = __ldcg(&partials[i].loc);
+      a = minloc_pick(a, p);
+    }
+    a = block_minloc<BS>(a, smem);
+    if (threadIdx.x == 0) {
+      *minloc_out = a.loc;
+      if (minval_out) *minval_out = a.val;
+      *counter = 0u;
+    }
+  }
+}
+
+dim3 rows_grid(int64_t jn, int64_t kn, int bs) {
+  int64_t gx = ceil_div(jn - 2 > 0 ? jn - 2 : 1, bs);
+  int64_t gy = kn - 2 > 0 ? kn - 2 : 1;
+  if (gy > 65535) gy = 65535;
+  return dim3(static_cast<unsigned>(gx), static_cast<unsigned>(gy), 1);
+}
+
+}  // namespace
+
+extern "C" {
+
+int b200_lcals_hydro_1d(double* x, const double* y, const double* z, double q,
+                        double r, double t, int64_t n, const b200_tune* tune,
+                        b200_stream_t stream) {
+  if (n < 0 || (n > 0 && (!x || !y || !z))) return invalid("b200_lcals_hydro_1d: bad args");
+  return launch_map1d("b200_lcals_hydro_1d", Hydro1D{x, y, z, q, r, t}, n, tune,
+                      as_stream(stream));
+}
+
+int b200_lcals_eos(double* x, const double* y, const double* z, const double* u,
+                   double q, double r, double t, int64_t n, const b200_tune* tune,
+                   b200_stream_t stream) {
+  if (n < 0 || (n > 0 && (!x || !y || !z || !u))) return invalid("b200_lcals_eos: bad args");
+  return launch_map1d("b200_lcals_eos", Eos{x, y, z, u, q, r, t}, n, tune,
+                      as_stream(stream));
+}
+
+int b200_lcals_first_diff(double* x, const double* y, int64_t n, const b200_tune* tune,
+                          b200_stream_t stream) {
+  if (n < 0 || (n > 0 && (!x || !y))) return invalid("b200_lcals_first_diff: bad args");
+  return launch_map1d("b200_lcals_first_diff", FirstDiff{x, y}, n, tune, as_stream(stream));
+}
+
+int b200_lcals_int_predict(double* px, double dm22, double dm23, double dm24,
+                           double dm25, double dm26, double dm27, double dm28,
+                           double c0, int64_t n, const b200_tune* tune,
+                           b200_stream_t stream) {
+  if (n < 0 || (n > 0 && !px)) return invalid("b200_lcals_int_predict: bad args");
+  return launch_map1d("b200_lcals_int_predict",
+                      IntPredict{px, n, dm22, dm23, dm24, dm25, dm26, dm27, dm28, c0}, n,
+                      tune, as_stream(stream));
+}
+
+int b200_lcals_diff_predict(double* px, const double* cx, int64_t n,
+                            const b200_tune* tune, b200_stream_t stream) {
+  if (n < 0 || (n > 0 && (!px || !cx))) return invalid("b200_lcals_diff_predict: bad args");
+  return launch_map1d("b200_lcals_diff_predict", DiffPredict{px, cx, n}, n, tune,
+                      as_stream(stream));
+}
+
+int b200_lcals_planckian(const double* x, double* y, const double* u, const double* v,
+                         double* w, int64_t n, const b200_tune* tune,
+                         b200_stream_t stream) {
+  if (n < 0 || (n > 0 && (!x || !y || !u || !v || !w)))
+    return invalid("b200_lcals_planckian: bad args");
+  return launch_map1d("b200_lcals_planckian", Planckian{x, y, u, v, w}, n, tune,
+                      as_stream(stream));
+}
+
+int b200_lcals_hydro_2d(double* za, double* zb, const double* zm, const double* zp,
+                        const double* zq, const double* zr, double* zu, double* zv,
+                        const double* zz, double* zrout, double* zzout, double s,
+                        double t, int64_t kn, int64_t jn, const b200_tune* tune,
+                        b200_stream_t stream) {
+  if (kn < 0 || jn < 0 || !za || !zb || !zm || !zp || !zq || !zr || !zu || !zv || !zz ||
+      !zrout || !zzout)
+    return invalid("b200_lcals_hydro_2d: bad args");
+  if (kn < 3 || jn < 3) return B200_OK;  // empty interior
+  int bs = (tune && tune->block_size) ? tune->block_size : 128;
+  if (!valid_block(bs)) return invalid("b200_lcals_hydro_2d: bad block size %d", bs);
+  cudaStream_t st = as_stream(stream);
+  dim3 grid = rows_grid(jn, kn, bs);
+  B200_DISPATCH_BLOCK(bs, BS,
+    hydro2d_body1<BS><<<grid, BS, 0, st>>>(za, zb, zm, zp, zq, zr, kn, jn);
+    hydro2d_body23<BS><<<grid, BS, 0, st>>>(za, zb, zr, zu, zv, zz, zrout, zzout, s, t,
+                                            kn, jn));
+  return after_launch("b200_lcals_hydro_2d", 2);
+}
+
+int b200_lcals_first_min(const double* x, int64_t n, double xmin_init, int64_t initloc,
+                         int64_t* minloc, double* minval, void* workspace,
+                         size_t workspace_bytes, const b200_tune* tune,
+                         b200_stream_t stream) {
+  if (n < 0 || (n > 0 && !x) || !minloc) return invalid("b200_lcals_first_min: bad args");
+  int block = (tune && tune->block_size) ? tune->block_size : 256;
+  int items = (tune && tune->items) ? tune->items : 4;
+  if (!valid_block(block)) return invalid("b200_lcals_first_min: bad block size %d", block);
+  int grid = reduce_grid(n, tune, block, items);
+  size_t need = reduce_ws_bytes_for_grid(grid);
+  if (!workspace || workspace_bytes < need) {
+    set_error("b200_lcals_first_min: workspace %zu bytes, need %zu", workspace_bytes, need);
+    return B200_ERR_WORKSPACE;
+  }
+  unsigned int* counter = static_cast<unsigned int*>(workspace);
+  MinLoc* partials = reinterpret_cast<MinLoc*>(static_cast<char*>(workspace) + 256);
+  cudaStream_t st = as_stream(stream);
+  B200_DISPATCH_BLOCK(block, BS, B200_DISPATCH_ITEMS(items, IT,
+    first_min_kernel<BS, IT><<<grid, BS, 0, st>>>(x, n, xmin_init, initloc, minloc, minval,
+                                                  partials, counter)));
+  return after_launch("b200_lcals_first_min");
+}
+
+}  // extern "C"

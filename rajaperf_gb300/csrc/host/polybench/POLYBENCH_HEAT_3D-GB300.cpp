@@ -1,0 +1,70 @@
+// Polybench_HEAT_3D.  Follows the suite's POLYBENCH_HEAT_3D.cpp:27-95:
+// N = cbrt(size) + 2 + cbrt(3) - 1, 20 time steps (--polybench_tsteps
+// overrides), A/B restored from Ainit/Binit before the timed rep loop.
+#include "Polybench.hpp"
+
+#include <cmath>
+
+namespace rajaperf {
+namespace polybench {
+
+POLYBENCH_HEAT_3D::POLYBENCH_HEAT_3D(const RunParams& params)
+    : KernelBase(rajaperf::Polybench_HEAT_3D, params) {
+  Index_type N_default = 102;
+  setDefaultProblemSize((N_default - 2) * (N_default - 2) * (N_default - 2));
+  setDefaultReps(20);
+  m_N = static_cast<Index_type>(std::cbrt(getTargetProblemSize()) + 2 + std::cbrt(3) - 1);
+  m_tsteps = params.getPolybenchTsteps() >= 0 ? params.getPolybenchTsteps() : 20;
+  setActualProblemSize((m_N - 2) * (m_N - 2) * (m_N - 2));
+  setItsPerRep(m_tsteps * (2 * getActualProblemSize()));
+  setKernelsPerRep(m_tsteps * 2);
+  setBytesReadPerRep((1 * sizeof(Real_type) * (m_N * m_N * m_N - 12 * (m_N - 2) - 8) +
+                      1 * sizeof(Real_type) * (m_N * m_N * m_N - 12 * (m_N - 2) - 8)) *
+                     m_tsteps);
+  setBytesWrittenPerRep((1 * sizeof(Real_type) * (m_N - 2) * (m_N - 2) * (m_N - 2) +
+                         1 * sizeof(Real_type) * (m_N - 2) * (m_N - 2) * (m_N - 2)) *
+                        m_tsteps);
+  setBytesAtomicModifyWrittenPerRep(0);
+  setFLOPsPerRep(m_tsteps * (15 * (m_N - 2) * (m_N - 2) * (m_N - 2) +
+                             15 * (m_N - 2) * (m_N - 2) * (m_N - 2)));
+  checksum_scale_factor = 0.0001 * (static_cast<Checksum_type>(getDefaultProblemSize()) /
+                                    getActualProblemSize());
+  setComplexity(Complexity::N);
+  setUsesFeature(Kernel);
+  setVariantDefined(Base_GB300);
+}
+
+void POLYBENCH_HEAT_3D::setUp(VariantID vid, size_t) {
+  allocAndInitData(m_Ainit, m_N * m_N * m_N, vid);
+  allocAndInitData(m_Binit, m_N * m_N * m_N, vid);
+  allocData(m_A, m_N * m_N * m_N, vid);
+  allocData(m_B, m_N * m_N * m_N, vid);
+}
+
+void POLYBENCH_HEAT_3D::prepareRun(size_t) {
+  copyDeviceToDevice(m_A, m_Ainit, m_N * m_N * m_N * sizeof(Real_type));
+  copyDeviceToDevice(m_B, m_Binit, m_N * m_N * m_N * sizeof(Real_type));
+}
+
+KernelBase::RepBody POLYBENCH_HEAT_3D::makeRepBody(size_t tune_idx) {
+  const b200_tune tn = getTune(tune_idx);
+  return [=](b200_stream_t s) {
+    checkB200(b200_polybench_heat_3d(m_A, m_B, m_N, m_tsteps, &tn, s),
+              "b200_polybench_heat_3d");
+  };
+}
+
+void POLYBENCH_HEAT_3D::updateChecksum(VariantID vid, size_t tune_idx) {
+  checksum[vid][tune_idx] += calcChecksum(m_A, m_N * m_N * m_N, checksum_scale_factor, vid);
+  checksum[vid][tune_idx] += calcChecksum(m_B, m_N * m_N * m_N, checksum_scale_factor, vid);
+}
+
+void POLYBENCH_HEAT_3D::tearDown(VariantID vid, size_t) {
+  deallocData(m_A, vid);
+  deallocData(m_B, vid);
+  deallocData(m_Ainit, vid);
+  deallocData(m_Binit, vid);
+}
+
+}  // namespace polybench
+}  // namespace rajaperf

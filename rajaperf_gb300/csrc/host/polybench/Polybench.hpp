@@ -1,0 +1,41 @@
+// Polybench group kernels (suite src/polybench).
+#pragma once
+
+#include "common/KernelDecl.hpp"
+
+namespace rajaperf {
+namespace polybench {
+
+RAJAPERF_GB300_KERNEL(POLYBENCH_JACOBI_2D,
+ public:
+  void prepareRun(size_t tune_idx) override;
+ private:
+  Index_type m_N = 0, m_tsteps = 0;
+  Real_ptr m_A = nullptr, m_B = nullptr, m_Ainit = nullptr, m_Binit = nullptr;)
+
+RAJAPERF_GB300_KERNEL(POLYBENCH_HEAT_3D,
+ public:
+  void prepareRun(size_t tune_idx) override;
+ private:
+  Index_type m_N = 0, m_tsteps = 0;
+  Real_ptr m_A = nullptr, m_B = nullptr, m_Ainit = nullptr, m_Binit = nullptr;)
+
+RAJAPERF_GB300_KERNEL(POLYBENCH_FDTD_2D,
+ private:
+  Index_type m_nx = 0, m_ny = 0, m_tsteps = 0;
+  Real_ptr m_fict = nullptr, m_ex = nullptr, m_ey = nullptr, m_hz = nullptr;)
+
+RAJAPERF_GB300_KERNEL(POLYBENCH_GEMM,
+ private:
+  Index_type m_ni = 0, m_nj = 0, m_nk = 0;
+  Real_type m_alpha = 0.0, m_beta = 0.0;
+  Real_ptr m_A = nullptr, m_B = nullptr, m_C = nullptr;)
+
+RAJAPERF_GB300_KERNEL(POLYBENCH_3MM,
+ private:
+  Index_type m_ni = 0, m_nj = 0, m_nk = 0, m_nl = 0, m_nm = 0;
+  Real_ptr m_A = nullptr, m_B = nullptr, m_C = nullptr, m_D = nullptr, m_E = nullptr,
+           m_F = nullptr, m_G = nullptr;)
+
+}  // namespace polybench
+}  // namespace rajaperf

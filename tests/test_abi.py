@@ -25,7 +25,14 @@ def test_host_exports_header():
 
 def test_python_signatures_cover_header():
     names = rp.declared_functions("b200.h")
-    assert set(names) <= set(rp.B200_SIGNATURES), set(names) - set(rp.B200_SIGNATURES)
+    sigs = rp.parse_signatures("b200.h")
+    assert set(names) == set(sigs), set(names) ^ set(sigs)
+    args, res = sigs["b200_stream_triad"]
+    assert len(args) == 7 and res is ctypes.c_int
+    args, res = sigs["b200_apps_energy"]
+    assert len(args) == 22
+    assert sigs["b200_last_error_string"] == ([], ctypes.c_char_p)
+    assert sigs["b200_reduce_workspace_bytes"][1] is ctypes.c_size_t
 
 
 def test_tune_struct_layout():

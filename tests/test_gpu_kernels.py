@@ -1,0 +1,261 @@
+"""Element-wise checks of the C ABI against the CPU oracle on random inputs,
+including inputs the suite's own data never produce (signed ENERGY
+compression, ties and negative zeros for FIRST_MIN, ragged sizes)."""
+import ctypes
+
+import numpy as np
+import pytest
+
+import oracle
+import rajaperf_gb300 as rp
+from tests import gpu_util as gu
+
+pytestmark = pytest.mark.gpu
+
+
+def close(got, want, rtol=1e-12):
+    got = np.asarray(got)
+    want = np.asarray(want)
+    scale = max(float(np.max(np.abs(want))) if want.size else 0.0, 1e-300)
+    assert np.all(np.abs(got - want) <= rtol * np.maximum(np.abs(want), scale * 1e-3)), \
+        float(np.max(np.abs(got - want)))
+
+
+def dev(a):
+    return gu.dev(a)
+
+
+def ws(nbytes):
+    torch = gu.torch_cuda()
+    return torch.zeros(max(int(nbytes), 1), dtype=torch.uint8, device="cuda")
+
+
+L = None
+
+
+def lib():
+    global L
+    if L is None:
+        L = rp.b200()
+    return L
+
+
+@pytest.mark.parametrize("kn,jn", [(3, 3), (5, 7), (64, 65), (257, 300)])
+def test_hydro_2d(kn, jn):
+    rng = np.random.default_rng(kn * 1000 + jn)
+    arrs = [rng.uniform(0.5, 1.5, kn * jn) for _ in range(11)]
+    d = [dev(a) for a in arrs]
+    rp.check(lib().b200_lcals_hydro_2d(*[t.data_ptr() for t in d], 0.0041, 0.0037, kn, jn,
+                                       None, gu.stream()))
+    ref = [a.copy() for a in arrs]
+    oracle.call("oracle_hydro_2d_rep", *ref, 0.0041, 0.0037, kn, jn)
+    for g, w in zip(d, ref):
+        close(gu.host(g), w)
+
+
+def test_del_dot_vec_2d_irregular_zones():
+    rng = np.random.default_rng(3)
+    jp, nn = 37, 37 * 40
+    x, y, xd, yd = (rng.uniform(0.5, 1.5, nn) for _ in range(4))
+    div = np.zeros(nn)
+    zones = rng.permutation(np.arange(0, nn - jp - 1))[:500].astype(np.int64)
+    dd = dev(div)
+    rp.check(lib().b200_apps_del_dot_vec_2d(dev(x).data_ptr(), dev(y).data_ptr(),
+                                            dev(xd).data_ptr(), dev(yd).data_ptr(),
+                                            dd.data_ptr(), dev(zones).data_ptr(), zones.size,
+                                            jp, 1e-20, 0.5, None, gu.stream()))
+    oracle.call("oracle_del_dot_vec_2d_rep", x, y, xd, yd, div, zones, zones.size, jp,
+                1e-20, 0.5)
+    close(gu.host(dd), div)
+
+
+def test_vol3d_random_mesh():
+    rng = np.random.default_rng(4)
+    jp, kp = 11, 11 * 13
+    nn = kp * 9
+    x, y, z = (rng.uniform(0.0, 3.0, nn) for _ in range(3))
+    vol = np.zeros(nn)
+    ib, ie = 5, nn - kp - jp - 2
+    dv = dev(vol)
+    rp.check(lib().b200_apps_vol3d(dev(x).data_ptr(), dev(y).data_ptr(), dev(z).data_ptr(),
+                                   dv.data_ptr(), 1.0 / 12, jp, kp, ib, ie, None, gu.stream()))
+    oracle.call("oracle_vol3d_rep", x, y, z, vol, 1.0 / 12, jp, kp, ib, ie)
+    close(gu.host(dv), vol, rtol=1e-10)
+
+
+@pytest.mark.parametrize("n", [1, 33, 10007])
+def test_energy_all_branches(n):
+    rng = np.random.default_rng(n)
+    arrs = [rng.uniform(0.1, 1.5, n) for _ in range(15)]
+    arrs[2] = rng.uniform(-1.0, 1.0, n)       # delvc: both signs
+    arrs[12] = rng.uniform(-1.0, 1.0, n)      # ql_old
+    arrs[5] = np.zeros(n)                     # q_new
+    arrs[0] = np.zeros(n)                     # e_new
+    arrs[11][::7] = -5.0                      # pbvc: drive ssc <= tiny
+    scal = (0.3, 0.01, -0.5, 0.02)
+    d = [dev(a) for a in arrs]
+    rp.check(lib().b200_apps_energy(*[t.data_ptr() for t in d], *scal, n, None, gu.stream()))
+    ref = [a.copy() for a in arrs]
+    oracle.call("oracle_energy_rep", *ref, *scal, n)
+    close(gu.host(d[0]), ref[0], rtol=1e-11)
+    close(gu.host(d[5]), ref[5], rtol=1e-11)
+
+
+def test_pressure_clamps():
+    n = 5000
+    rng = np.random.default_rng(9)
+    comp = rng.uniform(-1.2, 1.0, n)
+    eold = rng.uniform(-1.0, 1.0, n)
+    vnew = rng.uniform(0.0, 2.0, n)
+    bvc = np.zeros(n)
+    pnew = np.zeros(n)
+    cls, p_cut, pmin, eosvmax = 0.2, 0.01, -0.05, 1.7
+    db, dp = dev(bvc), dev(pnew)
+    rp.check(lib().b200_apps_pressure(dev(comp).data_ptr(), db.data_ptr(), dp.data_ptr(),
+                                      dev(eold).data_ptr(), dev(vnew).data_ptr(), cls, p_cut,
+                                      pmin, eosvmax, n, None, gu.stream()))
+    b = cls * (comp + 1.0)
+    p = b * eold
+    p = np.where(np.abs(p) < p_cut, 0.0, p)
+    p = np.where(vnew >= eosvmax, 0.0, p)
+    p = np.where(p < pmin, pmin, p)
+    assert np.array_equal(gu.host(db), b)
+    close(gu.host(dp), p)
+
+
+@pytest.mark.parametrize("N,ts", [(3, 1), (10, 3), (129, 5)])
+def test_jacobi_heat(N, ts):
+    rng = np.random.default_rng(N)
+    A, B = rng.uniform(0.5, 1.5, N * N), rng.uniform(0.5, 1.5, N * N)
+    dA, dB = dev(A), dev(B)
+    rp.check(lib().b200_polybench_jacobi_2d(dA.data_ptr(), dB.data_ptr(), N, ts, None,
+                                            gu.stream()))
+    oracle.call("oracle_jacobi_2d", A, B, N, ts)
+    close(gu.host(dA), A)
+    close(gu.host(dB), B)
+    M = max(3, N // 4)
+    A3, B3 = rng.uniform(0.5, 1.5, M ** 3), rng.uniform(0.5, 1.5, M ** 3)
+    dA3, dB3 = dev(A3), dev(B3)
+    rp.check(lib().b200_polybench_heat_3d(dA3.data_ptr(), dB3.data_ptr(), M, ts, None,
+                                          gu.stream()))
+    oracle.call("oracle_heat_3d", A3, B3, M, ts)
+    close(gu.host(dA3), A3)
+    close(gu.host(dB3), B3)
+
+
+@pytest.mark.parametrize("nx,ny,ts", [(1, 1, 1), (2, 5, 2), (33, 65, 4), (200, 130, 3)])
+def test_fdtd_2d(nx, ny, ts):
+    rng = np.random.default_rng(nx + ny)
+    ex, ey, hz = (rng.uniform(0.5, 1.5, nx * ny) for _ in range(3))
+    fict = rng.uniform(0.5, 1.5, ts)
+    d = [dev(a) for a in (ex, ey, hz)]
+    rp.check(lib().b200_polybench_fdtd_2d(d[0].data_ptr(), d[1].data_ptr(), d[2].data_ptr(),
+                                          dev(fict).data_ptr(), nx, ny, ts, None, gu.stream()))
+    oracle.call("oracle_fdtd_2d", ex, ey, hz, fict, nx, ny, ts)
+    for g, w in zip(d, (ex, ey, hz)):
+        close(gu.host(g), w)
+
+
+@pytest.mark.parametrize("n", [1, 2, 4095, 4096, 4097, 100003, 1 << 21])
+def test_scan_f64_and_i64(n):
+    rng = np.random.default_rng(n)
+    x = rng.uniform(0.0, 1.0, n)
+    xi = rng.integers(0, 100, n).astype(np.int64)
+    wsb = lib().b200_scan_workspace_bytes(n)
+    w = ws(wsb)
+    torch = gu.torch_cuda()
+    dy = torch.zeros(n, dtype=torch.float64, device="cuda")
+    dyi = torch.zeros(n, dtype=torch.int64, device="cuda")
+    for rep in range(3):  # the workspace is reused across calls
+        rp.check(lib().b200_algorithm_scan(dev(x).data_ptr(), dy.data_ptr(), n, 0.25,
+                                           w.data_ptr(), wsb, None, gu.stream()))
+        rp.check(lib().b200_algorithm_scan_i64(dev(xi).data_ptr(), dyi.data_ptr(), n, 7,
+                                               w.data_ptr(), wsb, None, gu.stream()))
+        want_i = 7 + np.concatenate([[0], np.cumsum(xi)[:-1]])
+        assert np.array_equal(gu.host(dyi), want_i)
+        want = np.zeros(n)
+        oracle.call("oracle_scan_f64", x, want, n)
+        want += 0.25
+        got = gu.host(dy)
+        assert np.all(np.abs(got - want) <= (n + 64) * gu.U * (np.abs(want) + 0.25))
+    hdr = gu.host(w)[:24].view(np.uint32)
+    assert hdr[4] == 0, "lookback wait gave up"
+
+
+@pytest.mark.parametrize("case", ["planted", "ties", "first", "last", "negzero", "tiny"])
+def test_first_min_exact(case):
+    n = 1 << 20 if case != "tiny" else 1
+    rng = np.random.default_rng(1)
+    x = rng.uniform(0.5, 1.5, n)
+    if case == "planted":
+        x[123457] = -1e10
+    elif case == "ties":
+        x[999] = x[5000] = x[777777] = -2.0
+    elif case == "first":
+        x[0] = -3.0
+        x[100] = -3.0
+    elif case == "last":
+        x[-1] = -1.0
+    elif case == "negzero":
+        x[:] = 1.0
+        x[4000] = 0.0
+        x[300] = -0.0
+    want = int(np.argmin(x))
+    torch = gu.torch_cuda()
+    loc = torch.full((1,), -1, dtype=torch.int64, device="cuda")
+    val = torch.zeros(1, dtype=torch.float64, device="cuda")
+    wsb = lib().b200_reduce_workspace_bytes(n, None)
+    w = ws(wsb)
+    for _ in range(2):
+        rp.check(lib().b200_lcals_first_min(dev(x).data_ptr(), n, float(x[0]), 0,
+                                            loc.data_ptr(), val.data_ptr(), w.data_ptr(), wsb,
+                                            None, gu.stream()))
+        # strict '<' scan from (x[0], 0): the first index holding the minimum
+        seq_loc, seq_val = 0, x[0]
+        assert int(gu.host(loc)[0]) == want
+        assert float(gu.host(val)[0]) == float(x[want])
+    del seq_loc, seq_val
+
+
+@pytest.mark.parametrize("n", [0, 1, 1000, 1 << 22])
+def test_reduce_sum(n):
+    rng = np.random.default_rng(n)
+    x = rng.uniform(0.5, 1.5, n)
+    torch = gu.torch_cuda()
+    out = torch.zeros(1, dtype=torch.float64, device="cuda")
+    wsb = lib().b200_reduce_workspace_bytes(n, None)
+    w = ws(wsb)
+    rp.check(lib().b200_algorithm_reduce_sum(dev(x).data_ptr() if n else 0, n, 1.5,
+                                             out.data_ptr(), w.data_ptr(), wsb, None,
+                                             gu.stream()))
+    got = float(gu.host(out)[0])
+    want = 1.5 + float(np.sum(x))
+    assert abs(got - want) <= gu.reduction_bound(max(n, 1), 1, want)
+
+
+@pytest.mark.parametrize("m,n,k", [(1, 1, 1), (7, 5, 3), (64, 64, 64), (100, 130, 77),
+                                   (257, 129, 300)])
+def test_gemm_f64(m, n, k):
+    rng = np.random.default_rng(m * n * k)
+    A, B, C = rng.uniform(-1, 1, m * k), rng.uniform(-1, 1, k * n), rng.uniform(-1, 1, m * n)
+    dC = dev(C)
+    rp.check(lib().b200_gemm_f64(dev(A).data_ptr(), dev(B).data_ptr(), dC.data_ptr(), m, n, k,
+                                 1.5, 1.2, None, gu.stream()))
+    want = 1.5 * (A.reshape(m, k) @ B.reshape(k, n)) + 1.2 * C.reshape(m, n)
+    bound = (k + 2) * gu.U * (1.5 * (np.abs(A.reshape(m, k)) @ np.abs(B.reshape(k, n))) +
+                              1.2 * np.abs(C.reshape(m, n)))
+    assert np.all(np.abs(gu.host(dC).reshape(m, n) - want) <= bound)
+
+
+@pytest.mark.parametrize("fn,args", [
+    ("b200_lcals_eos", 8), ("b200_lcals_hydro_1d", 7), ("b200_lcals_first_diff", 3),
+])
+def test_null_pointer_rejected(fn, args):
+    f = getattr(lib(), fn)
+    argv = [None] * (len(f.argtypes))
+    for i, t in enumerate(f.argtypes):
+        if t is ctypes.c_double:
+            argv[i] = 1.0
+        elif t in (ctypes.c_int64, ctypes.c_long):
+            argv[i] = 16
+    assert f(*argv) == rp.B200_ERR_INVALID_ARG
