@@ -62,6 +62,7 @@ scan_kernel(const T* __restrict__ x, T* __restrict__ y, int64_t n, T init,
   __shared__ T s_tile[kScanTile + kScanTile / 16];
   __shared__ T s_warp[kScanBlock / 32];
   __shared__ T s_excl;
+  __shared__ T s_agg;
   __shared__ unsigned int s_tile_id;
   __shared__ unsigned long long s_epoch;
   __shared__ bool s_last;
@@ -86,15 +87,11 @@ scan_kernel(const T* __restrict__ x, T* __restrict__ y, int64_t n, T init,
   }
   __syncthreads();
 
-  // each thread scans its IT consecutive items
-  T v[kScanItems];
+  // Each thread sums its IT consecutive items; a block scan of the thread
+  // totals gives every thread its offset inside the tile.
   T run = T(0);
 #pragma unroll
-  for (int u = 0; u < kScanItems; ++u) {
-    v[u] = run;  // exclusive within the thread
-    run += s_tile[padded(tid * kScanItems + u)];
-  }
-  // block scan of thread totals
+  for (int u = 0; u < kScanItems; ++u) run += s_tile[padded(tid * kScanItems + u)];
   T incl = warp_inclusive_scan(run);
   if (lane == 31) s_warp[warp] = incl;
   __syncthreads();
@@ -102,16 +99,14 @@ scan_kernel(const T* __restrict__ x, T* __restrict__ y, int64_t n, T init,
     T w = (lane < kScanBlock / 32) ? s_warp[lane] : T(0);
     T wi = warp_inclusive_scan(w);
     if (lane < kScanBlock / 32) s_warp[lane] = wi - w;  // exclusive warp offsets
+    if (lane == kScanBlock / 32 - 1) s_agg = wi;         // tile aggregate
   }
   __syncthreads();
   const T thread_excl = s_warp[warp] + (incl - run);
-  // The tile aggregate is the last thread's inclusive total.
-  __syncthreads();
-  if (tid == kScanBlock - 1) s_warp[0] = thread_excl + run;
-  __syncthreads();
-  const T agg = s_warp[0];
+  const T agg = s_agg;
 
-  // decoupled lookback (warp 0)
+  // Warp 0 resolves the tile's prefix (decoupled lookback) while the other
+  // warps turn their items into tile-local exclusive prefixes in place.
   if (warp == 0) {
     T exclusive = init;
     if (tile == 0) {
@@ -168,16 +163,23 @@ scan_kernel(const T* __restrict__ x, T* __restrict__ y, int64_t n, T init,
     }
     if (lane == 0) s_excl = exclusive;
   }
-  __syncthreads();
-  const T prefix = s_excl + thread_excl;
+  {
+    T r = thread_excl;
 #pragma unroll
-  for (int u = 0; u < kScanItems; ++u) s_tile[padded(tid * kScanItems + u)] = prefix + v[u];
+    for (int u = 0; u < kScanItems; ++u) {
+      const int k = padded(tid * kScanItems + u);
+      const T xv = s_tile[k];
+      s_tile[k] = r;
+      r += xv;
+    }
+  }
   __syncthreads();
+  const T prefix = s_excl;
 #pragma unroll
   for (int u = 0; u < kScanItems; ++u) {
     int k = u * kScanBlock + tid;
     int64_t i = base + k;
-    if (i < n) y[i] = s_tile[padded(k)];
+    if (i < n) y[i] = prefix + s_tile[padded(k)];
   }
 
   // the last CTA to finish prepares the workspace for the next call

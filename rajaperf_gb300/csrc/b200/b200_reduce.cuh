@@ -19,7 +19,7 @@ struct ReduceWorkspace {
 };
 
 inline int reduce_grid(int64_t n, const b200_tune* t, int block, int items) {
-  int64_t cap = static_cast<int64_t>(device_info().sm_count) * 4;
+  int64_t cap = static_cast<int64_t>(device_info().sm_count) * 8;
   if (t && t->grid_blocks) cap = t->grid_blocks;
   int64_t tiles = ceil_div(n > 0 ? n : 1, static_cast<int64_t>(block) * items);
   if (tiles > cap) tiles = cap;
@@ -84,6 +84,60 @@ __device__ __forceinline__ MinLoc block_minloc(MinLoc v, MinLoc* smem) {
       o.val = __shfl_xor_sync(0xffffffffu, v.val, off);
       o.loc = __shfl_xor_sync(0xffffffffu, v.loc, off);
       v = minloc_pick(v, o);
+    }
+  }
+  __syncthreads();
+  return v;
+}
+
+// Min-loc over order-preserving integer keys of doubles.  On GB300 a double
+// compare issues on the (narrow) FP64 pipe; comparing keys runs on the
+// integer pipe.  key(x) orders exactly as '<' on doubles: -0.0 is folded onto
+// +0.0 (they compare equal) and NaN maps to the largest key (a NaN never
+// compares less, so it is never selected).
+__device__ __forceinline__ long long order_key(long long bits) {
+  if (bits == static_cast<long long>(0x8000000000000000ULL)) bits = 0;  // -0 -> +0
+  const long long mag = bits & 0x7fffffffffffffffLL;
+  if (mag > 0x7ff0000000000000LL) return 0x7fffffffffffffffLL;          // NaN
+  return bits ^ ((bits >> 63) & 0x7fffffffffffffffLL);
+}
+
+struct KeyLoc {
+  long long key;
+  long long loc;
+};
+
+__device__ __forceinline__ KeyLoc keyloc_pick(KeyLoc a, KeyLoc b) {
+  if (b.key < a.key) return b;
+  if (a.key < b.key) return a;
+  return (b.loc < a.loc) ? b : a;
+}
+
+template <int BS>
+__device__ __forceinline__ KeyLoc block_keyloc(KeyLoc v, KeyLoc* smem) {
+#pragma unroll
+  for (int off = 16; off > 0; off >>= 1) {
+    KeyLoc o;
+    o.key = __shfl_xor_sync(0xffffffffu, v.key, off);
+    o.loc = __shfl_xor_sync(0xffffffffu, v.loc, off);
+    v = keyloc_pick(v, o);
+  }
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  if (lane == 0) smem[warp] = v;
+  __syncthreads();
+  if (warp == 0) {
+    if (lane < BS / 32) {
+      v = smem[lane];
+    } else {
+      v.key = 0x7fffffffffffffffLL;
+      v.loc = 0x7fffffffffffffffLL;
+    }
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) {
+      KeyLoc o;
+      o.key = __shfl_xor_sync(0xffffffffu, v.key, off);
+      o.loc = __shfl_xor_sync(0xffffffffu, v.loc, off);
+      v = keyloc_pick(v, o);
     }
   }
   __syncthreads();

@@ -149,48 +149,54 @@ hydro2d_body23(const double* __restrict__ za, const double* __restrict__ zb,
 // ---- FIRST_MIN --------------------------------------------------------------
 // lcals/FIRST_MIN.hpp:29-54, FIRST_MIN-Seq.cpp:34-48: strict '<' scan, so the
 // result is the smallest index holding the minimum (or initloc when the
-// initial value is not beaten).
+// initial value is not beaten).  Compares run on order-preserving integer keys
+// (order_key), which order exactly as '<' on the doubles.
 template <int BS, int IT>
 __global__ void __launch_bounds__(BS)
 first_min_kernel(const double* __restrict__ x, int64_t n, double xmin_init,
                  int64_t initloc, int64_t* __restrict__ minloc_out,
-                 double* __restrict__ minval_out, MinLoc* __restrict__ partials,
+                 double* __restrict__ minval_out, KeyLoc* __restrict__ partials,
                  unsigned int* __restrict__ counter) {
-  __shared__ MinLoc smem[BS / 32];
+  __shared__ KeyLoc smem[BS / 32];
   __shared__ bool last_flag;
-  MinLoc m;
-  m.val = xmin_init;
-  m.loc = initloc;
+  const long long* xb = reinterpret_cast<const long long*>(x);
+  // A NaN initial value is never beaten by a strict '<' scan: give it the
+  // smallest key so that nothing compares less.
+  const KeyLoc init{isnan(xmin_init) ? static_cast<long long>(0x8000000000000000ULL)
+                                     : order_key(__double_as_longlong(xmin_init)),
+                    initloc};
+  KeyLoc m = init;
   for (int64_t t0 = static_cast<int64_t>(blockIdx.x) * (BS * IT); t0 < n;
        t0 += static_cast<int64_t>(gridDim.x) * (BS * IT)) {
-    double v[IT];
+    long long v[IT];
 #pragma unroll
     for (int u = 0; u < IT; ++u) {
       int64_t i = t0 + u * BS + threadIdx.x;
-      v[u] = (i < n) ? __ldg(x + i) : 0.0;
+      v[u] = (i < n) ? __ldg(xb + i) : 0LL;
     }
 #pragma unroll
     for (int u = 0; u < IT; ++u) {
       int64_t i = t0 + u * BS + threadIdx.x;
-      if (i < n && v[u] < m.val) { m.val = v[u]; m.loc = i; }
+      long long k = order_key(v[u]);
+      if (i < n && k < m.key) { m.key = k; m.loc = i; }
     }
   }
-  m = block_minloc<BS>(m, smem);
+  m = block_keyloc<BS>(m, smem);
   if (threadIdx.x == 0) partials[blockIdx.x] = m;
   if (arrive_last(counter, &last_flag)) {
-    MinLoc a;
-    a.val = xmin_init;
-    a.loc = initloc;
+    KeyLoc a = init;
     for (int i = threadIdx.x; i < static_cast<int>(gridDim.x); i += BS) {
-      MinLoc p;
-      p.val = __ldcg(&partials[i].val);
+      KeyLoc p;
+      p.key = __ldcg(&partials[i].key);
       p.loc = __ldcg(&partials[i].loc);
-      a = minloc_pick(a, p);
+      a = keyloc_pick(a, p);
     }
-    a = block_minloc<BS>(a, smem);
+    a = block_keyloc<BS>(a, smem);
     if (threadIdx.x == 0) {
       *minloc_out = a.loc;
-      if (minval_out) *minval_out = a.val;
+      if (minval_out) {
+        *minval_out = (a.loc == initloc && a.key == init.key) ? xmin_init : x[a.loc];
+      }
       *counter = 0u;
     }
   }
@@ -281,7 +287,7 @@ int b200_lcals_first_min(const double* x, int64_t n, double xmin_init, int64_t i
                          b200_stream_t stream) {
   if (n < 0 || (n > 0 && !x) || !minloc) return invalid("b200_lcals_first_min: bad args");
   int block = (tune && tune->block_size) ? tune->block_size : 256;
-  int items = (tune && tune->items) ? tune->items : 4;
+  int items = (tune && tune->items) ? tune->items : 8;
   if (!valid_block(block)) return invalid("b200_lcals_first_min: bad block size %d", block);
   int grid = reduce_grid(n, tune, block, items);
   size_t need = reduce_ws_bytes_for_grid(grid);
@@ -290,7 +296,7 @@ int b200_lcals_first_min(const double* x, int64_t n, double xmin_init, int64_t i
     return B200_ERR_WORKSPACE;
   }
   unsigned int* counter = static_cast<unsigned int*>(workspace);
-  MinLoc* partials = reinterpret_cast<MinLoc*>(static_cast<char*>(workspace) + 256);
+  KeyLoc* partials = reinterpret_cast<KeyLoc*>(static_cast<char*>(workspace) + 256);
   cudaStream_t st = as_stream(stream);
   B200_DISPATCH_BLOCK(block, BS, B200_DISPATCH_ITEMS(items, IT,
     first_min_kernel<BS, IT><<<grid, BS, 0, st>>>(x, n, xmin_init, initloc, minloc, minval,

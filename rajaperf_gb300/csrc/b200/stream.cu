@@ -296,9 +296,9 @@ int b200_stream_triad(double* a, const double* b, const double* c,
 
 size_t b200_reduce_workspace_bytes(int64_t n, const b200_tune* tune) {
   int block = (tune && tune->block_size) ? tune->block_size : kBlock;
-  int items = (tune && tune->items) ? tune->items : kItems;
-  // The scalar path tiles by block*items elements: the largest grid.
-  return reduce_ws_bytes_for_grid(reduce_grid(n, tune, block, items));
+  // The smallest tile (1 item per thread) gives the largest grid, so the
+  // workspace covers every reduction entry point and item count.
+  return reduce_ws_bytes_for_grid(reduce_grid(n, tune, block, 1));
 }
 
 int b200_stream_dot(const double* a, const double* b, int64_t n,

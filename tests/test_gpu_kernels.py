@@ -59,11 +59,12 @@ def test_del_dot_vec_2d_irregular_zones():
     x, y, xd, yd = (rng.uniform(0.5, 1.5, nn) for _ in range(4))
     div = np.zeros(nn)
     zones = rng.permutation(np.arange(0, nn - jp - 1))[:500].astype(np.int64)
-    dd = dev(div)
-    rp.check(lib().b200_apps_del_dot_vec_2d(dev(x).data_ptr(), dev(y).data_ptr(),
-                                            dev(xd).data_ptr(), dev(yd).data_ptr(),
-                                            dd.data_ptr(), dev(zones).data_ptr(), zones.size,
-                                            jp, 1e-20, 0.5, None, gu.stream()))
+    # keep every device buffer referenced until the kernel has run: a
+    # temporary's memory would be handed to the next allocation
+    dd, dx, dy, dxd, dyd, dz = dev(div), dev(x), dev(y), dev(xd), dev(yd), dev(zones)
+    rp.check(lib().b200_apps_del_dot_vec_2d(dx.data_ptr(), dy.data_ptr(), dxd.data_ptr(),
+                                            dyd.data_ptr(), dd.data_ptr(), dz.data_ptr(),
+                                            zones.size, jp, 1e-20, 0.5, None, gu.stream()))
     oracle.call("oracle_del_dot_vec_2d_rep", x, y, xd, yd, div, zones, zones.size, jp,
                 1e-20, 0.5)
     close(gu.host(dd), div)
@@ -76,8 +77,8 @@ def test_vol3d_random_mesh():
     x, y, z = (rng.uniform(0.0, 3.0, nn) for _ in range(3))
     vol = np.zeros(nn)
     ib, ie = 5, nn - kp - jp - 2
-    dv = dev(vol)
-    rp.check(lib().b200_apps_vol3d(dev(x).data_ptr(), dev(y).data_ptr(), dev(z).data_ptr(),
+    dv, dx, dy, dz = dev(vol), dev(x), dev(y), dev(z)
+    rp.check(lib().b200_apps_vol3d(dx.data_ptr(), dy.data_ptr(), dz.data_ptr(),
                                    dv.data_ptr(), 1.0 / 12, jp, kp, ib, ie, None, gu.stream()))
     oracle.call("oracle_vol3d_rep", x, y, z, vol, 1.0 / 12, jp, kp, ib, ie)
     close(gu.host(dv), vol, rtol=1e-10)
@@ -110,9 +111,9 @@ def test_pressure_clamps():
     bvc = np.zeros(n)
     pnew = np.zeros(n)
     cls, p_cut, pmin, eosvmax = 0.2, 0.01, -0.05, 1.7
-    db, dp = dev(bvc), dev(pnew)
-    rp.check(lib().b200_apps_pressure(dev(comp).data_ptr(), db.data_ptr(), dp.data_ptr(),
-                                      dev(eold).data_ptr(), dev(vnew).data_ptr(), cls, p_cut,
+    db, dp, dc, de, dvn = dev(bvc), dev(pnew), dev(comp), dev(eold), dev(vnew)
+    rp.check(lib().b200_apps_pressure(dc.data_ptr(), db.data_ptr(), dp.data_ptr(),
+                                      de.data_ptr(), dvn.data_ptr(), cls, p_cut,
                                       pmin, eosvmax, n, None, gu.stream()))
     b = cls * (comp + 1.0)
     p = b * eold
@@ -149,8 +150,9 @@ def test_fdtd_2d(nx, ny, ts):
     ex, ey, hz = (rng.uniform(0.5, 1.5, nx * ny) for _ in range(3))
     fict = rng.uniform(0.5, 1.5, ts)
     d = [dev(a) for a in (ex, ey, hz)]
+    df = dev(fict)
     rp.check(lib().b200_polybench_fdtd_2d(d[0].data_ptr(), d[1].data_ptr(), d[2].data_ptr(),
-                                          dev(fict).data_ptr(), nx, ny, ts, None, gu.stream()))
+                                          df.data_ptr(), nx, ny, ts, None, gu.stream()))
     oracle.call("oracle_fdtd_2d", ex, ey, hz, fict, nx, ny, ts)
     for g, w in zip(d, (ex, ey, hz)):
         close(gu.host(g), w)
@@ -166,10 +168,11 @@ def test_scan_f64_and_i64(n):
     torch = gu.torch_cuda()
     dy = torch.zeros(n, dtype=torch.float64, device="cuda")
     dyi = torch.zeros(n, dtype=torch.int64, device="cuda")
+    dx, dxi = dev(x), dev(xi)
     for rep in range(3):  # the workspace is reused across calls
-        rp.check(lib().b200_algorithm_scan(dev(x).data_ptr(), dy.data_ptr(), n, 0.25,
+        rp.check(lib().b200_algorithm_scan(dx.data_ptr(), dy.data_ptr(), n, 0.25,
                                            w.data_ptr(), wsb, None, gu.stream()))
-        rp.check(lib().b200_algorithm_scan_i64(dev(xi).data_ptr(), dyi.data_ptr(), n, 7,
+        rp.check(lib().b200_algorithm_scan_i64(dxi.data_ptr(), dyi.data_ptr(), n, 7,
                                                w.data_ptr(), wsb, None, gu.stream()))
         want_i = 7 + np.concatenate([[0], np.cumsum(xi)[:-1]])
         assert np.array_equal(gu.host(dyi), want_i)
@@ -182,7 +185,8 @@ def test_scan_f64_and_i64(n):
     assert hdr[4] == 0, "lookback wait gave up"
 
 
-@pytest.mark.parametrize("case", ["planted", "ties", "first", "last", "negzero", "tiny"])
+@pytest.mark.parametrize("case", ["planted", "ties", "first", "last", "negzero", "tiny",
+                                  "nan", "inf"])
 def test_first_min_exact(case):
     n = 1 << 20 if case != "tiny" else 1
     rng = np.random.default_rng(1)
@@ -200,21 +204,30 @@ def test_first_min_exact(case):
         x[:] = 1.0
         x[4000] = 0.0
         x[300] = -0.0
-    want = int(np.argmin(x))
+    elif case == "nan":
+        x[10:1000] = np.nan
+        x[77777] = -7.0
+    elif case == "inf":
+        x[5] = np.inf
+        x[6000] = -np.inf
+        x[7000] = -np.inf
+    # strict '<' scan from (x[0], 0), as the suite's loop
+    finite = np.where(np.isnan(x), np.inf, x)
+    cand = int(np.argmin(finite))
+    want = cand if finite[cand] < x[0] else 0
     torch = gu.torch_cuda()
     loc = torch.full((1,), -1, dtype=torch.int64, device="cuda")
     val = torch.zeros(1, dtype=torch.float64, device="cuda")
     wsb = lib().b200_reduce_workspace_bytes(n, None)
     w = ws(wsb)
+    dx = dev(x)
     for _ in range(2):
-        rp.check(lib().b200_lcals_first_min(dev(x).data_ptr(), n, float(x[0]), 0,
+        rp.check(lib().b200_lcals_first_min(dx.data_ptr(), n, float(x[0]), 0,
                                             loc.data_ptr(), val.data_ptr(), w.data_ptr(), wsb,
                                             None, gu.stream()))
-        # strict '<' scan from (x[0], 0): the first index holding the minimum
-        seq_loc, seq_val = 0, x[0]
         assert int(gu.host(loc)[0]) == want
-        assert float(gu.host(val)[0]) == float(x[want])
-    del seq_loc, seq_val
+        got_val = float(gu.host(val)[0])
+        assert got_val == float(x[want]) or (np.isnan(got_val) and np.isnan(x[want]))
 
 
 @pytest.mark.parametrize("n", [0, 1, 1000, 1 << 22])
@@ -225,7 +238,8 @@ def test_reduce_sum(n):
     out = torch.zeros(1, dtype=torch.float64, device="cuda")
     wsb = lib().b200_reduce_workspace_bytes(n, None)
     w = ws(wsb)
-    rp.check(lib().b200_algorithm_reduce_sum(dev(x).data_ptr() if n else 0, n, 1.5,
+    dx = dev(x)
+    rp.check(lib().b200_algorithm_reduce_sum(dx.data_ptr() if n else 0, n, 1.5,
                                              out.data_ptr(), w.data_ptr(), wsb, None,
                                              gu.stream()))
     got = float(gu.host(out)[0])
@@ -238,8 +252,8 @@ def test_reduce_sum(n):
 def test_gemm_f64(m, n, k):
     rng = np.random.default_rng(m * n * k)
     A, B, C = rng.uniform(-1, 1, m * k), rng.uniform(-1, 1, k * n), rng.uniform(-1, 1, m * n)
-    dC = dev(C)
-    rp.check(lib().b200_gemm_f64(dev(A).data_ptr(), dev(B).data_ptr(), dC.data_ptr(), m, n, k,
+    dA, dB, dC = dev(A), dev(B), dev(C)
+    rp.check(lib().b200_gemm_f64(dA.data_ptr(), dB.data_ptr(), dC.data_ptr(), m, n, k,
                                  1.5, 1.2, None, gu.stream()))
     want = 1.5 * (A.reshape(m, k) @ B.reshape(k, n)) + 1.2 * C.reshape(m, n)
     bound = (k + 2) * gu.U * (1.5 * (np.abs(A.reshape(m, k)) @ np.abs(B.reshape(k, n))) +
