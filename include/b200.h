@@ -299,6 +299,22 @@ int b200_gemm_f64(const double* A, const double* B, double* C, int64_t m,
                   int64_t n, int64_t k, double alpha, double beta,
                   const b200_tune* tune, b200_stream_t stream);
 
+/* Workspace for b200_gemm_split (slices and scales of A and B). */
+size_t b200_gemm_split_workspace_bytes(int64_t m, int64_t n, int64_t k,
+                                       const b200_tune* tune);
+
+/* C = alpha*A*B + beta*C in FP64 by split precision on bf16 tensor cores:
+ * rows of A / columns of B are scaled by powers of two and cut into
+ * tune->items (default 11) balanced 5-bit integer slices held exactly in
+ * bf16; slice products of equal weight accumulate exactly in FP32 on the
+ * tensor cores; the weighted sum is formed in FP64.  k <= 8192 (the bound
+ * under which the FP32 accumulation stays exact).  Not in the reference: the
+ * split-precision form of polybench/POLYBENCH_GEMM.hpp:40-56.              */
+int b200_gemm_split(const double* A, const double* B, double* C, int64_t m,
+                    int64_t n, int64_t k, double alpha, double beta,
+                    void* workspace, size_t workspace_bytes,
+                    const b200_tune* tune, b200_stream_t stream);
+
 /* ---- Algorithm ---------------------------------------------------------- */
 
 /* Workspace for b200_algorithm_scan / _scan_i64 on n elements. */

@@ -33,10 +33,22 @@ POLYBENCH_3MM::POLYBENCH_3MM(const RunParams& params)
                                          getActualProblemSize());
   setComplexity(Complexity::N_to_the_three_halves);
   setUsesFeature(Kernel);
+  addTuning("split_bf16", b200_tune{}, false);
+  addTuning("split_bf16_graph", b200_tune{}, true);
   setVariantDefined(Base_GB300);
 }
 
-void POLYBENCH_3MM::setUp(VariantID vid, size_t) {
+bool POLYBENCH_3MM::isSplit(size_t tune_idx) const {
+  return getVariantTuningName(Base_GB300, tune_idx).rfind("split", 0) == 0;
+}
+
+void POLYBENCH_3MM::setUp(VariantID vid, size_t tune_idx) {
+  if (isSplit(tune_idx)) {
+    m_ws_bytes = std::max(std::max(b200_gemm_split_workspace_bytes(m_ni, m_nj, m_nk, nullptr),
+                                   b200_gemm_split_workspace_bytes(m_nj, m_nl, m_nm, nullptr)),
+                          b200_gemm_split_workspace_bytes(m_ni, m_nl, m_nj, nullptr));
+    m_ws = allocDeviceBytes(m_ws_bytes);
+  }
   allocAndInitData(m_A, m_ni * m_nk, vid);
   allocAndInitData(m_B, m_nk * m_nj, vid);
   allocAndInitData(m_C, m_nj * m_nm, vid);
@@ -48,6 +60,16 @@ void POLYBENCH_3MM::setUp(VariantID vid, size_t) {
 
 KernelBase::RepBody POLYBENCH_3MM::makeRepBody(size_t tune_idx) {
   const b200_tune tn = getTune(tune_idx);
+  if (isSplit(tune_idx)) {
+    return [=](b200_stream_t s) {
+      checkB200(b200_gemm_split(m_A, m_B, m_E, m_ni, m_nj, m_nk, 1.0, 0.0, m_ws, m_ws_bytes,
+                                nullptr, s), "b200_gemm_split");
+      checkB200(b200_gemm_split(m_C, m_D, m_F, m_nj, m_nl, m_nm, 1.0, 0.0, m_ws, m_ws_bytes,
+                                nullptr, s), "b200_gemm_split");
+      checkB200(b200_gemm_split(m_E, m_F, m_G, m_ni, m_nl, m_nj, 1.0, 0.0, m_ws, m_ws_bytes,
+                                nullptr, s), "b200_gemm_split");
+    };
+  }
   return [=](b200_stream_t s) {
     checkB200(b200_polybench_3mm(m_A, m_B, m_C, m_D, m_E, m_F, m_G, m_ni, m_nj, m_nk, m_nl,
                                  m_nm, &tn, s),
@@ -61,6 +83,8 @@ void POLYBENCH_3MM::updateChecksum(VariantID vid, size_t tune_idx) {
 
 void POLYBENCH_3MM::tearDown(VariantID vid, size_t) {
   for (Real_ptr* p : {&m_A, &m_B, &m_C, &m_D, &m_E, &m_F, &m_G}) deallocData(*p, vid);
+  deallocDeviceBytes(m_ws);
+  m_ws = nullptr;
 }
 
 }  // namespace polybench

@@ -29,17 +29,35 @@ POLYBENCH_GEMM::POLYBENCH_GEMM(const RunParams& params)
                                    getActualProblemSize());
   setComplexity(Complexity::N_to_the_three_halves);
   setUsesFeature(Kernel);
+  addTuning("split_bf16", b200_tune{}, false);
+  addTuning("split_bf16_graph", b200_tune{}, true);
   setVariantDefined(Base_GB300);
 }
 
-void POLYBENCH_GEMM::setUp(VariantID vid, size_t) {
+bool POLYBENCH_GEMM::isSplit(size_t tune_idx) const {
+  return getVariantTuningName(Base_GB300, tune_idx).rfind("split", 0) == 0;
+}
+
+void POLYBENCH_GEMM::setUp(VariantID vid, size_t tune_idx) {
   allocAndInitData(m_A, m_ni * m_nk, vid);
   allocAndInitData(m_B, m_nk * m_nj, vid);
   allocAndInitDataConst(m_C, m_ni * m_nj, 0.0, vid);
+  if (isSplit(tune_idx)) {
+    m_ws_bytes = b200_gemm_split_workspace_bytes(m_ni, m_nj, m_nk, nullptr);
+    m_ws = allocDeviceBytes(m_ws_bytes);
+  }
 }
 
 KernelBase::RepBody POLYBENCH_GEMM::makeRepBody(size_t tune_idx) {
   const b200_tune tn = getTune(tune_idx);
+  if (isSplit(tune_idx)) {
+    // C = alpha*A*B (the suite's beta scaling is overwritten by BODY4)
+    return [=](b200_stream_t s) {
+      checkB200(b200_gemm_split(m_A, m_B, m_C, m_ni, m_nj, m_nk, m_alpha, 0.0, m_ws,
+                                m_ws_bytes, nullptr, s),
+                "b200_gemm_split");
+    };
+  }
   return [=](b200_stream_t s) {
     checkB200(b200_polybench_gemm(m_A, m_B, m_C, m_ni, m_nj, m_nk, m_alpha, &tn, s),
               "b200_polybench_gemm");
@@ -54,6 +72,8 @@ void POLYBENCH_GEMM::tearDown(VariantID vid, size_t) {
   deallocData(m_A, vid);
   deallocData(m_B, vid);
   deallocData(m_C, vid);
+  deallocDeviceBytes(m_ws);
+  m_ws = nullptr;
 }
 
 }  // namespace polybench

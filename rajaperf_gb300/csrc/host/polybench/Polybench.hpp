@@ -25,17 +25,26 @@ RAJAPERF_GB300_KERNEL(POLYBENCH_FDTD_2D,
   Index_type m_nx = 0, m_ny = 0, m_tsteps = 0;
   Real_ptr m_fict = nullptr, m_ex = nullptr, m_ey = nullptr, m_hz = nullptr;)
 
+// GEMM and 3MM tunings: "default"/"graph" run the native FP64 kernel;
+// "split_bf16"/"split_bf16_graph" run the split-precision tensor-core GEMM
+// (b200_gemm_split; inner dimensions up to 8192).
 RAJAPERF_GB300_KERNEL(POLYBENCH_GEMM,
  private:
+  bool isSplit(size_t tune_idx) const;
   Index_type m_ni = 0, m_nj = 0, m_nk = 0;
   Real_type m_alpha = 0.0, m_beta = 0.0;
-  Real_ptr m_A = nullptr, m_B = nullptr, m_C = nullptr;)
+  Real_ptr m_A = nullptr, m_B = nullptr, m_C = nullptr;
+  void* m_ws = nullptr;
+  size_t m_ws_bytes = 0;)
 
 RAJAPERF_GB300_KERNEL(POLYBENCH_3MM,
  private:
+  bool isSplit(size_t tune_idx) const;
   Index_type m_ni = 0, m_nj = 0, m_nk = 0, m_nl = 0, m_nm = 0;
   Real_ptr m_A = nullptr, m_B = nullptr, m_C = nullptr, m_D = nullptr, m_E = nullptr,
-           m_F = nullptr, m_G = nullptr;)
+           m_F = nullptr, m_G = nullptr;
+  void* m_ws = nullptr;
+  size_t m_ws_bytes = 0;)
 
 }  // namespace polybench
 }  // namespace rajaperf

@@ -1,0 +1,98 @@
+"""Split-precision FP64 GEMM (b200_gemm_split) against an FP64 reference.
+
+The bound asked of it is a relative Frobenius error of 1e-13 against FP64;
+the test states it per case, including rows scaled by 2^k, k in [-20, 20]
+(the slicing is per row/column, so row scaling must not cost accuracy)."""
+import numpy as np
+import pytest
+
+import rajaperf_gb300 as rp
+from tests import gpu_util as gu
+
+pytestmark = pytest.mark.gpu
+
+REL_FROB = 1e-13
+
+
+def run_split(A, B, C, alpha, beta, slices=None):
+    torch = gu.torch_cuda()
+    m, k = A.shape
+    n = B.shape[1]
+    L = rp.b200()
+    t = rp.Tune(items=slices) if slices else None
+    tp = None
+    import ctypes
+    if t is not None:
+        tp = ctypes.byref(t)
+    ws_bytes = L.b200_gemm_split_workspace_bytes(m, n, k, tp)
+    ws = torch.zeros(ws_bytes, dtype=torch.uint8, device="cuda")
+    dA, dB, dC = gu.dev(A.ravel()), gu.dev(B.ravel()), gu.dev(C.ravel())
+    rp.check(L.b200_gemm_split(dA.data_ptr(), dB.data_ptr(), dC.data_ptr(), m, n, k, alpha,
+                               beta, ws.data_ptr(), ws_bytes, tp, gu.stream()), "gemm_split")
+    return gu.host(dC).reshape(m, n)
+
+
+def reference(A, B, C, alpha, beta):
+    # float128-free check: numpy FP64 matmul is itself accurate to ~k*u|A||B|,
+    # well inside the 1e-13 target at these sizes
+    return alpha * (A @ B) + beta * C
+
+
+@pytest.mark.parametrize("m,n,k", [(1, 1, 1), (5, 7, 3), (128, 128, 32), (130, 257, 200),
+                                   (256, 256, 1024), (64, 96, 8192)])
+def test_split_matches_fp64(m, n, k):
+    rng = np.random.default_rng(m + n + k)
+    A, B, C = rng.uniform(-1, 1, (m, k)), rng.uniform(-1, 1, (k, n)), rng.uniform(-1, 1, (m, n))
+    got = run_split(A, B, C, 1.5, 1.2)
+    want = reference(A, B, C, 1.5, 1.2)
+    err = np.linalg.norm(got - want) / np.linalg.norm(want)
+    assert err <= REL_FROB, err
+
+
+def test_split_row_scaled():
+    rng = np.random.default_rng(7)
+    m = n = 256
+    k = 512
+    A = rng.uniform(-1, 1, (m, k)) * np.exp2(rng.integers(-20, 21, m))[:, None]
+    B = rng.uniform(-1, 1, (k, n))
+    C = rng.uniform(-1, 1, (m, n))
+    got = run_split(A, B, C, 1.5, 1.2)
+    want = reference(A, B, C, 1.5, 1.2)
+    err = np.linalg.norm(got - want) / np.linalg.norm(want)
+    assert err <= REL_FROB, err
+    # per row, relative to that row's own scale
+    row_err = np.linalg.norm(got - want, axis=1) / np.linalg.norm(want, axis=1)
+    assert np.max(row_err) <= 10 * REL_FROB
+
+
+def test_split_nonnegative_worst_case_accumulation():
+    """All-positive data maximises the FP32 partial sums; the result must
+    still meet the bound at the largest K the entry point accepts."""
+    rng = np.random.default_rng(3)
+    m = n = 64
+    k = 8192
+    A, B = rng.uniform(0, 1, (m, k)), rng.uniform(0, 1, (k, n))
+    C = np.zeros((m, n))
+    got = run_split(A, B, C, 1.0, 0.0)
+    want = A @ B
+    err = np.linalg.norm(got - want) / np.linalg.norm(want)
+    assert err <= REL_FROB, err
+
+
+def test_split_fewer_slices_is_less_accurate():
+    rng = np.random.default_rng(11)
+    A, B = rng.uniform(-1, 1, (128, 256)), rng.uniform(-1, 1, (256, 128))
+    C = np.zeros((128, 128))
+    want = A @ B
+    e4 = np.linalg.norm(run_split(A, B, C, 1.0, 0.0, slices=4) - want) / np.linalg.norm(want)
+    e11 = np.linalg.norm(run_split(A, B, C, 1.0, 0.0) - want) / np.linalg.norm(want)
+    assert e11 < e4
+    assert 1e-9 < e4 < 1e-3
+
+
+def test_split_rejects_large_k():
+    torch = gu.torch_cuda()
+    L = rp.b200()
+    x = torch.zeros(16, dtype=torch.float64, device="cuda")
+    assert L.b200_gemm_split(x.data_ptr(), x.data_ptr(), x.data_ptr(), 1, 1, 8193, 1.0, 0.0,
+                             x.data_ptr(), 128, None, None) == rp.B200_ERR_INVALID_ARG

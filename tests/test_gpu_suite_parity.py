@@ -43,7 +43,17 @@ def test_kernel_matches_suite_base_seq(kernel):
     for rec in [r for r in RECORDS if r["kernel"] == kernel]:
         res = rp.run_suite(["--size", rec["size"], "--checkrun", rec["reps"], "-k", kernel,
                             "-t", "default", "graph", "--disable-warmup"])
-        assert {r["tuning"] for r in res} == {"default", "graph"}
+        assert {r["tuning"] for r in res} == {"default", "graph"}, res
+        for r in res:
+            _check(kernel, rec, r)
+
+
+@pytest.mark.parametrize("kernel", ["Polybench_GEMM", "Polybench_3MM"])
+def test_split_precision_tunings_match_base_seq(kernel):
+    for rec in [r for r in RECORDS if r["kernel"] == kernel]:
+        res = rp.run_suite(["--size", rec["size"], "--checkrun", rec["reps"], "-k", kernel,
+                            "-t", "split_bf16", "split_bf16_graph", "--disable-warmup"])
+        assert len(res) == 2
         for r in res:
             _check(kernel, rec, r)
 
