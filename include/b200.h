@@ -154,6 +154,23 @@ int b200_stream_dot(const double* a, const double* b, int64_t n,
                     size_t workspace_bytes, const b200_tune* tune,
                     b200_stream_t stream);
 
+/* The same dot product for callers that cannot allocate device memory where
+ * they need it -- code whose device heap is owned by someone else (a
+ * framework's caching allocator, a fixed arena) or a latency-critical loop
+ * that must not pay cudaMalloc's implicit synchronisation.  No counterpart in
+ * the reference.  The scratch is a library-owned __device__ array of
+ * b200_stream_dot_static_max_scratch_bytes() bytes (room for 4096 CTAs),
+ * held by every GPU that loads the library until the process exits; a launch
+ * shape needing more returns B200_ERR_WORKSPACE.  The call allocates nothing
+ * and clears the scratch counter itself.  All calls share the array, so
+ * calls that overlap on the GPU race and must be ordered by the caller.  The
+ * first call on a device looks the array's address up (cudaGetSymbolAddress)
+ * and should come before any stream capture that contains this call. */
+size_t b200_stream_dot_static_max_scratch_bytes(void);
+int b200_stream_dot_static(const double* a, const double* b, int64_t n,
+                           double dot_init, double* dot_accum,
+                           const b200_tune* tune, b200_stream_t stream);
+
 /* ---- Basic (kernels of the batched small-size suite) --------------------- */
 
 /* y[i] += a*x[i]                   -- basic/DAXPY.hpp, DAXPY-Cuda.cpp        */
