@@ -611,6 +611,67 @@ def run_gpu(args, rank, world):
     }
 
 
+def measure_gemm(torch, rp, stream, sizes=(1024, 4096, 8192), seed=4793):
+    """Square C = 1.5*A*B + 1.2*C, entries uniform in [-1, 1): native FP64
+    (b200_gemm_f64) against split precision (b200_gemm_split), TFLOP/s at
+    2*N^3 and the split result's relative Frobenius error against the native
+    FP64 result; plus a variant with rows of A scaled by 2^k, k in [-20, 20]."""
+    L = rp.b200()
+    s = stream.cuda_stream
+    out = []
+    for n in sizes:
+        g = torch.Generator(device="cuda").manual_seed(seed + n)
+        A = torch.rand(n, n, dtype=torch.float64, device="cuda", generator=g) * 2 - 1
+        B = torch.rand(n, n, dtype=torch.float64, device="cuda", generator=g) * 2 - 1
+        C0 = torch.rand(n, n, dtype=torch.float64, device="cuda", generator=g) * 2 - 1
+        ws_bytes = L.b200_gemm_split_workspace_bytes(n, n, n, None)
+        ws = torch.empty(ws_bytes, dtype=torch.uint8, device="cuda")
+        res = {"n": n}
+        for name, fn in (("native", lambda C: L.b200_gemm_f64(A.data_ptr(), B.data_ptr(),
+                                                             C.data_ptr(), n, n, n, 1.5, 1.2,
+                                                             None, s)),
+                         ("split", lambda C: L.b200_gemm_split(A.data_ptr(), B.data_ptr(),
+                                                               C.data_ptr(), n, n, n, 1.5, 1.2,
+                                                               ws.data_ptr(), ws_bytes, None,
+                                                               s))):
+            C = C0.clone()
+            rp.check(fn(C), name)  # warm-up
+            reps = 1 if (name == "native" and n >= 8192) else 3
+            best = None
+            for _ in range(reps):
+                C = C0.clone()
+                e0 = torch.cuda.Event(enable_timing=True)
+                e1 = torch.cuda.Event(enable_timing=True)
+                e0.record(stream)
+                rp.check(fn(C), name)
+                e1.record(stream)
+                torch.cuda.synchronize()
+                t = e0.elapsed_time(e1) / 1e3
+                best = t if best is None else min(best, t)
+            res[f"{name}_ms"] = round(best * 1e3, 3)
+            res[f"{name}_tflops"] = round(2.0 * n ** 3 / best / 1e12, 3)
+            res[f"C_{name}"] = C
+        err = (res["C_split"] - res["C_native"]).norm() / res["C_native"].norm()
+        res["rel_err_vs_fp64"] = float(err)
+        res["speedup"] = round(res["split_tflops"] / res["native_tflops"], 2)
+        del res["C_split"], res["C_native"]
+        if n == sizes[-1] or n <= 4096:
+            # row-scaled variant (accuracy only)
+            k = torch.randint(-20, 21, (n, 1), device="cuda", generator=g).to(torch.float64)
+            As = A * torch.exp2(k)
+            Cn, Cs = C0.clone(), C0.clone()
+            rp.check(L.b200_gemm_f64(As.data_ptr(), B.data_ptr(), Cn.data_ptr(), n, n, n, 1.5,
+                                     1.2, None, s))
+            rp.check(L.b200_gemm_split(As.data_ptr(), B.data_ptr(), Cs.data_ptr(), n, n, n,
+                                       1.5, 1.2, ws.data_ptr(), ws_bytes, None, s))
+            torch.cuda.synchronize()
+            res["row_scaled_rel_err"] = float((Cs - Cn).norm() / Cn.norm())
+        out.append(res)
+        del A, B, C0, ws
+        torch.cuda.empty_cache()
+    return out
+
+
 def measure_fp64_peak(torch, rp, stream):
     """FP64 FMA rate of this GPU from the library's probe (best of 3)."""
     L = rp.b200()
@@ -622,7 +683,7 @@ def measure_fp64_peak(torch, rp, stream):
         e0 = torch.cuda.Event(enable_timing=True)
         e1 = torch.cuda.Event(enable_timing=True)
         e0.record(stream)
-        rp.check(L.b200_probe_dfma(out.data_ptr(), 2048, ctypes.byref(cnt), stream.cuda_stream))
+        rp.check(L.b200_probe_dfma(out.data_ptr(), 512, ctypes.byref(cnt), stream.cuda_stream))
         e1.record(stream)
         torch.cuda.synchronize()
         rate = cnt.value / (e0.elapsed_time(e1) / 1e3)
@@ -707,6 +768,9 @@ def main():
                     help="skip the host-buffer end-to-end leg")
     ap.add_argument("--kernels", type=lambda s: s.split(","), default=None,
                     help="comma list: run only these kernels of the workload")
+    ap.add_argument("--gemm", choices=["auto", "on", "off"], default="auto",
+                    help="split-precision vs native FP64 GEMM leg (auto: on for the "
+                         "default workload without --kernels)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3) if args.impl == "gb300" else args.warmup
     rank = int(os.environ.get("RANK", "0"))
@@ -747,6 +811,11 @@ def main():
 
     res = run_gpu(args, rank, world)
     dist = res.pop("dist")
+    gemm = None
+    if args.gemm == "on" or (args.gemm == "auto" and not args.kernels and rank == 0):
+        import torch
+        import rajaperf_gb300 as rp
+        gemm = measure_gemm(torch, rp, torch.cuda.current_stream())
     value = res["value"]
     if dist:
         import torch
@@ -772,6 +841,7 @@ def main():
         "config": config, "e2e": res["e2e"], "roofline": res["roofline"],
         "cpu_baseline": cpu, "clocks": res["clocks"], "gpu_launches": res["launches"],
         "fp64_peak_gflops": round(res["fp64"]["gflops"], 1),
+        "gemm_split_vs_fp64": gemm,
         "per_kernel": [{k: (round(v, 4) if isinstance(v, float) else v) for k, v in p.items()}
                        for p in res["per_kernel"]],
     }

@@ -86,7 +86,7 @@ int b200_device_caps(b200_caps* out);
 /* Number of kernels this library has launched since it was loaded. */
 int64_t b200_launch_count(void);
 
-/* FP64 pipe probe: launches 8 independent fma chains of `iters` steps in
+/* FP64 pipe probe: launches 16 independent fma chains of `iters` steps in
  * each of b200_probe_dfma_threads() threads (out must hold that many
  * doubles) and reports the number of fused multiply-adds issued.  Timing the
  * launch gives the device's FP64 FMA rate, the roofline of the FP64-bound
@@ -94,6 +94,14 @@ int64_t b200_launch_count(void);
 int64_t b200_probe_dfma_threads(void);
 int b200_probe_dfma(double* out, int32_t iters, int64_t* fma_count,
                     b200_stream_t stream);
+
+/* Self-test of the integer-pipe FP64 arithmetic used by the mixed-pipe
+ * stencils: n operand pairs from `seed` (arbitrary bit patterns, close and
+ * distant exponents, range edges, [0.5, 1.5)), op 0 = add, 1 = sub, 2 = mul;
+ * adds to *mismatches (device) the number of results whose bits differ from
+ * the FP64 pipe's.  Not in the reference. */
+int b200_f64emu_selftest(int64_t n, uint64_t seed, int32_t op,
+                         unsigned long long* mismatches, b200_stream_t stream);
 
 /* ---- data initialisation (DataUtils.cpp) -------------------------------- */
 
@@ -280,12 +288,17 @@ int b200_apps_del_dot_vec_2d(const double* x, const double* y,
 /* ---- Polybench ---------------------------------------------------------- */
 
 /* tsteps x (B <- 5-point average of A, then A <- of B) on an N x N grid
- *   -- polybench/POLYBENCH_JACOBI_2D.hpp:38-44, -Cuda.cpp:86-114            */
+ *   -- polybench/POLYBENCH_JACOBI_2D.hpp:38-44, -Cuda.cpp:86-114
+ * tune->algo > 0 selects the mixed-pipe kernel: algo-1 of every 8 warps run
+ * bit-identical integer-pipe FP64 (rows per warp: tile_y emulated, tile_z
+ * native).                                                                  */
 int b200_polybench_jacobi_2d(double* A, double* B, int64_t N, int64_t tsteps,
                              const b200_tune* tune, b200_stream_t stream);
 
 /* tsteps x (B <- 7-point heat update of A, then A <- of B) on N^3
- *   -- polybench/POLYBENCH_HEAT_3D.hpp:47-82, -Cuda.cpp:97-113              */
+ *   -- polybench/POLYBENCH_HEAT_3D.hpp:47-82, -Cuda.cpp:97-113
+ * tune->algo > 0 selects the mixed-pipe kernel as for JACOBI_2D (tile_x =
+ * planes per CTA).                                                          */
 int b200_polybench_heat_3d(double* A, double* B, int64_t N, int64_t tsteps,
                            const b200_tune* tune, b200_stream_t stream);
 

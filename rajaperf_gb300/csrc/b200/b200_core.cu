@@ -1,5 +1,6 @@
 // libb200 core: error state, launch accounting, device properties, tuning
 // resolution and the data-initialisation kernels.
+#include "b200_f64emu.cuh"
 #include "b200_internal.cuh"
 
 #include <mutex>
@@ -261,18 +262,22 @@ int b200_init_uniform_i64(int64_t* p, int64_t n, uint64_t seed,
 
 namespace {
 
-// Eight independent FMA chains per thread; out[] receives one value per thread
-// so the chains are live.  `out` must hold probe_threads() doubles.
+// Sixteen independent FMA chains per thread (enough to cover the pipe's
+// latency at full occupancy); out[] receives one value per thread so the
+// chains are live.  `out` must hold probe_threads() doubles.
 __global__ void __launch_bounds__(256) dfma_probe_kernel(double* out, double a, double b,
                                                          int iters) {
-  double x0 = threadIdx.x * 1e-3, x1 = x0 + 1, x2 = x0 + 2, x3 = x0 + 3;
-  double x4 = x0 + 4, x5 = x0 + 5, x6 = x0 + 6, x7 = x0 + 7;
+  double x[16];
+#pragma unroll
+  for (int c = 0; c < 16; ++c) x[c] = threadIdx.x * 1e-3 + c;
   for (int i = 0; i < iters; ++i) {
-    x0 = fma(x0, a, b); x1 = fma(x1, a, b); x2 = fma(x2, a, b); x3 = fma(x3, a, b);
-    x4 = fma(x4, a, b); x5 = fma(x5, a, b); x6 = fma(x6, a, b); x7 = fma(x7, a, b);
+#pragma unroll
+    for (int c = 0; c < 16; ++c) x[c] = fma(x[c], a, b);
   }
-  out[static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x] =
-      x0 + x1 + x2 + x3 + x4 + x5 + x6 + x7;
+  double s = 0.0;
+#pragma unroll
+  for (int c = 0; c < 16; ++c) s += x[c];
+  out[static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x] = s;
 }
 
 }  // namespace
@@ -287,8 +292,79 @@ int b200_probe_dfma(double* out, int32_t iters, int64_t* fma_count, b200_stream_
   if (!out || iters <= 0 || !fma_count) return invalid("b200_probe_dfma: bad args");
   int blocks = device_info().sm_count * 8;
   dfma_probe_kernel<<<blocks, 256, 0, as_stream(stream)>>>(out, 0.999999, 1e-7, iters);
-  *fma_count = static_cast<int64_t>(blocks) * 256 * 8 * iters;
+  *fma_count = static_cast<int64_t>(blocks) * 256 * 16 * iters;
   return after_launch("b200_probe_dfma");
 }
 
 }  // extern "C"
+
+// ---- integer-pipe FP64 self-test ------------------------------------------------
+
+namespace {
+
+__device__ __forceinline__ uint64_t rnd64(uint64_t seed, uint64_t i) {
+  return mix64(mix64(seed + 0x9e3779b97f4a7c15ULL * (i + 1)) ^ 0x5bd1e995ULL);
+}
+
+// Operand pairs from five families: arbitrary bit patterns (every class,
+// NaNs and infinities included), nearby exponents (cancellation), exponents
+// far apart (sticky), values near the overflow / underflow edges, and
+// uniform [0.5, 1.5).  Counts results whose bits differ from the FP64 pipe's
+// (two NaNs count as equal).
+__global__ void f64emu_check_kernel(int64_t n, uint64_t seed, int op,
+                                    unsigned long long* mismatches) {
+  unsigned long long bad = 0;
+  const int64_t stride = static_cast<int64_t>(gridDim.x) * blockDim.x;
+  for (int64_t i = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; i < n;
+       i += stride) {
+    uint64_t ra = rnd64(seed, 2 * i), rb = rnd64(seed, 2 * i + 1);
+    uint64_t A = ra, B = rb;
+    switch (i % 5) {
+      case 0: break;
+      case 1: {  // exponents within 2 of each other
+        const uint64_t e = ((ra >> 12) % 2000u) + 20u;
+        A = (ra & 0x800FFFFFFFFFFFFFULL) | (e << 52);
+        B = (rb & 0x800FFFFFFFFFFFFFULL) | ((e + (rb >> 60) % 3u - 1u) << 52);
+        break;
+      }
+      case 2: {  // exponents up to 70 apart
+        const uint64_t e = ((ra >> 12) % 1800u) + 100u;
+        A = (ra & 0x800FFFFFFFFFFFFFULL) | (e << 52);
+        B = (rb & 0x800FFFFFFFFFFFFFULL) | ((e - (rb >> 56) % 71u) << 52);
+        break;
+      }
+      case 3: {  // near the ends of the exponent range
+        const uint64_t e1 = (ra >> 60) & 1u ? 2046u - (ra >> 56) % 8u : 1u + (ra >> 56) % 8u;
+        const uint64_t e2 = (rb >> 60) & 1u ? 1023u + (rb >> 56) % 8u : 1023u - (rb >> 56) % 8u;
+        A = (ra & 0x800FFFFFFFFFFFFFULL) | (e1 << 52);
+        B = (rb & 0x800FFFFFFFFFFFFFULL) | (e2 << 52);
+        break;
+      }
+      default: {
+        A = __double_as_longlong(0.5 + static_cast<double>(ra >> 11) * 0x1.0p-53);
+        B = __double_as_longlong(0.5 + static_cast<double>(rb >> 11) * 0x1.0p-53);
+        break;
+      }
+    }
+    const double a = __longlong_as_double(static_cast<long long>(A));
+    const double b = __longlong_as_double(static_cast<long long>(B));
+    double want, got;
+    if (op == 0) { want = __dadd_rn(a, b); got = b200::f64emu::add(a, b); }
+    else if (op == 1) { want = __dadd_rn(a, -b); got = b200::f64emu::sub(a, b); }
+    else { want = __dmul_rn(a, b); got = b200::f64emu::mul(a, b); }
+    const bool same = (__double_as_longlong(want) == __double_as_longlong(got)) ||
+                      (isnan(want) && isnan(got));
+    if (!same) ++bad;
+  }
+  if (bad) atomicAdd(mismatches, bad);
+}
+
+}  // namespace
+
+extern "C" int b200_f64emu_selftest(int64_t n, uint64_t seed, int32_t op,
+                                    unsigned long long* mismatches, b200_stream_t stream) {
+  if (n < 0 || !mismatches || op < 0 || op > 2) return invalid("b200_f64emu_selftest: bad args");
+  const int blocks = device_info().sm_count * 8;
+  f64emu_check_kernel<<<blocks, 256, 0, as_stream(stream)>>>(n, seed, op, mismatches);
+  return after_launch("b200_f64emu_selftest");
+}

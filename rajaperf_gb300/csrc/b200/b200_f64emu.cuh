@@ -1,0 +1,129 @@
+// Exactly rounded FP64 add and multiply on the integer pipe.
+//
+// GB300 issues about 0.53 T FP64 instructions/s but about 20 T integer
+// multiply-adds/s, and the FP64-bound stencils leave the integer pipe idle.
+// These routines compute IEEE-754 binary64 round-to-nearest-even results
+// with 32/64-bit integer arithmetic only, bit-identical to the FP64 pipe's
+// a + b and a * b, so a kernel can hand part of its points to integer-pipe
+// warps without changing a single result bit.
+//
+// Fast path: both operands normal (biased exponent 1..2046) and a normal
+// result.  Everything else -- zeros, subnormals, infinities, NaNs, overflow,
+// underflow -- falls back to the native operation, so every input gives the
+// native result.  Exact cancellation returns +0 (round-to-nearest rule).
+//
+// Rounding: operands are aligned with 10 guard bits below the 53-bit
+// significand and a sticky bit (OR of every bit shifted out) in bit 0.  Any
+// inexact alignment makes the working sum odd, so it can never equal the
+// exact half-way value; after at most one normalising shift the guard/sticky
+// comparison against half an ulp decides round-to-nearest-even correctly.
+#pragma once
+
+#include <cstdint>
+
+namespace b200 {
+namespace f64emu {
+
+constexpr uint64_t kSign = 0x8000000000000000ULL;
+constexpr uint64_t kFrac = 0x000FFFFFFFFFFFFFULL;
+constexpr uint64_t kHidden = 0x0010000000000000ULL;
+
+__device__ __forceinline__ uint64_t bits(double x) {
+  return static_cast<uint64_t>(__double_as_longlong(x));
+}
+__device__ __forceinline__ double from_bits(uint64_t u) {
+  return __longlong_as_double(static_cast<long long>(u));
+}
+
+// a + b, correctly rounded (RN-even), integer pipe on the fast path.
+__device__ __forceinline__ double add(double a, double b) {
+  const uint64_t A = bits(a), B = bits(b);
+  const uint32_t eA = static_cast<uint32_t>(A >> 52) & 0x7ffu;
+  const uint32_t eB = static_cast<uint32_t>(B >> 52) & 0x7ffu;
+  if (eA - 1u >= 2046u || eB - 1u >= 2046u) return a + b;  // zero/subnormal/inf/nan
+  const bool swap = (B & ~kSign) > (A & ~kSign);
+  const uint64_t X = swap ? B : A, Y = swap ? A : B;
+  const int ex = static_cast<int>(swap ? eB : eA);
+  const uint32_t d = swap ? (eB - eA) : (eA - eB);
+  const uint64_t MX = ((X & kFrac) | kHidden) << 10;
+  const uint64_t my = ((Y & kFrac) | kHidden) << 10;
+  uint64_t MY;
+  if (d >= 63u) {
+    MY = 1u;  // only the sticky bit survives
+  } else {
+    MY = my >> d;
+    MY |= ((my & ((1ULL << d) - 1u)) != 0u) ? 1u : 0u;
+  }
+  uint64_t S;
+  int e = ex;
+  if (((X ^ Y) & kSign) == 0u) {
+    S = MX + MY;
+    if (S >> 63) {
+      S = (S >> 1) | (S & 1u);
+      e += 1;
+    }
+  } else {
+    S = MX - MY;
+    if (S == 0u) return 0.0;
+    const int lz = __clzll(static_cast<long long>(S)) - 1;  // leading one to bit 62
+    S <<= lz;
+    e -= lz;
+  }
+  uint64_t mant = S >> 10;
+  const uint32_t rem = static_cast<uint32_t>(S) & 0x3ffu;
+  if (rem > 0x200u || (rem == 0x200u && (mant & 1u))) {
+    mant += 1u;
+    if (mant >> 53) {
+      mant >>= 1;
+      e += 1;
+    }
+  }
+  if (e <= 0 || e >= 2047) return a + b;  // result under/overflows: native
+  return from_bits((X & kSign) | ((static_cast<uint64_t>(e - 1) << 52) + mant));
+}
+
+__device__ __forceinline__ double sub(double a, double b) { return add(a, -b); }
+
+// a * b, correctly rounded (RN-even), integer pipe on the fast path.
+__device__ __forceinline__ double mul(double a, double b) {
+  const uint64_t A = bits(a), B = bits(b);
+  const uint32_t eA = static_cast<uint32_t>(A >> 52) & 0x7ffu;
+  const uint32_t eB = static_cast<uint32_t>(B >> 52) & 0x7ffu;
+  if (eA - 1u >= 2046u || eB - 1u >= 2046u) return a * b;
+  const uint64_t mA = (A & kFrac) | kHidden, mB = (B & kFrac) | kHidden;
+  const uint64_t lo = mA * mB;
+  const uint64_t hi = __umul64hi(mA, mB);  // product < 2^106: hi < 2^42
+  int e = static_cast<int>(eA) + static_cast<int>(eB) - 1023;
+  uint64_t mant, rem, half;
+  if (hi >> 41) {  // product in [2^105, 2^106): keep bits 105..53
+    mant = (hi << 11) | (lo >> 53);
+    rem = lo & ((1ULL << 53) - 1u);
+    half = 1ULL << 52;
+    e += 1;
+  } else {         // product in [2^104, 2^105): keep bits 104..52
+    mant = (hi << 12) | (lo >> 52);
+    rem = lo & ((1ULL << 52) - 1u);
+    half = 1ULL << 51;
+  }
+  if (rem > half || (rem == half && (mant & 1u))) {
+    mant += 1u;
+    if (mant >> 53) {
+      mant >>= 1;
+      e += 1;
+    }
+  }
+  if (e <= 0 || e >= 2047) return a * b;
+  return from_bits(((A ^ B) & kSign) | ((static_cast<uint64_t>(e - 1) << 52) + mant));
+}
+
+// x * 2^k for a small |k|: exact exponent arithmetic; native when the result
+// would leave the normal range (or x is not a normal number).
+__device__ __forceinline__ double scale2(double x, int k) {
+  const uint64_t X = bits(x);
+  const int e = static_cast<int>((X >> 52) & 0x7ffu);
+  if (e == 0 || e == 2047 || e + k <= 0 || e + k >= 2047) return x * scalbn(1.0, k);
+  return from_bits(X + (static_cast<uint64_t>(static_cast<int64_t>(k)) << 52));
+}
+
+}  // namespace f64emu
+}  // namespace b200

@@ -3,16 +3,17 @@
 // Ozaki-style splitting with exact integer slices:
 //  1. Every row i of A gets a power-of-two scale 2^Ea(i) with
 //     |A(i,k)| < 2^(Ea(i)-1); every column j of B likewise 2^Eb(j).
-//  2. q = round(A(i,k) * 2^(5S - Ea(i))) is an integer with |q| < 2^(5S-1)
-//     (S slices of 5 bits); its balanced base-32 digits d_1..d_S (d_1 most
-//     significant, every |d_s| <= 16) are stored as bf16, which holds them
-//     exactly.  B is cut the same way and stored transposed (N x K).
+//  2. q = round(A(i,k) * 2^(5S - Ea(i))) is an integer with |q| <= 2^(5S-1)
+//     (S slices of 5 bits); its base-32 digits d_1..d_S (d_1 most
+//     significant; d_2..d_S balanced in [-16, 15], |d_1| <= 17) are stored as
+//     bf16, which holds them exactly.  B is cut the same way and stored
+//     transposed (N x K).
 //  3. For every digit weight w = s + t the products A_s * B_t are summed over
 //     k on the tensor cores in one FP32 accumulator.  Each product is an
-//     integer of magnitude <= 256 and K <= kMaxK, so every partial sum is an
-//     integer below 2^24 whenever at most 8 slice pairs share a weight: the
+//     integer of magnitude <= 289 and K <= kMaxK, so every partial sum is an
+//     integer below 2^24 whenever at most 7 slice pairs share a weight: the
 //     tensor-core accumulation is exact for the weights that carry the result
-//     (larger weights contribute below 2^-50 of it).
+//     (larger weights contribute below 2^-45 of it).
 //  4. The epilogue adds 2^(-5w) * acc_w into an FP64 accumulator, and finally
 //     C = alpha * 2^(Ea+Eb-10S) * acc64 + beta * C in FP64.
 // Only weights w <= S + 1 are formed (the dropped products lie below the
@@ -68,16 +69,17 @@ __global__ void col_scale_kernel(const double* __restrict__ B, int64_t K, int64_
   E[j] = scale_exponent(m);
 }
 
-// Balanced base-32 digits of round(v * 2^shift), least significant first.
+// Base-32 digits of q = round(v * 2^shift), |q| <= 2^(5S-1): the S-1 low
+// digits are balanced (in [-16, 15]); the top digit takes what is left,
+// |d_0| <= 17 (balanced digits alone only reach 0.484 * 32^S).
 __device__ __forceinline__ void digits_of(double v, int shift, int S, float* d) {
   long long q = __double2ll_rn(scalbn(v, shift));
-  for (int s = S - 1; s >= 0; --s) {
+  for (int s = S - 1; s >= 1; --s) {
     long long r = ((q + 16) & 31) - 16;   // in [-16, 15]
     d[s] = static_cast<float>(r);
     q = (q - r) >> kSliceBits;
   }
-  // |q| < 2^(5S-1) is inside the range of S balanced digits, so nothing is
-  // left over (q == 0 here).
+  d[0] = static_cast<float>(q);
 }
 
 // As[s][i][k] (Mp x Kp, zero padded) from A (M x K).

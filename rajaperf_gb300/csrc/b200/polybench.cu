@@ -10,6 +10,7 @@
 // accumulators per thread, K in steps of 16 with the next K slice prefetched
 // into registers while the current one is consumed.  Each C element's dot
 // product runs over k in increasing order, as the suite's loop does.
+#include "b200_f64emu.cuh"
 #include "b200_internal.cuh"
 
 using namespace b200;
@@ -83,6 +84,122 @@ fdtd2d_h(const double* __restrict__ ex, const double* __restrict__ ey,
     const int64_t c = j + i * ny;
     hz[c] = hz[c] - 0.7 * (ld(ex + c + 1) - ld(ex + c) + ld(ey + c + ny) - ld(ey + c));
   }
+}
+
+// ---- mixed FP64-pipe / integer-pipe stencils ----------------------------------
+// A CTA of 8 warps owns a tile of 32 contiguous columns.  Warps [0, E) compute
+// their rows with the integer-pipe emulation (b200_f64emu.cuh), warps [E, 8)
+// with the FP64 pipe; emulated warps take `he` rows each and native warps `hn`,
+// so both pipes finish together.  Each thread walks down its rows keeping the
+// vertical neighbours in registers.  The emulated arithmetic is bit-identical
+// to the FP64 pipe's, so the split never changes a result.
+struct MixShape {
+  int E, he, hn;
+  __host__ __device__ int rows() const { return E * he + (8 - E) * hn; }
+};
+
+template <bool EMU>
+__device__ __forceinline__ double jacobi_pt(double c, double l, double r, double d, double u) {
+  if (EMU) {
+    using namespace f64emu;
+    return mul(0.2, add(add(add(add(c, l), r), d), u));
+  }
+  return 0.2 * (c + l + r + d + u);
+}
+
+template <bool EMU>
+__device__ __forceinline__ void jacobi_rows(const double* __restrict__ S, double* __restrict__ D,
+                                            int64_t N, int64_t j, int64_t i_first, int rows) {
+  if (i_first >= N - 1) return;  // this warp's rows lie past the interior
+  int64_t c = j + i_first * N;
+  double up = ld(S + c - N), mid = ld(S + c);
+  for (int r = 0; r < rows; ++r, c += N) {
+    if (i_first + r >= N - 1) break;
+    const double down = ld(S + c + N);
+    D[c] = jacobi_pt<EMU>(mid, ld(S + c - 1), ld(S + c + 1), down, up);
+    up = mid;
+    mid = down;
+  }
+}
+
+__global__ void __launch_bounds__(256)
+jacobi2d_mixed(const double* __restrict__ S, double* __restrict__ D, int64_t N, MixShape m) {
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int64_t j = 1 + static_cast<int64_t>(blockIdx.x) * 32 + lane;
+  if (j >= N - 1) return;
+  const bool emu = warp < m.E;
+  const int r0 = emu ? warp * m.he : m.E * m.he + (warp - m.E) * m.hn;
+  const int rows = emu ? m.he : m.hn;
+  for (int64_t tile = blockIdx.y; tile * m.rows() < N - 2; tile += gridDim.y) {
+    const int64_t i_first = 1 + tile * m.rows() + r0;
+    if (emu) jacobi_rows<true>(S, D, N, j, i_first, rows);
+    else jacobi_rows<false>(S, D, N, j, i_first, rows);
+  }
+}
+
+// HEAT_3D point: the suite's body, with 2.0*a and 0.125*u as exact
+// power-of-two scalings on the emulated path.
+template <bool EMU>
+__device__ __forceinline__ double heat_pt(double a, double ip, double im, double jp, double jm,
+                                          double kp, double km) {
+  if (EMU) {
+    using namespace f64emu;
+    const double a2 = scale2(a, 1);
+    const double t1 = scale2(add(sub(ip, a2), im), -3);
+    const double t2 = scale2(add(sub(jp, a2), jm), -3);
+    const double t3 = scale2(add(sub(kp, a2), km), -3);
+    return add(add(add(t1, t2), t3), a);
+  }
+  return 0.125 * (ip - 2.0 * a + im) + 0.125 * (jp - 2.0 * a + jm) +
+         0.125 * (kp - 2.0 * a + km) + a;
+}
+
+// Thread (j, k) walks planes i in [i0, i0 + ni): the i-neighbours stay in
+// registers.  Index k + N*(j + N*i).
+template <bool EMU>
+__device__ __forceinline__ void heat_rows(const double* __restrict__ S, double* __restrict__ D,
+                                          int64_t N, int64_t k, int64_t j_first, int rows,
+                                          int64_t i0, int64_t ni) {
+  const int64_t NN = N * N;
+  for (int r = 0; r < rows; ++r) {
+    const int64_t j = j_first + r;
+    if (j >= N - 1) break;
+    int64_t c = k + N * (j + N * i0);
+    double im = ld(S + c - NN), a = ld(S + c);
+    for (int64_t i = i0; i < i0 + ni && i < N - 1; ++i, c += NN) {
+      const double ip = ld(S + c + NN);
+      D[c] = heat_pt<EMU>(a, ip, im, ld(S + c + N), ld(S + c - N), ld(S + c + 1), ld(S + c - 1));
+      im = a;
+      a = ip;
+    }
+  }
+}
+
+__global__ void __launch_bounds__(256)
+heat3d_mixed(const double* __restrict__ S, double* __restrict__ D, int64_t N, MixShape m,
+             int64_t chunk) {
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int64_t k = 1 + static_cast<int64_t>(blockIdx.x) * 32 + lane;
+  if (k >= N - 1) return;
+  const bool emu = warp < m.E;
+  const int r0 = emu ? warp * m.he : m.E * m.he + (warp - m.E) * m.hn;
+  const int rows = emu ? m.he : m.hn;
+  const int64_t j_first = 1 + static_cast<int64_t>(blockIdx.y) * m.rows() + r0;
+  const int64_t i0 = 1 + static_cast<int64_t>(blockIdx.z) * chunk;
+  if (emu) heat_rows<true>(S, D, N, k, j_first, rows, i0, chunk);
+  else heat_rows<false>(S, D, N, k, j_first, rows, i0, chunk);
+}
+
+MixShape mix_shape(const b200_tune* t, MixShape def) {
+  MixShape m = def;
+  if (t && t->algo > 0) m.E = t->algo - 1;   // algo = 1 + emulated warps (0..8)
+  if (t && t->tile_y > 0) m.he = t->tile_y;
+  if (t && t->tile_z > 0) m.hn = t->tile_z;
+  if (m.E < 0) m.E = 0;
+  if (m.E > 8) m.E = 8;
+  if (m.he < 1) m.he = 1;
+  if (m.hn < 1) m.hn = 1;
+  return m;
 }
 
 // ---- GEMM (FP64, DFMA) -------------------------------------------------------
@@ -184,8 +301,19 @@ int b200_polybench_jacobi_2d(double* A, double* B, int64_t N, int64_t tsteps,
                              const b200_tune* tune, b200_stream_t stream) {
   if (!A || !B || N < 0 || tsteps < 0) return invalid("b200_polybench_jacobi_2d: bad args");
   if (N < 3 || tsteps == 0) return B200_OK;
-  (void)tune;
   cudaStream_t st = as_stream(stream);
+  if (tune && tune->algo > 0) {
+    // mixed FP64 / integer pipes (algo = 1 + emulated warps of 8)
+    const MixShape m = mix_shape(tune, MixShape{4, 4, 10});
+    int64_t gy = ceil_div(N - 2, m.rows());
+    if (gy > 65535) gy = 65535;
+    dim3 g(static_cast<unsigned>(ceil_div(N - 2, 32)), static_cast<unsigned>(gy));
+    for (int64_t t = 0; t < tsteps; ++t) {
+      jacobi2d_mixed<<<g, 256, 0, st>>>(A, B, N, m);
+      jacobi2d_mixed<<<g, 256, 0, st>>>(B, A, N, m);
+    }
+    return after_launch("b200_polybench_jacobi_2d", static_cast<int>(2 * tsteps));
+  }
   constexpr int BX = 64, BY = 4;
   dim3 g = grid2(N - 2, N - 2, BX, BY);
   for (int64_t t = 0; t < tsteps; ++t) {
@@ -199,8 +327,20 @@ int b200_polybench_heat_3d(double* A, double* B, int64_t N, int64_t tsteps,
                            const b200_tune* tune, b200_stream_t stream) {
   if (!A || !B || N < 0 || tsteps < 0) return invalid("b200_polybench_heat_3d: bad args");
   if (N < 3 || tsteps == 0) return B200_OK;
-  (void)tune;
   cudaStream_t st = as_stream(stream);
+  if (tune && tune->algo > 0) {
+    const MixShape m = mix_shape(tune, MixShape{4, 2, 5});
+    const int64_t chunk = (tune->tile_x > 0) ? tune->tile_x : 32;
+    const int64_t gy = ceil_div(N - 2, m.rows()), gz = ceil_div(N - 2, chunk);
+    if (gy > 65535 || gz > 65535) return invalid("b200_polybench_heat_3d: N too large");
+    dim3 g(static_cast<unsigned>(ceil_div(N - 2, 32)), static_cast<unsigned>(gy),
+           static_cast<unsigned>(gz));
+    for (int64_t t = 0; t < tsteps; ++t) {
+      heat3d_mixed<<<g, 256, 0, st>>>(A, B, N, m, chunk);
+      heat3d_mixed<<<g, 256, 0, st>>>(B, A, N, m, chunk);
+    }
+    return after_launch("b200_polybench_heat_3d", static_cast<int>(2 * tsteps));
+  }
   constexpr int BX = 32, BY = 8;
   int64_t gz = N - 2;
   if (gz > 65535) gz = 65535;

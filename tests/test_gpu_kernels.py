@@ -273,3 +273,43 @@ def test_null_pointer_rejected(fn, args):
         elif t in (ctypes.c_int64, ctypes.c_long):
             argv[i] = 16
     assert f(*argv) == rp.B200_ERR_INVALID_ARG
+
+
+@pytest.mark.parametrize("op", [0, 1, 2])
+def test_integer_pipe_fp64_is_bit_exact(op):
+    """The integer-pipe add/sub/mul used by the mixed-pipe stencils against
+    the FP64 pipe on 16M operand pairs (every class of double)."""
+    torch = gu.torch_cuda()
+    bad = torch.zeros(1, dtype=torch.int64, device="cuda")
+    rp.check(lib().b200_f64emu_selftest(1 << 24, 12345 + op, op, bad.data_ptr(), gu.stream()))
+    assert int(gu.host(bad)[0]) == 0
+
+
+@pytest.mark.parametrize("N,ts", [(3, 1), (37, 2), (300, 3)])
+@pytest.mark.parametrize("shape", [(5, 4, 10), (1, 1, 3), (9, 2, 1), (4, 1, 7)])
+def test_jacobi_mixed_pipes_bit_identical(N, ts, shape):
+    rng = np.random.default_rng(N * 7 + shape[0])
+    A, B = rng.uniform(0.5, 1.5, N * N), rng.uniform(0.5, 1.5, N * N)
+    dA1, dB1, dA2, dB2 = dev(A), dev(B), dev(A), dev(B)
+    rp.check(lib().b200_polybench_jacobi_2d(dA1.data_ptr(), dB1.data_ptr(), N, ts, None,
+                                            gu.stream()))
+    t = rp.Tune(algo=shape[0], tile_y=shape[1], tile_z=shape[2])
+    rp.check(lib().b200_polybench_jacobi_2d(dA2.data_ptr(), dB2.data_ptr(), N, ts,
+                                            ctypes.byref(t), gu.stream()))
+    assert np.array_equal(gu.host(dA1), gu.host(dA2))
+    assert np.array_equal(gu.host(dB1), gu.host(dB2))
+
+
+@pytest.mark.parametrize("N,ts", [(3, 1), (20, 2), (70, 2)])
+@pytest.mark.parametrize("shape", [(5, 2, 5, 32), (1, 1, 2, 3), (9, 1, 1, 7), (3, 3, 1, 5)])
+def test_heat_mixed_pipes_bit_identical(N, ts, shape):
+    rng = np.random.default_rng(N * 11 + shape[0])
+    A, B = rng.uniform(0.5, 1.5, N ** 3), rng.uniform(0.5, 1.5, N ** 3)
+    dA1, dB1, dA2, dB2 = dev(A), dev(B), dev(A), dev(B)
+    rp.check(lib().b200_polybench_heat_3d(dA1.data_ptr(), dB1.data_ptr(), N, ts, None,
+                                          gu.stream()))
+    t = rp.Tune(algo=shape[0], tile_y=shape[1], tile_z=shape[2], tile_x=shape[3])
+    rp.check(lib().b200_polybench_heat_3d(dA2.data_ptr(), dB2.data_ptr(), N, ts,
+                                          ctypes.byref(t), gu.stream()))
+    assert np.array_equal(gu.host(dA1), gu.host(dA2))
+    assert np.array_equal(gu.host(dB1), gu.host(dB2))
