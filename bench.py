@@ -616,8 +616,12 @@ def measure_gemm(torch, rp, stream, sizes=(1024, 4096, 8192), seed=4793):
     (b200_gemm_f64) against split precision (b200_gemm_split), TFLOP/s at
     2*N^3 and the split result's relative Frobenius error against the native
     FP64 result; plus a variant with rows of A scaled by 2^k, k in [-20, 20]."""
+    import ctypes
     L = rp.b200()
     s = stream.cuda_stream
+    legacy = rp.Tune(algo=1)  # the mma.sync engine, for comparison
+    slices = 11
+    pairs = slices * (slices + 1) // 2  # slice products formed per C element
     out = []
     for n in sizes:
         g = torch.Generator(device="cuda").manual_seed(seed + n)
@@ -633,10 +637,13 @@ def measure_gemm(torch, rp, stream, sizes=(1024, 4096, 8192), seed=4793):
                          ("split", lambda C: L.b200_gemm_split(A.data_ptr(), B.data_ptr(),
                                                                C.data_ptr(), n, n, n, 1.5, 1.2,
                                                                ws.data_ptr(), ws_bytes, None,
-                                                               s))):
+                                                               s)),
+                         ("split_mma_sync", lambda C: L.b200_gemm_split(
+                             A.data_ptr(), B.data_ptr(), C.data_ptr(), n, n, n, 1.5, 1.2,
+                             ws.data_ptr(), ws_bytes, ctypes.byref(legacy), s))):
             C = C0.clone()
             rp.check(fn(C), name)  # warm-up
-            reps = 1 if (name == "native" and n >= 8192) else 3
+            reps = 1 if (name != "split" and n >= 8192) else 3
             best = None
             for _ in range(reps):
                 C = C0.clone()
@@ -654,7 +661,10 @@ def measure_gemm(torch, rp, stream, sizes=(1024, 4096, 8192), seed=4793):
         err = (res["C_split"] - res["C_native"]).norm() / res["C_native"].norm()
         res["rel_err_vs_fp64"] = float(err)
         res["speedup"] = round(res["split_tflops"] / res["native_tflops"], 2)
-        del res["C_split"], res["C_native"]
+        res["speedup_vs_mma_sync"] = round(res["split_tflops"] / res["split_mma_sync_tflops"], 2)
+        # bf16 tensor work actually issued: `pairs` slice products of 2*n^3 each
+        res["split_bf16_tflops"] = round(res["split_tflops"] * pairs, 1)
+        del res["C_split"], res["C_native"], res["C_split_mma_sync"]
         if n == sizes[-1] or n <= 4096:
             # row-scaled variant (accuracy only)
             k = torch.randint(-20, 21, (n, 1), device="cuda", generator=g).to(torch.float64)

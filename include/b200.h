@@ -338,7 +338,11 @@ size_t b200_gemm_split_workspace_bytes(int64_t m, int64_t n, int64_t k,
  * tune->items (default 11) balanced 5-bit integer slices held exactly in
  * bf16; slice products of equal weight accumulate exactly in FP32 on the
  * tensor cores; the weighted sum is formed in FP64.  k <= 8192 (the bound
- * under which the FP32 accumulation stays exact).  Not in the reference: the
+ * under which the FP32 accumulation stays exact).  tune->algo picks the
+ * engine: 0 (default) tcgen05 MMA with TMA-fed operands and tensor-memory
+ * accumulators, 1 the legacy mma.sync path.  The 32-bit word at the start of
+ * the workspace is cleared by every call and set to 1 if a bounded wait of
+ * the tcgen05 engine gave up (C is then invalid).  Not in the reference: the
  * split-precision form of polybench/POLYBENCH_GEMM.hpp:40-56.              */
 int b200_gemm_split(const double* A, const double* B, double* C, int64_t m,
                     int64_t n, int64_t k, double alpha, double beta,

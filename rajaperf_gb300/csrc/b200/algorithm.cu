@@ -18,8 +18,10 @@ using namespace b200;
 namespace {
 
 constexpr int kScanBlock = 256;
-constexpr int kScanItems = 16;
-constexpr int kScanTile = kScanBlock * kScanItems;
+constexpr int kScanItemsMin = 16;                       // smallest tile: 4096 items
+constexpr int kScanItemsDefault = 32;                   // default tile: 8192 items
+constexpr int kScanTileMin = kScanBlock * kScanItemsMin;
+constexpr int kLookbackPerLane = 4;                     // 128 predecessors per round
 constexpr long long kSpinLimit = 1LL << 22;
 
 struct ScanHeader {
@@ -54,12 +56,36 @@ __device__ __forceinline__ T warp_inclusive_scan(T v) {
   return v;
 }
 
-template <typename T>
+// Waits (bounded) until predecessor p has published at least its aggregate
+// for this launch; returns the flag.  A wait that gives up records the error
+// and reports an inclusive prefix so the lookback terminates.
+__device__ __forceinline__ unsigned long long wait_flag(const unsigned long long* flags,
+                                                        int64_t p, unsigned long long AGG,
+                                                        unsigned long long INC,
+                                                        ScanHeader* hdr) {
+  unsigned long long f = ld_acquire(&flags[p]);
+  long long spins = 0;
+  while (f < AGG) {
+    if (++spins > kSpinLimit) {
+      atomicExch(&hdr->error, 1u);
+      return INC;
+    }
+    if (spins > 64) __nanosleep(64);
+    f = ld_acquire(&flags[p]);
+  }
+  return f;
+}
+
+// Tile = kScanBlock * IT items, staged in dynamic shared memory (padded so
+// the per-thread runs of IT consecutive items are conflict-free).
+template <typename T, int IT>
 __global__ void __launch_bounds__(kScanBlock)
 scan_kernel(const T* __restrict__ x, T* __restrict__ y, int64_t n, T init,
             ScanHeader* __restrict__ hdr, unsigned long long* __restrict__ flags,
             T* __restrict__ aggs, T* __restrict__ incs) {
-  __shared__ T s_tile[kScanTile + kScanTile / 16];
+  constexpr int kTile = kScanBlock * IT;
+  extern __shared__ __align__(16) unsigned char s_raw[];
+  T* s_tile = reinterpret_cast<T*>(s_raw);
   __shared__ T s_warp[kScanBlock / 32];
   __shared__ T s_excl;
   __shared__ T s_agg;
@@ -76,14 +102,22 @@ scan_kernel(const T* __restrict__ x, T* __restrict__ y, int64_t n, T init,
   const unsigned int tile = s_tile_id;
   const unsigned long long epoch = s_epoch;
   const unsigned long long AGG = epoch * 4 + 1, INC = epoch * 4 + 2;
-  const int64_t base = static_cast<int64_t>(tile) * kScanTile;
+  const int64_t base = static_cast<int64_t>(tile) * kTile;
 
   // striped, coalesced load into shared memory
+  if (base + kTile <= n) {
 #pragma unroll
-  for (int u = 0; u < kScanItems; ++u) {
-    int k = u * kScanBlock + tid;
-    int64_t i = base + k;
-    s_tile[padded(k)] = (i < n) ? __ldg(x + i) : T(0);
+    for (int u = 0; u < IT; ++u) {
+      const int k = u * kScanBlock + tid;
+      s_tile[padded(k)] = __ldcs(x + base + k);
+    }
+  } else {
+#pragma unroll
+    for (int u = 0; u < IT; ++u) {
+      const int k = u * kScanBlock + tid;
+      const int64_t i = base + k;
+      s_tile[padded(k)] = (i < n) ? __ldcs(x + i) : T(0);
+    }
   }
   __syncthreads();
 
@@ -91,7 +125,7 @@ scan_kernel(const T* __restrict__ x, T* __restrict__ y, int64_t n, T init,
   // totals gives every thread its offset inside the tile.
   T run = T(0);
 #pragma unroll
-  for (int u = 0; u < kScanItems; ++u) run += s_tile[padded(tid * kScanItems + u)];
+  for (int u = 0; u < IT; ++u) run += s_tile[padded(tid * IT + u)];
   T incl = warp_inclusive_scan(run);
   if (lane == 31) s_warp[warp] = incl;
   __syncthreads();
@@ -106,7 +140,10 @@ scan_kernel(const T* __restrict__ x, T* __restrict__ y, int64_t n, T init,
   const T agg = s_agg;
 
   // Warp 0 resolves the tile's prefix (decoupled lookback) while the other
-  // warps turn their items into tile-local exclusive prefixes in place.
+  // warps turn their items into tile-local exclusive prefixes in place.  One
+  // lookback round examines 32 * kLookbackPerLane predecessors, nearest
+  // first (window slot w = j * 32 + lane is predecessor p_hi - w), so that
+  // the INC frontier keeps up with the rate at which tiles start.
   if (warp == 0) {
     T exclusive = init;
     if (tile == 0) {
@@ -125,34 +162,36 @@ scan_kernel(const T* __restrict__ x, T* __restrict__ y, int64_t n, T init,
       int64_t p_hi = static_cast<int64_t>(tile) - 1;  // nearest unexamined predecessor
       bool done = false;
       while (!done) {
-        int64_t p = p_hi - lane;
-        unsigned long long f = INC;  // lanes past tile 0 act as a terminator
-        T val = T(0);
-        if (p >= 0) {
-          long long spins = 0;
-          f = ld_acquire(&flags[p]);
-          while (f < AGG) {
-            if (++spins > kSpinLimit) {
-              atomicExch(&hdr->error, 1u);
-              f = INC;
-              break;
-            }
-            if (spins > 64) __nanosleep(64);
-            f = ld_acquire(&flags[p]);
-          }
-          // L1-bypassing loads: the values were written by other SMs.
-          if (f >= AGG) val = (f == INC) ? __ldcg(incs + p) : __ldcg(aggs + p);
+        unsigned long long f[kLookbackPerLane];
+#pragma unroll
+        for (int j = 0; j < kLookbackPerLane; ++j) {
+          const int64_t p = p_hi - (j * 32 + lane);
+          f[j] = (p >= 0) ? wait_flag(flags, p, AGG, INC, hdr) : INC;  // p < 0: terminator
         }
-        // first lane (nearest predecessor) holding an inclusive prefix
-        unsigned int inc_mask = __ballot_sync(0xffffffffu, f == INC);
-        int stop = inc_mask ? (__ffs(inc_mask) - 1) : 32;
-        if (lane > stop) val = T(0);
-        // fixed lane order: nearest predecessor first
+        T v[kLookbackPerLane];
+#pragma unroll
+        for (int j = 0; j < kLookbackPerLane; ++j) {
+          const int64_t p = p_hi - (j * 32 + lane);
+          // L1-bypassing loads: the values were written by other SMs.
+          v[j] = (p < 0) ? T(0) : (f[j] == INC) ? __ldcg(incs + p) : __ldcg(aggs + p);
+        }
+        // nearest window slot holding an inclusive prefix
+        int stop = 32 * kLookbackPerLane;
+#pragma unroll
+        for (int j = kLookbackPerLane - 1; j >= 0; --j) {
+          const unsigned int m = __ballot_sync(0xffffffffu, f[j] == INC);
+          if (m) stop = j * 32 + __ffs(m) - 1;
+        }
+        // fixed order: slots j = 0.. summed per lane, then a fixed lane tree
+        T val = T(0);
+#pragma unroll
+        for (int j = 0; j < kLookbackPerLane; ++j)
+          if (j * 32 + lane <= stop) val += v[j];
 #pragma unroll
         for (int off = 16; off > 0; off >>= 1) val += __shfl_down_sync(0xffffffffu, val, off);
         acc += __shfl_sync(0xffffffffu, val, 0);
-        if (stop < 32) done = true;
-        p_hi -= 32;
+        if (stop < 32 * kLookbackPerLane) done = true;
+        p_hi -= 32 * kLookbackPerLane;
       }
       exclusive = acc;
       if (lane == 0) {
@@ -166,8 +205,8 @@ scan_kernel(const T* __restrict__ x, T* __restrict__ y, int64_t n, T init,
   {
     T r = thread_excl;
 #pragma unroll
-    for (int u = 0; u < kScanItems; ++u) {
-      const int k = padded(tid * kScanItems + u);
+    for (int u = 0; u < IT; ++u) {
+      const int k = padded(tid * IT + u);
       const T xv = s_tile[k];
       s_tile[k] = r;
       r += xv;
@@ -175,11 +214,19 @@ scan_kernel(const T* __restrict__ x, T* __restrict__ y, int64_t n, T init,
   }
   __syncthreads();
   const T prefix = s_excl;
+  if (base + kTile <= n) {
 #pragma unroll
-  for (int u = 0; u < kScanItems; ++u) {
-    int k = u * kScanBlock + tid;
-    int64_t i = base + k;
-    if (i < n) y[i] = prefix + s_tile[padded(k)];
+    for (int u = 0; u < IT; ++u) {
+      const int k = u * kScanBlock + tid;
+      __stcs(y + base + k, prefix + s_tile[padded(k)]);
+    }
+  } else {
+#pragma unroll
+    for (int u = 0; u < IT; ++u) {
+      const int k = u * kScanBlock + tid;
+      const int64_t i = base + k;
+      if (i < n) __stcs(y + i, prefix + s_tile[padded(k)]);
+    }
   }
 
   // the last CTA to finish prepares the workspace for the next call
@@ -197,27 +244,50 @@ scan_kernel(const T* __restrict__ x, T* __restrict__ y, int64_t n, T init,
   }
 }
 
-int64_t scan_tiles(int64_t n) { return ceil_div(n > 0 ? n : 1, kScanTile); }
+// The workspace is sized for the smallest tile, so it serves every tile size.
+int64_t scan_tiles_max(int64_t n) { return ceil_div(n > 0 ? n : 1, kScanTileMin); }
+
+template <typename T, int IT>
+int launch_scan_it(const T* x, T* y, int64_t n, T init, char* w, cudaStream_t st) {
+  constexpr int kTile = kScanBlock * IT;
+  constexpr size_t kSmem = static_cast<size_t>(kTile + kTile / 16) * sizeof(T);
+  const cudaError_t attr = cudaFuncSetAttribute(
+      scan_kernel<T, IT>, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(kSmem));
+  if (attr != cudaSuccess) {
+    set_error("scan: shared memory attribute: %s", cudaGetErrorString(attr));
+    return B200_ERR_LAUNCH;
+  }
+  const int64_t tiles = ceil_div(n, kTile);
+  const int64_t slots = scan_tiles_max(n);
+  ScanHeader* hdr = reinterpret_cast<ScanHeader*>(w);
+  unsigned long long* flags = reinterpret_cast<unsigned long long*>(w + 256);
+  T* aggs = reinterpret_cast<T*>(w + 256 + slots * 8);
+  T* incs = reinterpret_cast<T*>(w + 256 + slots * 16);
+  scan_kernel<T, IT><<<static_cast<int>(tiles), kScanBlock, kSmem, st>>>(x, y, n, init, hdr,
+                                                                          flags, aggs, incs);
+  return B200_OK;
+}
 
 template <typename T>
 int launch_scan(const char* name, const T* x, T* y, int64_t n, T init, void* ws,
-                size_t ws_bytes, cudaStream_t st) {
+                size_t ws_bytes, const b200_tune* tune, cudaStream_t st) {
   if (n < 0 || (n > 0 && (!x || !y))) return invalid("%s: bad args", name);
   if (n == 0) return B200_OK;
-  int64_t tiles = scan_tiles(n);
-  if (tiles > 0x7fffffffLL) return invalid("%s: n too large", name);
-  size_t need = 256 + static_cast<size_t>(tiles) * 24;
+  const int64_t slots = scan_tiles_max(n);
+  if (slots > 0x7fffffffLL) return invalid("%s: n too large", name);
+  if (tune && tune->block_size && tune->block_size != kScanBlock)
+    return invalid("%s: block size %d (only %d)", name, tune->block_size, kScanBlock);
+  const int items = (tune && tune->items) ? tune->items : kScanItemsDefault;
+  if (items != 16 && items != 32) return invalid("%s: items %d (16 or 32)", name, items);
+  size_t need = 256 + static_cast<size_t>(slots) * 24;
   if (!ws || ws_bytes < need) {
     set_error("%s: workspace %zu bytes, need %zu", name, ws_bytes, need);
     return B200_ERR_WORKSPACE;
   }
   char* w = static_cast<char*>(ws);
-  ScanHeader* hdr = reinterpret_cast<ScanHeader*>(w);
-  unsigned long long* flags = reinterpret_cast<unsigned long long*>(w + 256);
-  T* aggs = reinterpret_cast<T*>(w + 256 + tiles * 8);
-  T* incs = reinterpret_cast<T*>(w + 256 + tiles * 16);
-  scan_kernel<T><<<static_cast<int>(tiles), kScanBlock, 0, st>>>(x, y, n, init, hdr, flags,
-                                                                 aggs, incs);
+  const int rc = (items == 16) ? launch_scan_it<T, 16>(x, y, n, init, w, st)
+                               : launch_scan_it<T, 32>(x, y, n, init, w, st);
+  if (rc != B200_OK) return rc;
   return after_launch(name);
 }
 
@@ -260,26 +330,24 @@ reduce_sum_kernel(const double* __restrict__ x, int64_t n, double init,
 extern "C" {
 
 size_t b200_scan_workspace_bytes(int64_t n) {
-  return 256 + static_cast<size_t>(scan_tiles(n)) * 24;
+  return 256 + static_cast<size_t>(scan_tiles_max(n)) * 24;
 }
 
 int b200_algorithm_scan(const double* x, double* y, int64_t n, double init,
                         void* workspace, size_t workspace_bytes, const b200_tune* tune,
                         b200_stream_t stream) {
-  (void)tune;
   return launch_scan<double>("b200_algorithm_scan", x, y, n, init, workspace,
-                             workspace_bytes, as_stream(stream));
+                             workspace_bytes, tune, as_stream(stream));
 }
 
 int b200_algorithm_scan_i64(const int64_t* x, int64_t* y, int64_t n, int64_t init,
                             void* workspace, size_t workspace_bytes,
                             const b200_tune* tune, b200_stream_t stream) {
-  (void)tune;
   return launch_scan<long long>("b200_algorithm_scan_i64",
                                 reinterpret_cast<const long long*>(x),
                                 reinterpret_cast<long long*>(y), n,
                                 static_cast<long long>(init), workspace, workspace_bytes,
-                                as_stream(stream));
+                                tune, as_stream(stream));
 }
 
 int b200_algorithm_reduce_sum(const double* x, int64_t n, double sum_init, double* sum,

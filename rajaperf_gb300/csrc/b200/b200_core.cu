@@ -34,6 +34,16 @@ int invalid(const char* fmt, ...) {
   return B200_ERR_INVALID_ARG;
 }
 
+int unsupported(const char* fmt, ...) {
+  char buf[512];
+  va_list ap;
+  va_start(ap, fmt);
+  std::vsnprintf(buf, sizeof(buf), fmt, ap);
+  va_end(ap);
+  g_last_error = buf;
+  return B200_ERR_UNSUPPORTED;
+}
+
 int after_launch(const char* what, int nlaunches) {
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) {

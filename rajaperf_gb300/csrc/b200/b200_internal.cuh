@@ -22,6 +22,9 @@ void clear_error();
 // Records a failed argument check and returns B200_ERR_INVALID_ARG.
 int invalid(const char* fmt, ...);
 
+// Records an unsupported device or configuration; returns B200_ERR_UNSUPPORTED.
+int unsupported(const char* fmt, ...);
+
 // Checks the launch that was just issued and counts it.  Returns B200_OK or
 // B200_ERR_LAUNCH with the CUDA error recorded.
 int after_launch(const char* what, int nlaunches = 1);

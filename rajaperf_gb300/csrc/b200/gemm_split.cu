@@ -20,11 +20,27 @@
 // slicing error).  The error against an FP64 GEMM is measured per size by the
 // tests and bench.
 //
-// Engine: mma.sync.m16n8k16 bf16 -> fp32, 128x128 C tile per CTA (8 warps of
-// 64x32), 32-wide K stages double-buffered through shared memory with cp.async.
+// Engines (tune->algo):
+//  0 (default) tcgen05: one 128x128 C tile per CTA.  Warp 0 streams 128x64
+//    slice tiles of A and B into a 6-stage shared-memory ring with TMA
+//    (128-byte swizzle); warp 1 issues tcgen05.mma (kind::f16, bf16 in, FP32
+//    out) into one of two FP32 accumulators in tensor memory, one per digit
+//    weight; warps 2-5 read a finished weight's accumulator with tcgen05.ld
+//    and fold it into an FP64 accumulator that also lives in tensor memory
+//    (two 32-bit columns per element), so weight w+1's MMAs overlap weight
+//    w's FP64 epilogue.  TMEM: 2 x 128 FP32 columns + 256 FP64 columns = 512.
+//  1 mma.sync.m16n8k16 bf16 -> fp32, 128x128 C tile per CTA (8 warps of
+//    64x32), 32-wide K stages double-buffered through shared memory with
+//    cp.async (the legacy tensor-core path, kept for comparison).
+// Every wait of the tcgen05 engine is bounded (1 s); one that gives up sets
+// the error word at the start of the workspace and the CTA winds down.
 #include "b200_internal.cuh"
 
+#include <cuda.h>
+#include <cudaTypedefs.h>
 #include <cuda_bf16.h>
+
+#include <mutex>
 
 using namespace b200;
 
@@ -36,6 +52,7 @@ constexpr int kDefaultSlices = 11;
 constexpr int64_t kMaxK = 8192;  // exactness bound of the FP32 accumulation
 constexpr int TM = 128, TN = 128, TK = 32;
 constexpr int kLds = TK + 8;     // padded smem row (80 bytes): conflict-free ldmatrix
+constexpr int kPadK = 64;        // K padding of the slice arrays (one TMA row = 128 B)
 
 inline int64_t round_up(int64_t v, int64_t m) { return (v + m - 1) / m * m; }
 
@@ -271,18 +288,410 @@ __global__ void __launch_bounds__(256, 1) ozaki_mma_kernel(SplitArgs g) {
   }
 }
 
+// ---- tcgen05 engine ------------------------------------------------------------
+namespace tc {
+
+constexpr int BM = 128, BN = 128, BK = 64;          // BK bf16 = one 128-byte swizzle row
+constexpr int kStages = 6;
+constexpr uint32_t kTileBytes = BM * BK * 2;        // 16 KB per operand tile
+constexpr uint32_t kStageBytes = 2 * kTileBytes;    // A + B
+constexpr int kThreads = 192;                       // TMA, MMA, 4 epilogue warps
+constexpr uint32_t kTmemCols = 512;
+constexpr uint32_t kAcc64Col = 2 * BN;              // FP64 accumulator columns 256..511
+constexpr uint64_t kWaitLimitNs = 1000000000ull;    // 1 s
+constexpr size_t kSmemBytes = 1024 + kStages * kStageBytes + 256;
+
+// Instruction descriptor, kind::f16: D = F32 (bits 4-5 = 1), A = B = BF16
+// (bits 7-9, 10-12 = 1), both K-major, N >> 3 at bits 17-22, M >> 4 at 24-28.
+constexpr uint32_t kIdesc = (1u << 4) | (1u << 7) | (1u << 10) |
+                            (static_cast<uint32_t>(BN >> 3) << 17) |
+                            (static_cast<uint32_t>(BM >> 4) << 24);
+static_assert(kSmemBytes <= 232448, "shared memory budget");
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+  return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+__device__ __forceinline__ uint64_t globaltimer() {
+  uint64_t t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+__device__ __forceinline__ void mbar_init(uint64_t* b, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(b)), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_arrive(uint64_t* b) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(b)) : "memory");
+}
+__device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t* b, uint32_t tx) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(b)), "r"(tx)
+               : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(uint64_t* b, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+      "selp.u32 %0, 1, 0, p;\n\t}"
+      : "=r"(ok)
+      : "r"(smem_u32(b)), "r"(parity)
+      : "memory");
+  return ok != 0u;
+}
+// Waits for the phase of parity `parity` to complete.  Gives up after 1 s
+// (setting the CTA's abort flag) or when another role has aborted.
+__device__ bool mbar_wait(uint64_t* b, uint32_t parity, volatile int* abort_flag) {
+  if (mbar_try_wait(b, parity)) return true;
+  const uint64_t t0 = globaltimer();
+  for (;;) {
+    if (mbar_try_wait(b, parity)) return true;
+    if (*abort_flag) return false;
+    if (globaltimer() - t0 > kWaitLimitNs) {
+      *abort_flag = 1;
+      return false;
+    }
+  }
+}
+// The same wait for the wind-down after an abort: bounded, ignores the flag.
+__device__ bool mbar_wait_drain(uint64_t* b, uint32_t parity) {
+  const uint64_t t0 = globaltimer();
+  while (!mbar_try_wait(b, parity))
+    if (globaltimer() - t0 > kWaitLimitNs) return false;
+  return true;
+}
+__device__ __forceinline__ void tma_load_2d(void* dst, const CUtensorMap* map, uint64_t* bar,
+                                            int x, int y) {
+  asm volatile(
+      "cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes"
+      " [%0], [%1, {%3, %4}], [%2];" ::"r"(smem_u32(dst)),
+      "l"(reinterpret_cast<uint64_t>(map)), "r"(smem_u32(bar)), "r"(x), "r"(y)
+      : "memory");
+}
+__device__ __forceinline__ void tc_fence_before() {
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+}
+__device__ __forceinline__ void tc_fence_after() {
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+}
+// K-major operand tile of 8-row x 128-byte swizzle atoms (as TMA's 128-byte
+// swizzle writes it): start >> 4, leading offset 16 B (unused for this
+// layout), stride 1024 B between 8-row groups, descriptor version 1,
+// swizzle mode 2 (128 B).
+__device__ __forceinline__ uint64_t sw128_desc(uint32_t saddr) {
+  return static_cast<uint64_t>((saddr >> 4) & 0x3FFFu) | (1ull << 16) |
+         (static_cast<uint64_t>(1024 >> 4) << 32) | (1ull << 46) | (2ull << 61);
+}
+__device__ __forceinline__ void umma_bf16(uint32_t d_tmem, uint64_t adesc, uint64_t bdesc,
+                                          uint32_t accumulate) {
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "setp.ne.b32 p, %4, 0;\n\t"
+      "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(d_tmem),
+      "l"(adesc), "l"(bdesc), "r"(kIdesc), "r"(accumulate)
+      : "memory");
+}
+__device__ __forceinline__ void umma_commit(uint64_t* bar) {
+  asm volatile(
+      "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+          smem_u32(bar))
+      : "memory");
+}
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, uint32_t (&r)[16]) {
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 "
+      "{%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
+        "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]),
+        "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+      : "r"(taddr));
+}
+// tcgen05.wait::ld, tied to the loaded registers so that no use of them is
+// scheduled before the wait.
+__device__ __forceinline__ void tmem_ld_wait(uint32_t (&r)[16]) {
+  asm volatile("tcgen05.wait::ld.sync.aligned;"
+               : "+r"(r[0]), "+r"(r[1]), "+r"(r[2]), "+r"(r[3]), "+r"(r[4]), "+r"(r[5]),
+                 "+r"(r[6]), "+r"(r[7]), "+r"(r[8]), "+r"(r[9]), "+r"(r[10]), "+r"(r[11]),
+                 "+r"(r[12]), "+r"(r[13]), "+r"(r[14]), "+r"(r[15])
+               :
+               : "memory");
+}
+__device__ __forceinline__ void tmem_keep(uint32_t (&r)[16]) {
+  asm volatile(""
+               : "+r"(r[0]), "+r"(r[1]), "+r"(r[2]), "+r"(r[3]), "+r"(r[4]), "+r"(r[5]),
+                 "+r"(r[6]), "+r"(r[7]), "+r"(r[8]), "+r"(r[9]), "+r"(r[10]), "+r"(r[11]),
+                 "+r"(r[12]), "+r"(r[13]), "+r"(r[14]), "+r"(r[15])
+               :
+               : "memory");
+}
+__device__ __forceinline__ void tmem_st16(uint32_t taddr, const uint32_t (&r)[16]) {
+  asm volatile(
+      "tcgen05.st.sync.aligned.32x32b.x16.b32 [%0], "
+      "{%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,%16};" ::"r"(taddr),
+      "r"(r[0]), "r"(r[1]), "r"(r[2]), "r"(r[3]), "r"(r[4]), "r"(r[5]), "r"(r[6]), "r"(r[7]),
+      "r"(r[8]), "r"(r[9]), "r"(r[10]), "r"(r[11]), "r"(r[12]), "r"(r[13]), "r"(r[14]),
+      "r"(r[15])
+      : "memory");
+}
+__device__ __forceinline__ void tmem_st_wait() {
+  asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory");
+}
+__device__ __forceinline__ double pair_to_double(uint32_t lo, uint32_t hi) {
+  return __hiloint2double(static_cast<int>(hi), static_cast<int>(lo));
+}
+
+struct TcArgs {
+  const int* Ea;
+  const int* Eb;
+  double* C;
+  unsigned int* error;
+  int64_t M, N, Mp, Np, Kp;
+  double alpha, beta;
+  int S;
+};
+
+__global__ void __launch_bounds__(kThreads, 1)
+ozaki_tc_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
+                TcArgs g) {
+  extern __shared__ unsigned char smem_raw[];
+  // stage ring aligned to 1024 B (the 128-byte swizzle atom), then barriers
+  unsigned char* ring = smem_raw + ((1024u - (smem_u32(smem_raw) & 1023u)) & 1023u);
+  uint64_t* full = reinterpret_cast<uint64_t*>(ring + kStages * kStageBytes);
+  uint64_t* empty = full + kStages;
+  uint64_t* acc_full = empty + kStages;
+  uint64_t* acc_empty = acc_full + 2;
+  uint64_t* mma_done = acc_empty + 2;
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(mma_done + 1);
+  volatile int* abort_flag = reinterpret_cast<volatile int*>(tmem_slot + 1);
+
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  if (threadIdx.x == 0) {
+    for (int st = 0; st < kStages; ++st) {
+      mbar_init(full + st, 1);
+      mbar_init(empty + st, 1);
+    }
+    for (int b = 0; b < 2; ++b) {
+      mbar_init(acc_full + b, 1);
+      mbar_init(acc_empty + b, 4);  // one arrival per epilogue warp
+    }
+    mbar_init(mma_done, 1);
+    *abort_flag = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+  }
+  if (warp == 1) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
+                     smem_u32(tmem_slot)),
+                 "r"(kTmemCols)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem = *tmem_slot;
+
+  const int S = g.S;
+  const int nkb = static_cast<int>(g.Kp / BK);
+  const int64_t i0 = static_cast<int64_t>(blockIdx.y) * BM;
+  const int64_t j0 = static_cast<int64_t>(blockIdx.x) * BN;
+
+  if (warp == 0) {
+    if (lane == 0) {
+      // producer: (weight, slice pair, k block) in the MMA warp's order
+      uint32_t it = 0;
+      bool ok = true;
+      for (int w = 2; ok && w <= S + 1; ++w) {
+        for (int s = 1; ok && s <= w - 1; ++s) {
+          const int t = w - s;
+          for (int kb = 0; kb < nkb; ++kb, ++it) {
+            const int st = static_cast<int>(it % kStages);
+            const uint32_t ph = (it / kStages) & 1u;
+            if (!mbar_wait(empty + st, ph ^ 1u, abort_flag)) {
+              ok = false;
+              break;
+            }
+            unsigned char* a = ring + st * kStageBytes;
+            mbar_arrive_expect_tx(full + st, kStageBytes);
+            tma_load_2d(a, &tmA, full + st, kb * BK, static_cast<int>((s - 1) * g.Mp + i0));
+            tma_load_2d(a + kTileBytes, &tmB, full + st, kb * BK,
+                        static_cast<int>((t - 1) * g.Np + j0));
+          }
+        }
+      }
+      if (!ok) {
+        // wind-down: let the copies already issued land before the CTA exits
+        const uint32_t first = it > static_cast<uint32_t>(kStages) ? it - kStages : 0u;
+        for (uint32_t j = first; j < it; ++j)
+          mbar_wait_drain(full + (j % kStages), (j / kStages) & 1u);
+      }
+    }
+  } else if (warp == 1) {
+    if (lane == 0) {
+      uint32_t it = 0;
+      bool ok = true;
+      int wi = 0;
+      for (int w = 2; ok && w <= S + 1; ++w, ++wi) {
+        const int buf = wi & 1;
+        const uint32_t use = static_cast<uint32_t>(wi >> 1);
+        if (!mbar_wait(acc_empty + buf, (use & 1u) ^ 1u, abort_flag)) {
+          ok = false;
+          break;
+        }
+        tc_fence_after();
+        const uint32_t d_acc = tmem + static_cast<uint32_t>(buf * BN);
+        uint32_t accumulate = 0u;
+        for (int s = 1; ok && s <= w - 1; ++s) {
+          for (int kb = 0; kb < nkb; ++kb, ++it) {
+            const int st = static_cast<int>(it % kStages);
+            if (!mbar_wait(full + st, (it / kStages) & 1u, abort_flag)) {
+              ok = false;
+              break;
+            }
+            tc_fence_after();
+            const uint32_t a_addr = smem_u32(ring + st * kStageBytes);
+            const uint64_t ad = sw128_desc(a_addr), bd = sw128_desc(a_addr + kTileBytes);
+#pragma unroll
+            for (int kk = 0; kk < BK / 16; ++kk) {
+              // advance 16 bf16 (32 B) along K inside the swizzle atom
+              umma_bf16(d_acc, ad + 2u * kk, bd + 2u * kk, accumulate);
+              accumulate = 1u;
+            }
+            umma_commit(empty + st);
+          }
+        }
+        if (ok) umma_commit(acc_full + buf);
+      }
+      // every MMA issued by this thread completes before teardown
+      umma_commit(mma_done);
+      mbar_wait_drain(mma_done, 0u);
+    }
+  } else {
+    // epilogue warps 2..5 own TMEM lane quadrants (warp % 4): tile row = lane
+    const int q = warp & 3;
+    const uint32_t lane_base = static_cast<uint32_t>(32 * q) << 16;
+    bool ok = true;
+    int wi = 0;
+    for (int w = 2; w <= S + 1; ++w, ++wi) {
+      const int buf = wi & 1;
+      const uint32_t use = static_cast<uint32_t>(wi >> 1);
+      if (!mbar_wait(acc_full + buf, use & 1u, abort_flag)) {
+        ok = false;
+        break;
+      }
+      tc_fence_after();
+      const double wscale = scalbn(1.0, -kSliceBits * w);
+      for (int c = 0; c < BN; c += 16) {
+        uint32_t f[16], d0[16], d1[16];
+        tmem_ld16(tmem + lane_base + static_cast<uint32_t>(buf * BN + c), f);
+        if (wi > 0) {
+          tmem_ld16(tmem + lane_base + kAcc64Col + static_cast<uint32_t>(2 * c), d0);
+          tmem_ld16(tmem + lane_base + kAcc64Col + static_cast<uint32_t>(2 * c + 16), d1);
+          tmem_ld_wait(d0);
+          tmem_keep(d1);
+        } else {
+#pragma unroll
+          for (int e = 0; e < 16; ++e) d0[e] = d1[e] = 0u;
+        }
+        tmem_ld_wait(f);
+        tmem_keep(d1);
+#pragma unroll
+        for (int e = 0; e < 8; ++e) {
+          double v0 = pair_to_double(d0[2 * e], d0[2 * e + 1]);
+          double v1 = pair_to_double(d1[2 * e], d1[2 * e + 1]);
+          v0 = fma(static_cast<double>(__uint_as_float(f[e])), wscale, v0);
+          v1 = fma(static_cast<double>(__uint_as_float(f[e + 8])), wscale, v1);
+          d0[2 * e] = static_cast<uint32_t>(__double2loint(v0));
+          d0[2 * e + 1] = static_cast<uint32_t>(__double2hiint(v0));
+          d1[2 * e] = static_cast<uint32_t>(__double2loint(v1));
+          d1[2 * e + 1] = static_cast<uint32_t>(__double2hiint(v1));
+        }
+        tmem_st16(tmem + lane_base + kAcc64Col + static_cast<uint32_t>(2 * c), d0);
+        tmem_st16(tmem + lane_base + kAcc64Col + static_cast<uint32_t>(2 * c + 16), d1);
+      }
+      tmem_st_wait();
+      tc_fence_before();
+      __syncwarp();
+      if (lane == 0) mbar_arrive(acc_empty + buf);
+    }
+    if (ok) {
+      // C = alpha * 2^(Ea+Eb) * acc64 + beta * C
+      const int64_t i = i0 + 32 * q + lane;
+      const bool row_ok = i < g.M;
+      const int ea = row_ok ? g.Ea[i] : 0;
+      for (int c = 0; c < BN; c += 16) {
+        uint32_t d0[16], d1[16];
+        tmem_ld16(tmem + lane_base + kAcc64Col + static_cast<uint32_t>(2 * c), d0);
+        tmem_ld16(tmem + lane_base + kAcc64Col + static_cast<uint32_t>(2 * c + 16), d1);
+        tmem_ld_wait(d0);
+        tmem_keep(d1);
+        if (row_ok) {
+#pragma unroll
+          for (int e = 0; e < 16; ++e) {
+            const int64_t j = j0 + c + e;
+            if (j < g.N) {
+              const double acc = (e < 8) ? pair_to_double(d0[2 * e], d0[2 * e + 1])
+                                         : pair_to_double(d1[2 * e - 16], d1[2 * e - 15]);
+              const double ab = scalbn(acc, ea + g.Eb[j]);
+              double* p = g.C + i * g.N + j;
+              *p = (g.beta == 0.0) ? g.alpha * ab : g.alpha * ab + g.beta * (*p);
+            }
+          }
+        }
+      }
+    }
+    tc_fence_before();
+  }
+  __syncthreads();
+  if (threadIdx.x == 0 && *abort_flag) atomicExch(g.error, 1u);
+  if (warp == 1) {
+    tc_fence_after();
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem),
+                 "r"(kTmemCols)
+                 : "memory");
+  }
+}
+
+PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
+  static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+  static std::once_flag once;
+  std::call_once(once, [] {
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault,
+                                         &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+  });
+  return fn;
+}
+
+// 2-D bf16 view [rows][Kp] with a 64 x 128 box and 128-byte swizzle.
+bool encode_slices(CUtensorMap* map, const void* base, int64_t rows, int64_t Kp) {
+  PFN_cuTensorMapEncodeTiled_v12000 fn = encode_fn();
+  if (!fn) return false;
+  cuuint64_t dims[2] = {static_cast<cuuint64_t>(Kp), static_cast<cuuint64_t>(rows)};
+  cuuint64_t strides[1] = {static_cast<cuuint64_t>(Kp) * 2u};
+  cuuint32_t box[2] = {static_cast<cuuint32_t>(BK), static_cast<cuuint32_t>(BM)};
+  cuuint32_t estr[2] = {1u, 1u};
+  return fn(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, const_cast<void*>(base), dims, strides,
+            box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+            CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
+}  // namespace tc
+
 struct SplitLayout {
   int64_t Mp, Np, Kp;
-  size_t off_ea, off_eb, off_as, off_bt, total;
+  size_t off_err, off_ea, off_eb, off_as, off_bt, total;
 };
 
 SplitLayout split_layout(int64_t m, int64_t n, int64_t k, int S) {
   SplitLayout L;
   L.Mp = round_up(m > 0 ? m : 1, TM);
   L.Np = round_up(n > 0 ? n : 1, TN);
-  L.Kp = round_up(k > 0 ? k : 1, TK);
-  L.off_ea = 0;
-  L.off_eb = round_up(L.Mp * 4, 256);
+  L.Kp = round_up(k > 0 ? k : 1, kPadK);
+  L.off_err = 0;
+  L.off_ea = 256;
+  L.off_eb = L.off_ea + round_up(L.Mp * 4, 256);
   L.off_as = L.off_eb + round_up(L.Np * 4, 256);
   L.off_bt = L.off_as + round_up(static_cast<int64_t>(S) * L.Mp * L.Kp * 2, 256);
   L.total = L.off_bt + round_up(static_cast<int64_t>(S) * L.Np * L.Kp * 2, 256);
@@ -307,6 +716,8 @@ int b200_gemm_split(const double* A, const double* B, double* C, int64_t m, int6
   if (!A || !B || !C || m < 0 || n < 0 || k < 0) return invalid("b200_gemm_split: bad args");
   const int S = slices_of(tune);
   if (S < 2 || S > kMaxSlices) return invalid("b200_gemm_split: slices %d not in [2, %d]", S, kMaxSlices);
+  const int engine = (tune && tune->algo) ? tune->algo : 0;
+  if (engine != 0 && engine != 1) return invalid("b200_gemm_split: engine %d (0 or 1)", engine);
   if (k > kMaxK)
     return invalid("b200_gemm_split: k = %lld exceeds %lld (FP32 exactness bound)",
                    static_cast<long long>(k), static_cast<long long>(kMaxK));
@@ -317,7 +728,10 @@ int b200_gemm_split(const double* A, const double* B, double* C, int64_t m, int6
     return B200_ERR_WORKSPACE;
   }
   if (L.Mp / TM > 65535) return invalid("b200_gemm_split: m too large");
+  if (engine == 0 && device_info().cc_major < 10)
+    return unsupported("b200_gemm_split: the tcgen05 engine needs compute capability 10.x");
   char* w = static_cast<char*>(workspace);
+  unsigned int* err = reinterpret_cast<unsigned int*>(w + L.off_err);
   int* Ea = reinterpret_cast<int*>(w + L.off_ea);
   int* Eb = reinterpret_cast<int*>(w + L.off_eb);
   __nv_bfloat16* As = reinterpret_cast<__nv_bfloat16*>(w + L.off_as);
@@ -331,9 +745,30 @@ int b200_gemm_split(const double* A, const double* B, double* C, int64_t m, int6
                    256, 0, st>>>(A, m, k, Ea, S, L.Mp, L.Kp, As);
   slice_b_kernel<<<dim3(static_cast<unsigned>(ceil_div(L.Np, 32)), static_cast<unsigned>(ceil_div(L.Kp, 32))),
                    dim3(32, 8), 0, st>>>(B, k, n, Eb, S, L.Np, L.Kp, Bt);
-  SplitArgs g{As, Bt, Ea, Eb, C, m, n, L.Mp, L.Np, L.Kp, alpha, beta, S};
-  ozaki_mma_kernel<<<dim3(static_cast<unsigned>(L.Np / TN), static_cast<unsigned>(L.Mp / TM)),
-                     256, 0, st>>>(g);
+  if (engine == 1) {
+    SplitArgs g{As, Bt, Ea, Eb, C, m, n, L.Mp, L.Np, L.Kp, alpha, beta, S};
+    ozaki_mma_kernel<<<dim3(static_cast<unsigned>(L.Np / TN), static_cast<unsigned>(L.Mp / TM)),
+                       256, 0, st>>>(g);
+    return after_launch("b200_gemm_split", 5);
+  }
+  CUtensorMap tmA, tmB;
+  if (!tc::encode_slices(&tmA, As, S * L.Mp, L.Kp) || !tc::encode_slices(&tmB, Bt, S * L.Np, L.Kp))
+    return unsupported("b200_gemm_split: cuTensorMapEncodeTiled unavailable or rejected the slices");
+  const cudaError_t attr = cudaFuncSetAttribute(tc::ozaki_tc_kernel,
+                                                cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                static_cast<int>(tc::kSmemBytes));
+  if (attr != cudaSuccess) {
+    set_error("b200_gemm_split: shared memory attribute: %s", cudaGetErrorString(attr));
+    return B200_ERR_LAUNCH;
+  }
+  const cudaError_t ms = cudaMemsetAsync(err, 0, sizeof(unsigned int), st);
+  if (ms != cudaSuccess) {
+    set_error("b200_gemm_split: clearing the error word: %s", cudaGetErrorString(ms));
+    return B200_ERR_LAUNCH;
+  }
+  tc::TcArgs g{Ea, Eb, C, err, m, n, L.Mp, L.Np, L.Kp, alpha, beta, S};
+  tc::ozaki_tc_kernel<<<dim3(static_cast<unsigned>(L.Np / tc::BN), static_cast<unsigned>(L.Mp / tc::BM)),
+                        tc::kThreads, tc::kSmemBytes, st>>>(tmA, tmB, g);
   return after_launch("b200_gemm_split", 5);
 }
 

@@ -3,6 +3,8 @@
 The bound asked of it is a relative Frobenius error of 1e-13 against FP64;
 the test states it per case, including rows scaled by 2^k, k in [-20, 20]
 (the slicing is per row/column, so row scaling must not cost accuracy)."""
+import ctypes
+
 import numpy as np
 import pytest
 
@@ -14,22 +16,25 @@ pytestmark = pytest.mark.gpu
 REL_FROB = 1e-13
 
 
-def run_split(A, B, C, alpha, beta, slices=None):
+ENGINES = [0, 1]  # tcgen05 (default), mma.sync
+
+
+def run_split(A, B, C, alpha, beta, slices=None, engine=0):
     torch = gu.torch_cuda()
     m, k = A.shape
     n = B.shape[1]
     L = rp.b200()
-    t = rp.Tune(items=slices) if slices else None
-    tp = None
-    import ctypes
-    if t is not None:
-        tp = ctypes.byref(t)
+    t = rp.Tune(items=slices or 0, algo=engine)
+    tp = ctypes.byref(t)
     ws_bytes = L.b200_gemm_split_workspace_bytes(m, n, k, tp)
-    ws = torch.zeros(ws_bytes, dtype=torch.uint8, device="cuda")
+    ws = torch.full((ws_bytes,), 0xAB, dtype=torch.uint8, device="cuda")
     dA, dB, dC = gu.dev(A.ravel()), gu.dev(B.ravel()), gu.dev(C.ravel())
     rp.check(L.b200_gemm_split(dA.data_ptr(), dB.data_ptr(), dC.data_ptr(), m, n, k, alpha,
                                beta, ws.data_ptr(), ws_bytes, tp, gu.stream()), "gemm_split")
-    return gu.host(dC).reshape(m, n)
+    got = gu.host(dC).reshape(m, n)
+    if engine == 0:
+        assert int(gu.host(ws[:4]).view(np.uint32)[0]) == 0, "a bounded wait gave up"
+    return got
 
 
 def reference(A, B, C, alpha, beta):
@@ -38,25 +43,27 @@ def reference(A, B, C, alpha, beta):
     return alpha * (A @ B) + beta * C
 
 
+@pytest.mark.parametrize("engine", ENGINES)
 @pytest.mark.parametrize("m,n,k", [(1, 1, 1), (5, 7, 3), (128, 128, 32), (130, 257, 200),
-                                   (256, 256, 1024), (64, 96, 8192)])
-def test_split_matches_fp64(m, n, k):
+                                   (256, 256, 1024), (64, 96, 8192), (384, 520, 700)])
+def test_split_matches_fp64(m, n, k, engine):
     rng = np.random.default_rng(m + n + k)
     A, B, C = rng.uniform(-1, 1, (m, k)), rng.uniform(-1, 1, (k, n)), rng.uniform(-1, 1, (m, n))
-    got = run_split(A, B, C, 1.5, 1.2)
+    got = run_split(A, B, C, 1.5, 1.2, engine=engine)
     want = reference(A, B, C, 1.5, 1.2)
     err = np.linalg.norm(got - want) / np.linalg.norm(want)
     assert err <= REL_FROB, err
 
 
-def test_split_row_scaled():
+@pytest.mark.parametrize("engine", ENGINES)
+def test_split_row_scaled(engine):
     rng = np.random.default_rng(7)
     m = n = 256
     k = 512
     A = rng.uniform(-1, 1, (m, k)) * np.exp2(rng.integers(-20, 21, m))[:, None]
     B = rng.uniform(-1, 1, (k, n))
     C = rng.uniform(-1, 1, (m, n))
-    got = run_split(A, B, C, 1.5, 1.2)
+    got = run_split(A, B, C, 1.5, 1.2, engine=engine)
     want = reference(A, B, C, 1.5, 1.2)
     err = np.linalg.norm(got - want) / np.linalg.norm(want)
     assert err <= REL_FROB, err
@@ -65,7 +72,8 @@ def test_split_row_scaled():
     assert np.max(row_err) <= 10 * REL_FROB
 
 
-def test_split_nonnegative_worst_case_accumulation():
+@pytest.mark.parametrize("engine", ENGINES)
+def test_split_nonnegative_worst_case_accumulation(engine):
     """All-positive data maximises the FP32 partial sums; the result must
     still meet the bound at the largest K the entry point accepts."""
     rng = np.random.default_rng(3)
@@ -73,7 +81,7 @@ def test_split_nonnegative_worst_case_accumulation():
     k = 8192
     A, B = rng.uniform(0, 1, (m, k)), rng.uniform(0, 1, (k, n))
     C = np.zeros((m, n))
-    got = run_split(A, B, C, 1.0, 0.0)
+    got = run_split(A, B, C, 1.0, 0.0, engine=engine)
     want = A @ B
     err = np.linalg.norm(got - want) / np.linalg.norm(want)
     assert err <= REL_FROB, err
@@ -96,3 +104,23 @@ def test_split_rejects_large_k():
     x = torch.zeros(16, dtype=torch.float64, device="cuda")
     assert L.b200_gemm_split(x.data_ptr(), x.data_ptr(), x.data_ptr(), 1, 1, 8193, 1.0, 0.0,
                              x.data_ptr(), 128, None, None) == rp.B200_ERR_INVALID_ARG
+
+
+def test_engines_bit_identical_when_accumulation_is_exact():
+    """For k <= 1024 every FP32 partial sum is an integer below 2^24, so both
+    engines form identical weight sums and identical FP64 results."""
+    rng = np.random.default_rng(21)
+    A, B = rng.uniform(-1, 1, (200, 1024)), rng.uniform(-1, 1, (1024, 300))
+    C = rng.uniform(-1, 1, (200, 300))
+    a = run_split(A, B, C, 0.75, -0.5, engine=0)
+    b = run_split(A, B, C, 0.75, -0.5, engine=1)
+    assert np.array_equal(a, b)
+
+
+def test_split_rejects_unknown_engine():
+    torch = gu.torch_cuda()
+    L = rp.b200()
+    x = torch.zeros(16, dtype=torch.float64, device="cuda")
+    t = rp.Tune(algo=7)
+    assert L.b200_gemm_split(x.data_ptr(), x.data_ptr(), x.data_ptr(), 1, 1, 1, 1.0, 0.0,
+                             x.data_ptr(), 128, ctypes.byref(t), None) == rp.B200_ERR_INVALID_ARG

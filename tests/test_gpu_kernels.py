@@ -158,8 +158,11 @@ def test_fdtd_2d(nx, ny, ts):
         close(gu.host(g), w)
 
 
-@pytest.mark.parametrize("n", [1, 2, 4095, 4096, 4097, 100003, 1 << 21])
-def test_scan_f64_and_i64(n):
+@pytest.mark.parametrize("n", [1, 2, 4095, 4096, 4097, 8191, 8193, 100003, 1 << 21])
+@pytest.mark.parametrize("items", [0, 16, 32])
+def test_scan_f64_and_i64(n, items):
+    """Default (8192-item) and 4096-item tiles; the calls alternate tile
+    sizes on one workspace, which the epoch-tagged flags must tolerate."""
     rng = np.random.default_rng(n)
     x = rng.uniform(0.0, 1.0, n)
     xi = rng.integers(0, 100, n).astype(np.int64)
@@ -169,11 +172,15 @@ def test_scan_f64_and_i64(n):
     dy = torch.zeros(n, dtype=torch.float64, device="cuda")
     dyi = torch.zeros(n, dtype=torch.int64, device="cuda")
     dx, dxi = dev(x), dev(xi)
+    t = rp.Tune(items=items)
+    other = rp.Tune(items=16 if items != 16 else 32)
     for rep in range(3):  # the workspace is reused across calls
         rp.check(lib().b200_algorithm_scan(dx.data_ptr(), dy.data_ptr(), n, 0.25,
-                                           w.data_ptr(), wsb, None, gu.stream()))
+                                           w.data_ptr(), wsb, ctypes.byref(other), gu.stream()))
+        rp.check(lib().b200_algorithm_scan(dx.data_ptr(), dy.data_ptr(), n, 0.25,
+                                           w.data_ptr(), wsb, ctypes.byref(t), gu.stream()))
         rp.check(lib().b200_algorithm_scan_i64(dxi.data_ptr(), dyi.data_ptr(), n, 7,
-                                               w.data_ptr(), wsb, None, gu.stream()))
+                                               w.data_ptr(), wsb, ctypes.byref(t), gu.stream()))
         want_i = 7 + np.concatenate([[0], np.cumsum(xi)[:-1]])
         assert np.array_equal(gu.host(dyi), want_i)
         want = np.zeros(n)
