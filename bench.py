@@ -416,6 +416,170 @@ def _bandwidth_cases():
             "Algorithm_SCAN": ScanI64}
 
 
+# --------------------------------------------------------------------------
+# every 1-D kernel at 2^27 elements
+# --------------------------------------------------------------------------
+
+# FP64 instructions per element (DADD/DMUL/DFMA and double compares, one
+# correctly rounded divide counted as 8 and exp as 20) and the suite's
+# Bytes/rep per element.  A kernel with fewer FP64 instructions per byte than
+# the GPU's balance point (FP64 instruction rate / HBM copy rate) is
+# HBM-bound; the others are bounded by the FP64 pipe first.
+BW27 = {
+    # kernel: (bytes/elem, fp64 instr/elem, arrays (name, length factor, init), scalars)
+    "Stream_COPY": (16, 0), "Stream_MUL": (16, 1), "Stream_ADD": (24, 1),
+    "Stream_TRIAD": (24, 1), "Stream_DOT": (16, 1), "Basic_DAXPY": (24, 1),
+    "Basic_INIT3": (40, 1), "Basic_MULADDSUB": (40, 3), "Lcals_HYDRO_1D": (24, 3),
+    "Lcals_EOS": (32, 8), "Lcals_FIRST_DIFF": (16, 1), "Lcals_INT_PREDICT": (88, 10),
+    "Lcals_FIRST_MIN": (8, 0), "Lcals_DIFF_PREDICT": (160, 9), "Lcals_PLANCKIAN": (40, 36),
+    "Apps_PRESSURE": (48, 6), "Apps_ENERGY": (216, 40), "Algorithm_SCAN": (16, 0),
+    "Algorithm_REDUCE_SUM": (8, 1),
+}
+
+
+def bw27_run(torch, rp, name, n, seed):
+    """Allocates one kernel's arrays (uniform [0.5, 1.5) on the device) and
+    returns (run(stream) -> status, keep-alive list)."""
+    L = rp.b200()
+    sid = [0]
+
+    def u(m):
+        t = torch.empty(m, dtype=torch.float64, device="cuda")
+        rp.check(L.b200_init_uniform(t.data_ptr(), m, seed, sid[0], 0.5, 1.5, None), "init")
+        sid[0] += 1
+        return t
+
+    def z(m, dtype=torch.float64):
+        return torch.zeros(m, dtype=dtype, device="cuda")
+
+    P = lambda t: t.data_ptr()
+    if name == "Stream_COPY":
+        a, c = u(n), z(n)
+        return (lambda s: L.b200_stream_copy(P(a), P(c), n, None, s)), [a, c]
+    if name == "Stream_MUL":
+        b, c = z(n), u(n)
+        return (lambda s: L.b200_stream_mul(P(b), P(c), 0.5, n, None, s)), [b, c]
+    if name == "Stream_ADD":
+        a, b, c = u(n), u(n), z(n)
+        return (lambda s: L.b200_stream_add(P(a), P(b), P(c), n, None, s)), [a, b, c]
+    if name == "Stream_TRIAD":
+        a, b, c = z(n), u(n), u(n)
+        return (lambda s: L.b200_stream_triad(P(a), P(b), P(c), 0.5, n, None, s)), [a, b, c]
+    if name == "Stream_DOT":
+        a, b, acc = u(n), u(n), z(1)
+        wb = L.b200_reduce_workspace_bytes(n, None)
+        ws = z(wb, torch.uint8)
+        return (lambda s: L.b200_stream_dot(P(a), P(b), n, 0.0, P(acc), P(ws), wb, None, s)), \
+            [a, b, acc, ws]
+    if name == "Basic_DAXPY":
+        y, x = z(n), u(n)
+        return (lambda s: L.b200_basic_daxpy(P(y), P(x), 0.5, n, None, s)), [y, x]
+    if name in ("Basic_INIT3", "Basic_MULADDSUB"):
+        o1, o2, o3, i1, i2 = z(n), z(n), z(n), u(n), u(n)
+        fn = L.b200_basic_init3 if name == "Basic_INIT3" else L.b200_basic_muladdsub
+        return (lambda s: fn(P(o1), P(o2), P(o3), P(i1), P(i2), n, None, s)), \
+            [o1, o2, o3, i1, i2]
+    if name == "Lcals_HYDRO_1D":
+        x, y, zz = z(n + 12), u(n + 12), u(n + 12)
+        return (lambda s: L.b200_lcals_hydro_1d(P(x), P(y), P(zz), 0.0979, 0.1958, 0.0979, n,
+                                                None, s)), [x, y, zz]
+    if name == "Lcals_EOS":
+        x, y, zz, uu = z(n + 7), u(n + 7), u(n + 7), u(n + 7)
+        return (lambda s: L.b200_lcals_eos(P(x), P(y), P(zz), P(uu), 0.0979, 0.1958, 0.0979, n,
+                                           None, s)), [x, y, zz, uu]
+    if name == "Lcals_FIRST_DIFF":
+        x, y = z(n + 1), u(n + 1)
+        return (lambda s: L.b200_lcals_first_diff(P(x), P(y), n, None, s)), [x, y]
+    if name == "Lcals_INT_PREDICT":
+        px = u(13 * n)
+        return (lambda s: L.b200_lcals_int_predict(P(px), 0.1, 0.2, 0.3, 0.4, 0.5, 0.6, 0.7,
+                                                   0.8, n, None, s)), [px]
+    if name == "Lcals_FIRST_MIN":
+        x = u(n)
+        x[n // 3] = -0.5
+        loc = z(1, torch.int64)
+        wb = L.b200_reduce_workspace_bytes(n, None)
+        ws = z(wb, torch.uint8)
+        return (lambda s: L.b200_lcals_first_min(P(x), n, 0.5, 0, P(loc), None, P(ws), wb,
+                                                 None, s)), [x, loc, ws]
+    if name == "Lcals_DIFF_PREDICT":
+        px, cx = z(14 * n), u(14 * n)
+        return (lambda s: L.b200_lcals_diff_predict(P(px), P(cx), n, None, s)), [px, cx]
+    if name == "Lcals_PLANCKIAN":
+        x, y, uu, v, w = u(n), z(n), u(n), u(n), z(n)
+        return (lambda s: L.b200_lcals_planckian(P(x), P(y), P(uu), P(v), P(w), n, None, s)), \
+            [x, y, uu, v, w]
+    if name == "Apps_PRESSURE":
+        comp, bvc, pn, eo, vn = u(n), z(n), z(n), u(n), u(n)
+        return (lambda s: L.b200_apps_pressure(P(comp), P(bvc), P(pn), P(eo), P(vn), 0.5,
+                                               1e-7, 0.0, 1.2, n, None, s)), \
+            [comp, bvc, pn, eo, vn]
+    if name == "Apps_ENERGY":
+        arrs = [z(n)] + [u(n) for _ in range(4)] + [z(n)] + [u(n) for _ in range(9)]
+        return (lambda s: L.b200_apps_energy(*[P(t) for t in arrs], 1.1, 1e-7, 0.0, 1e-7, n,
+                                             None, s)), arrs
+    if name == "Algorithm_SCAN":
+        x = torch.empty(n, dtype=torch.int64, device="cuda")
+        rp.check(L.b200_init_uniform_i64(P(x), n, seed, 0, 0, 100, None))
+        y = z(n, torch.int64)
+        wb = L.b200_scan_workspace_bytes(n)
+        ws = z(wb, torch.uint8)
+        return (lambda s: L.b200_algorithm_scan_i64(P(x), P(y), n, 0, P(ws), wb, None, s)), \
+            [x, y, ws]
+    if name == "Algorithm_REDUCE_SUM":
+        x, out = u(n), z(1)
+        wb = L.b200_reduce_workspace_bytes(n, None)
+        ws = z(wb, torch.uint8)
+        return (lambda s: L.b200_algorithm_reduce_sum(P(x), n, 0.0, P(out), P(ws), wb, None,
+                                                      s)), [x, out, ws]
+    raise KeyError(name)
+
+
+def measure_bw27(torch, rp, stream, peaks, fp64_instr_rate, seed, n=1 << 27, steps=5,
+                 warmup=3, only=None):
+    """Times every 1-D kernel at n elements (inputs far larger than L2, so no
+    flush is needed) and reports GB/s against the copy peak, the kernel's
+    bound (HBM or FP64 pipe) and geomeans over all kernels and over the
+    HBM-bound ones."""
+    s = stream.cuda_stream
+    balance = fp64_instr_rate / (peaks["hbm_gbs"] * 1e9)  # FP64 instr per byte
+    rows = []
+    for name, (bpe, ipe) in BW27.items():
+        if only and name not in only and name.split("_", 1)[1] not in only:
+            continue
+        run, keep = bw27_run(torch, rp, name, n, seed)
+        for _ in range(warmup):
+            rp.check(run(s), name)
+        ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+              for _ in range(steps)]
+        torch.cuda.synchronize()
+        for e0, e1 in ev:
+            e0.record(stream)
+            rp.check(run(s), name)
+            e1.record(stream)
+        torch.cuda.synchronize()
+        t = sorted(e0.elapsed_time(e1) for e0, e1 in ev)[len(ev) // 2] / 1e3
+        gbs = bpe * n / t / 1e9
+        bound = "hbm" if ipe / bpe <= balance else "fp64"
+        # the kernel's own ceiling: HBM time or FP64-pipe time, whichever is longer
+        t_floor = max(bpe * n / (peaks["hbm_gbs"] * 1e9), ipe * n / fp64_instr_rate)
+        rows.append({"kernel": name, "ms": round(t * 1e3, 4), "gbs": round(gbs, 1),
+                     "pct_hbm": round(100 * gbs / peaks["hbm_gbs"], 2), "bound": bound,
+                     "fp64_instr_per_byte": round(ipe / bpe, 4),
+                     "pct_of_own_bound": round(100 * t_floor / t, 2)})
+        del run, keep
+        torch.cuda.empty_cache()
+    hbm_rows = [r for r in rows if r["bound"] == "hbm"]
+    return {
+        "n": n, "balance_fp64_instr_per_byte": round(balance, 4),
+        "geomean_pct_hbm_all": round(geomean([r["pct_hbm"] for r in rows]), 2),
+        "geomean_pct_hbm_hbm_bound": round(geomean([r["pct_hbm"] for r in hbm_rows]), 2),
+        "geomean_pct_of_own_bound_all": round(geomean([r["pct_of_own_bound"] for r in rows]),
+                                              2),
+        "per_kernel": rows,
+    }
+
+
 # workload -> list of (kernel, size, oracle kwargs for the CPU baseline)
 WORKLOADS = {
     "bandwidth_stencil": {
@@ -682,6 +846,47 @@ def measure_gemm(torch, rp, stream, sizes=(1024, 4096, 8192), seed=4793):
     return out
 
 
+BATCH_KERNELS = ["Stream_COPY", "Stream_MUL", "Stream_ADD", "Stream_TRIAD", "Stream_DOT",
+                 "Lcals_HYDRO_1D", "Lcals_HYDRO_2D", "Lcals_EOS", "Lcals_FIRST_DIFF",
+                 "Lcals_INT_PREDICT", "Lcals_FIRST_MIN", "Apps_DEL_DOT_VEC_2D", "Apps_VOL3D",
+                 "Apps_ENERGY", "Apps_PRESSURE", "Basic_DAXPY", "Basic_INIT3",
+                 "Basic_MULADDSUB", "Lcals_DIFF_PREDICT", "Lcals_PLANCKIAN"]
+
+
+def measure_graph_batch(rp, seed, reps=100):
+    """The 20-kernel small-size suite: sizes log-uniform in [2^12, 2^18] per
+    kernel (seeded), FP64 uniform [0.5, 1.5) data, `reps` reps.  The whole
+    group's rep loop runs once as individual library calls and once as one
+    captured CUDA graph, with the library's default launch shapes and again
+    with shapes the autotuner measured for these kernels and sizes."""
+    import random
+    import tempfile
+    rng = random.Random(seed)
+    sizes = {k: int(round(2.0 ** rng.uniform(12.0, 18.0))) for k in BATCH_KERNELS}
+    base = ["--graph-batch", str(reps), "-k", *BATCH_KERNELS, "--size-map",
+            *[f"{k}={n}" for k, n in sizes.items()], "--init", "uniform", "--seed", str(seed)]
+    out = {"kernels": len(BATCH_KERNELS), "reps": reps, "sizes": sizes}
+    with tempfile.TemporaryDirectory() as tmp:
+        table = os.path.join(tmp, "autotuned.txt")
+        for label, extra in (("default_shapes", []), ("autotuned", ["--autotune", table])):
+            r = rp.graph_batch(base + extra)
+            out[label] = {
+                "launch_time_ms": round(r["launch_time_s"] * 1e3, 3),
+                "graph_time_ms": round(r["graph_time_s"] * 1e3, 3),
+                "per_rep_launch_us": round(r["launch_time_s"] / reps * 1e6, 2),
+                "per_rep_graph_us": round(r["graph_time_s"] / reps * 1e6, 2),
+                "launches_per_rep": r["launches_per_rep"],
+                "speedup": round(r["launch_time_s"] / r["graph_time_s"], 2),
+            }
+        shapes = {}
+        for line in open(table):
+            f = line.split("#", 1)[0].split()
+            if f:
+                shapes[f[0]] = " ".join(f[3:]) or "default"
+        out["autotuned"]["shapes"] = shapes
+    return out
+
+
 def measure_fp64_peak(torch, rp, stream):
     """FP64 FMA rate of this GPU from the library's probe (best of 3)."""
     L = rp.b200()
@@ -781,6 +986,13 @@ def main():
     ap.add_argument("--gemm", choices=["auto", "on", "off"], default="auto",
                     help="split-precision vs native FP64 GEMM leg (auto: on for the "
                          "default workload without --kernels)")
+    ap.add_argument("--gemm-sizes", type=lambda s: [int(x) for x in s.split(",")],
+                    default=[1024, 4096, 8192], help="square sizes of the GEMM leg")
+    ap.add_argument("--extras", choices=["auto", "on", "off", "bw", "batch"], default="auto",
+                    help="every 1-D kernel at 2^27 elements and the 20-kernel graph batch "
+                         "(auto: on for the default workload without --kernels)")
+    ap.add_argument("--bw-size", type=int, default=1 << 27,
+                    help="element count of the all-kernels bandwidth leg")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3) if args.impl == "gb300" else args.warmup
     rank = int(os.environ.get("RANK", "0"))
@@ -825,7 +1037,19 @@ def main():
     if args.gemm == "on" or (args.gemm == "auto" and not args.kernels and rank == 0):
         import torch
         import rajaperf_gb300 as rp
-        gemm = measure_gemm(torch, rp, torch.cuda.current_stream())
+        gemm = measure_gemm(torch, rp, torch.cuda.current_stream(), sizes=args.gemm_sizes)
+    bw27 = batch = None
+    extras = args.extras
+    if extras == "auto":
+        extras = "on" if (not args.kernels and rank == 0) else "off"
+    if extras in ("on", "bw") and rank == 0:
+        import torch
+        import rajaperf_gb300 as rp
+        bw27 = measure_bw27(torch, rp, torch.cuda.current_stream(), peaks,
+                            res["fp64"]["fma_per_s"], args.seed, n=args.bw_size)
+    if extras in ("on", "batch") and rank == 0:
+        import rajaperf_gb300 as rp
+        batch = measure_graph_batch(rp, args.seed)
     value = res["value"]
     if dist:
         import torch
@@ -852,6 +1076,8 @@ def main():
         "cpu_baseline": cpu, "clocks": res["clocks"], "gpu_launches": res["launches"],
         "fp64_peak_gflops": round(res["fp64"]["gflops"], 1),
         "gemm_split_vs_fp64": gemm,
+        "bandwidth_all_1d": bw27,
+        "graph_batch": batch,
         "per_kernel": [{k: (round(v, 4) if isinstance(v, float) else v) for k, v in p.items()}
                        for p in res["per_kernel"]],
     }

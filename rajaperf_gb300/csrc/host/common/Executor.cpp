@@ -1,5 +1,6 @@
 #include "Executor.hpp"
 
+#include "Autotuner.hpp"
 #include "GraphRepRunner.hpp"
 #include "TuningTable.hpp"
 
@@ -88,6 +89,7 @@ void Executor::reportRunSummary(std::ostream& os) const {
 void Executor::runSuite() {
   if (!ok() || run_params.getInputState() == RunParams::DryRun) return;
   checkCuda(cudaFree(nullptr), "cuda context");
+  if (!run_params.getAutotuneFile().empty()) runAutotune();
   if (run_params.graphBatch()) {
     runGraphBatch();
     return;
@@ -154,6 +156,25 @@ void Executor::collectResults() {
       r.bytes_per_rep = k->getBytesPerRep();
       r.flops_per_rep = k->getFLOPsPerRep();
       results_.push_back(r);
+    }
+  }
+}
+
+// Measures launch shapes for the selected kernels (Autotuner.hpp), installs
+// the winners ahead of any loaded tuning table and writes them out.
+void Executor::runAutotune() {
+  autotune_ = autotune(kernels_, tunings_);
+  std::vector<TuningTable::Entry> entries;
+  for (const AutotuneRecord& r : autotune_)
+    entries.push_back(TuningTable::Entry{r.kernel, r.size, r.size, r.best});
+  TuningTable::instance().prepend(entries);
+  if (!writeAutotuneTable(autotune_, run_params.getAutotuneFile()))
+    throw std::runtime_error("cannot write " + run_params.getAutotuneFile());
+  if (run_params.showProgress()) {
+    for (const AutotuneRecord& r : autotune_) {
+      getCout() << "  autotune " << r.kernel << " size " << r.size << ": "
+                << TuningTable::format(TuningTable::Entry{r.kernel, r.size, r.size, r.best})
+                << " " << r.best_s * 1e6 << " us (default " << r.default_s * 1e6 << ")\n";
     }
   }
 }

@@ -12,6 +12,7 @@
 // issued as individual launches.
 #pragma once
 
+#include "Autotuner.hpp"
 #include "KernelBase.hpp"
 #include "RunParams.hpp"
 
@@ -64,8 +65,10 @@ class Executor {
 
   const std::vector<RunResult>& results() const { return results_; }
   const GraphBatchResult& graphBatchResult() const { return batch_; }
+  const std::vector<AutotuneRecord>& autotuneRecords() const { return autotune_; }
 
  private:
+  void runAutotune();
   void runGraphBatch();
   void collectResults();
   void writeTimingCSV(const std::string& fname, int mode) const;
@@ -80,6 +83,7 @@ class Executor {
   std::vector<RunResult> results_;
   std::vector<std::string> errors_;           // per (kernel,tuning) run errors
   GraphBatchResult batch_;
+  std::vector<AutotuneRecord> autotune_;
 };
 
 }  // namespace rajaperf

@@ -139,6 +139,8 @@ RunParams::RunParams(int argc, const char* const* argv) {
       }
     } else if (opt == "--tuning-table") {
       tuning_table_file = takeValue(i, opt);
+    } else if (opt == "--autotune") {
+      autotune_file = takeValue(i, opt);
     } else if (opt == "--graph-batch") {
       graph_batch = true;
       if (i + 1 < args.size() && !isOption(args[i + 1])) {
@@ -249,6 +251,9 @@ std::string RunParams::usage() {
       "  --polybench_tsteps T         override Polybench time steps\n"
       "  --size-map K=N,...           per-kernel sizes\n"
       "  --tuning-table FILE          tuning table (kernel size-bucket params)\n"
+      "  --autotune FILE              measure launch shapes for the selected\n"
+      "                               kernels and sizes, use them and write\n"
+      "                               them to FILE as a tuning table\n"
       "  --graph-batch [R]            capture every kernel's R-rep loop into\n"
       "                               one CUDA graph and compare with launches\n"
       "  -od DIR, -of PREFIX          report directory and file prefix\n"

@@ -51,6 +51,7 @@ class RunParams {
   double getKernelSize(KernelID kid) const;
 
   const std::string& getTuningTableFile() const { return tuning_table_file; }
+  const std::string& getAutotuneFile() const { return autotune_file; }
   const std::string& getOutputDirName() const { return outdir; }
   const std::string& getOutputFilePrefix() const { return outfile_prefix; }
 
@@ -88,6 +89,7 @@ class RunParams {
 
   std::map<KernelID, double> size_map;
   std::string tuning_table_file;
+  std::string autotune_file;
   std::string outdir = ".";
   std::string outfile_prefix = "RAJAPerf";
 

@@ -77,6 +77,11 @@ bool TuningTable::load(const std::string& path, std::string* error) {
 
 bool TuningTable::lookup(const std::string& kernel, long long size,
                          b200_tune* out) const {
+  if (has_override_ && override_.kernel == kernel && size >= override_.min_size &&
+      (override_.max_size < 0 || size <= override_.max_size)) {
+    *out = override_.tune;
+    return true;
+  }
   for (const Entry& e : entries_) {
     if (e.kernel == kernel && size >= e.min_size &&
         (e.max_size < 0 || size <= e.max_size)) {
@@ -85,6 +90,10 @@ bool TuningTable::lookup(const std::string& kernel, long long size,
     }
   }
   return false;
+}
+
+void TuningTable::prepend(const std::vector<Entry>& entries) {
+  entries_.insert(entries_.begin(), entries.begin(), entries.end());
 }
 
 std::string TuningTable::format(const Entry& e) {

@@ -32,14 +32,25 @@ class TuningTable {
   bool parse(const std::string& text, std::string* error);
   void clear() { entries_.clear(); }
 
-  // Returns true and fills `out` when an entry covers (kernel, size).
+  // Returns true and fills `out` when an entry covers (kernel, size).  An
+  // override (set by the autotuner while it measures) is consulted first.
   bool lookup(const std::string& kernel, long long size, b200_tune* out) const;
+
+  // Puts entries ahead of the current ones (the autotuner's winners).
+  void prepend(const std::vector<Entry>& entries);
+  void setOverride(const Entry& e) {
+    override_ = e;
+    has_override_ = true;
+  }
+  void clearOverride() { has_override_ = false; }
 
   const std::vector<Entry>& entries() const { return entries_; }
   static std::string format(const Entry& e);
 
  private:
   std::vector<Entry> entries_;
+  Entry override_{};
+  bool has_override_ = false;
 };
 
 // Parses "key=value" launch-shape fields into `t`; false on an unknown key.

@@ -123,3 +123,28 @@ def test_bad_command_lines():
         rp.run_suite(["--size", 10, "--sizefact", 2])
     with pytest.raises(RuntimeError, match="not available"):
         rp.run_suite(["-v", "Base_CUDA"])
+
+
+def test_autotune_table_and_graph_batch(tmp_path):
+    """--autotune measures shapes for the selected kernels at their sizes,
+    writes a table --tuning-table reads back, and the graph batch runs with
+    it; checksums with the tuned shapes still match Base_Seq."""
+    table = tmp_path / "autotuned.txt"
+    kernels = ["Stream_TRIAD", "Stream_DOT", "Lcals_FIRST_MIN", "Lcals_EOS", "Lcals_HYDRO_2D",
+               "Algorithm_SCAN", "Polybench_JACOBI_2D"]
+    b = rp.graph_batch(["--graph-batch", 5, "-k", *kernels, "--size", 65537,
+                        "--autotune", str(table)])
+    assert b["kernels"] == len(kernels) and b["reps"] == 5
+    assert b["launch_time_s"] > 0 and b["graph_time_s"] > 0 and b["launches_per_rep"] > 0
+    entries = [ln.split("#", 1)[0].split() for ln in table.read_text().splitlines()]
+    tuned = {e[0] for e in entries if e}
+    # every kernel with more than one candidate shape gets an entry
+    assert tuned == set(kernels) - {"Polybench_JACOBI_2D"}, tuned
+    for e in entries:
+        if e:
+            assert e[1] == e[2] and all("=" in kv for kv in e[3:]), e
+    for kernel in ["Stream_TRIAD", "Stream_DOT", "Lcals_FIRST_MIN", "Lcals_EOS"]:
+        rec = [r for r in RECORDS if r["kernel"] == kernel and r["size"] == 65537][0]
+        res = rp.run_suite(["--size", rec["size"], "--checkrun", rec["reps"], "-k", kernel,
+                            "-t", "default", "--disable-warmup", "--tuning-table", str(table)])
+        _check(kernel, rec, res[0])
