@@ -386,6 +386,35 @@ def _bandwidth_cases():
             return self.L.b200_polybench_heat_3d(self.A.data_ptr(), self.B.data_ptr(), self.N,
                                                  self.tsteps, None, s)
 
+    class Fdtd2D(Case):
+        name = "Polybench_FDTD_2D"
+
+        def __init__(self, torch, rp, seed, size, tsteps=40):
+            super().__init__(torch, rp, seed)
+            nx = ny = self.nx = self.ny = int(math.sqrt(size) + 1 + math.sqrt(2) - 1)
+            self.tsteps = tsteps
+            self.launches = 2 * tsteps
+            self.hz = self.zeros(nx * ny)
+            self.ex, self.ey = self.uniform(nx * ny), self.uniform(nx * ny)
+            self.fict = self.uniform(tsteps)
+            rd = 8 * (1 + (nx - 1) * ny + nx * ny + nx * (ny - 1) + nx * ny +
+                      (nx - 1) * (ny - 1) + (nx - 1) * ny + nx * (ny - 1))
+            wr = 8 * (ny + (nx - 1) * ny + nx * (ny - 1) + (nx - 1) * (ny - 1))
+            self.bytes_per_rep = (rd + wr) * tsteps
+            self.flops_per_rep = tsteps * (3 * (nx - 1) * ny + 3 * nx * (ny - 1) +
+                                           5 * (nx - 1) * (ny - 1))
+
+        def inputs(self):
+            return [self.ex, self.ey, self.hz, self.fict]
+
+        def outputs(self):
+            return [self.hz]
+
+        def run(self, s):
+            return self.L.b200_polybench_fdtd_2d(self.ex.data_ptr(), self.ey.data_ptr(),
+                                                 self.hz.data_ptr(), self.fict.data_ptr(),
+                                                 self.nx, self.ny, self.tsteps, None, s)
+
     class ScanI64(Case):
         name = "Algorithm_SCAN"
 
@@ -413,16 +442,17 @@ def _bandwidth_cases():
     return {"Lcals_HYDRO_2D": Hydro2D, "Lcals_EOS": Eos, "Lcals_FIRST_DIFF": FirstDiff,
             "Lcals_FIRST_MIN": FirstMin, "Apps_DEL_DOT_VEC_2D": DelDotVec2D,
             "Polybench_JACOBI_2D": Jacobi2D, "Polybench_HEAT_3D": Heat3D,
-            "Algorithm_SCAN": ScanI64}
+            "Polybench_FDTD_2D": Fdtd2D, "Algorithm_SCAN": ScanI64}
 
 
 # --------------------------------------------------------------------------
 # every 1-D kernel at 2^27 elements
 # --------------------------------------------------------------------------
 
-# FP64 instructions per element (DADD/DMUL/DFMA and double compares, one
-# correctly rounded divide counted as 8 and exp as 20) and the suite's
-# Bytes/rep per element.  A kernel with fewer FP64 instructions per byte than
+# FP64-pipe instructions per element, as ncu counts them for these kernels
+# (sm__inst_executed_pipe_fp64 x 32 / elements; DADD/DMUL/DFMA, double
+# compares, the divides' and exp's FP64 steps), and the suite's Bytes/rep per
+# element.  A kernel with fewer FP64 instructions per byte than
 # the GPU's balance point (FP64 instruction rate / HBM copy rate) is
 # HBM-bound; the others are bounded by the FP64 pipe first.
 BW27 = {
@@ -431,8 +461,8 @@ BW27 = {
     "Stream_TRIAD": (24, 1), "Stream_DOT": (16, 1), "Basic_DAXPY": (24, 1),
     "Basic_INIT3": (40, 1), "Basic_MULADDSUB": (40, 3), "Lcals_HYDRO_1D": (24, 3),
     "Lcals_EOS": (32, 8), "Lcals_FIRST_DIFF": (16, 1), "Lcals_INT_PREDICT": (88, 10),
-    "Lcals_FIRST_MIN": (8, 0), "Lcals_DIFF_PREDICT": (160, 9), "Lcals_PLANCKIAN": (40, 36),
-    "Apps_PRESSURE": (48, 6), "Apps_ENERGY": (216, 40), "Algorithm_SCAN": (16, 0),
+    "Lcals_FIRST_MIN": (8, 0), "Lcals_DIFF_PREDICT": (160, 9), "Lcals_PLANCKIAN": (40, 32),
+    "Apps_PRESSURE": (48, 6), "Apps_ENERGY": (216, 29), "Algorithm_SCAN": (16, 0),
     "Algorithm_REDUCE_SUM": (8, 1),
 }
 
@@ -598,6 +628,17 @@ WORKLOADS = {
                     ("Stream_ADD", 1 << 27), ("Stream_TRIAD", 1 << 27),
                     ("Stream_DOT", 1 << 27)],
     },
+    "large": {
+        "description": "FP64, uniform [0.5,1.5) from a seed: Stream COPY/MUL/ADD/TRIAD at "
+                       "2^28 (2 GiB per array); HEAT_3D 768^3, 100 tsteps; FDTD_2D 8192x8192, "
+                       "100 tsteps; JACOBI_2D 16384x16384, 40 tsteps",
+        "kernels": [("Stream_COPY", 1 << 28), ("Stream_MUL", 1 << 28),
+                    ("Stream_ADD", 1 << 28), ("Stream_TRIAD", 1 << 28),
+                    ("Polybench_HEAT_3D", 766 ** 3), ("Polybench_FDTD_2D", 8191 * 8192),
+                    ("Polybench_JACOBI_2D", 16382 * 16382)],
+        "params": {"Polybench_HEAT_3D": {"tsteps": 100}, "Polybench_FDTD_2D": {"tsteps": 100},
+                   "Polybench_JACOBI_2D": {"tsteps": 40}},
+    },
 }
 DEFAULT_WORKLOAD = "bandwidth_stencil"
 
@@ -613,7 +654,9 @@ def build_cases(torch, rp, workload, seed, only=None):
     registry = {}
     registry.update(_stream_cases())
     registry.update(_bandwidth_cases())
-    return [registry[k](torch, rp, seed, n) for k, n in workload_kernels(workload, only)]
+    params = WORKLOADS[workload].get("params", {})
+    return [registry[k](torch, rp, seed, n, **params.get(k, {}))
+            for k, n in workload_kernels(workload, only)]
 
 
 # --------------------------------------------------------------------------
@@ -767,7 +810,10 @@ def run_gpu(args, rank, world):
                 "fp64": {"achieved_gflops": round(dom["gflops"], 1),
                          "peak_gflops": round(fp64["gflops"], 1),
                          "frac": round(dom["fp64_frac"], 4),
-                         "peak_source": "measured in this run (b200_probe_dfma, FMA = 2 flops)"}}
+                         "peak_source": "measured in this run: max of the DFMA probe and "
+                                        "native FP64 GEMM 2048^3 (FMA = 2 flops)",
+                         "probe_gflops": fp64["probe_gflops"],
+                         "dgemm_gflops": fp64["dgemm_gflops"]}}
     return {
         "value": value, "step_s": step_s, "per_kernel": per_kernel, "e2e": e2e,
         "roofline": roofline, "clocks": clocks, "launches": launches, "wall_s": wall,
@@ -856,8 +902,9 @@ BATCH_KERNELS = ["Stream_COPY", "Stream_MUL", "Stream_ADD", "Stream_TRIAD", "Str
 def measure_graph_batch(rp, seed, reps=100):
     """The 20-kernel small-size suite: sizes log-uniform in [2^12, 2^18] per
     kernel (seeded), FP64 uniform [0.5, 1.5) data, `reps` reps.  The whole
-    group's rep loop runs once as individual library calls and once as one
-    captured CUDA graph, with the library's default launch shapes and again
+    group's rep loop runs once as individual library calls and as one
+    captured CUDA graph (one branch per kernel, branches concurrent; also a
+    single-chain graph), with the library's default launch shapes and again
     with shapes the autotuner measured for these kernels and sizes."""
     import random
     import tempfile
@@ -873,10 +920,12 @@ def measure_graph_batch(rp, seed, reps=100):
             out[label] = {
                 "launch_time_ms": round(r["launch_time_s"] * 1e3, 3),
                 "graph_time_ms": round(r["graph_time_s"] * 1e3, 3),
+                "graph_serial_time_ms": round(r["graph_serial_time_s"] * 1e3, 3),
                 "per_rep_launch_us": round(r["launch_time_s"] / reps * 1e6, 2),
                 "per_rep_graph_us": round(r["graph_time_s"] / reps * 1e6, 2),
                 "launches_per_rep": r["launches_per_rep"],
                 "speedup": round(r["launch_time_s"] / r["graph_time_s"], 2),
+                "speedup_serial_graph": round(r["launch_time_s"] / r["graph_serial_time_s"], 2),
             }
         shapes = {}
         for line in open(table):
@@ -888,12 +937,15 @@ def measure_graph_batch(rp, seed, reps=100):
 
 
 def measure_fp64_peak(torch, rp, stream):
-    """FP64 FMA rate of this GPU from the library's probe (best of 3)."""
+    """FP64 FMA rate of this GPU, measured two ways in this run: the library's
+    DFMA probe (independent FMA chains, best of 4) and the native FP64 GEMM
+    (b200_gemm_f64, 2048^3, best of 3: all DFMA).  The higher of the two is
+    the FP64 peak the FP64-bound kernels are measured against."""
+    import ctypes
     L = rp.b200()
     out = torch.empty(int(L.b200_probe_dfma_threads()), dtype=torch.float64, device="cuda")
-    import ctypes
     cnt = ctypes.c_int64(0)
-    best = 0.0
+    probe = 0.0
     for _ in range(4):
         e0 = torch.cuda.Event(enable_timing=True)
         e1 = torch.cuda.Event(enable_timing=True)
@@ -901,9 +953,25 @@ def measure_fp64_peak(torch, rp, stream):
         rp.check(L.b200_probe_dfma(out.data_ptr(), 512, ctypes.byref(cnt), stream.cuda_stream))
         e1.record(stream)
         torch.cuda.synchronize()
-        rate = cnt.value / (e0.elapsed_time(e1) / 1e3)
-        best = max(best, rate)
-    return {"fma_per_s": best, "gflops": 2.0 * best / 1e9}
+        probe = max(probe, cnt.value / (e0.elapsed_time(e1) / 1e3))
+    n = 2048
+    g = torch.Generator(device="cuda").manual_seed(1)
+    A = torch.rand(n, n, dtype=torch.float64, device="cuda", generator=g)
+    B = torch.rand(n, n, dtype=torch.float64, device="cuda", generator=g)
+    C = torch.zeros(n, n, dtype=torch.float64, device="cuda")
+    gemm = 0.0
+    for _ in range(4):
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        rp.check(L.b200_gemm_f64(A.data_ptr(), B.data_ptr(), C.data_ptr(), n, n, n, 1.0, 0.0,
+                                 None, stream.cuda_stream))
+        e1.record(stream)
+        torch.cuda.synchronize()
+        gemm = max(gemm, float(n) ** 3 / (e0.elapsed_time(e1) / 1e3))
+    best = max(probe, gemm)
+    return {"fma_per_s": best, "gflops": 2.0 * best / 1e9,
+            "probe_gflops": round(2.0 * probe / 1e9, 1), "dgemm_gflops": round(2.0 * gemm / 1e9, 1)}
 
 
 def run_e2e(torch, rp, cases, s, stream, args, peaks):
@@ -956,6 +1024,7 @@ def run_cpu(workload, seed, threads, peaks, only=None):
     fr, per = [], []
     for kname, size in workload_kernels(workload, only):
         kw = dict(WORKLOAD_ORACLE_ARGS.get(kname, {}))
+        kw.update(WORKLOADS[workload].get("params", {}).get(kname, {}))
         r = oracle.run(kname, size=size, reps=1, init="uniform", seed=seed,
                        threads=threads, skip_checksum=True, **kw)
         gbs = r["bytes_per_rep"] / max(r["time_s"], 1e-9) / 1e9

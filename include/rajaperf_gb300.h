@@ -44,8 +44,11 @@ typedef struct rp_batch_result {
   int32_t reserved;
   int64_t reps;
   int64_t launches_per_rep;
-  double launch_time_s;      /* reps x kernels as individual launches    */
-  double graph_time_s;       /* the same work as one captured CUDA graph */
+  double launch_time_s;       /* reps x kernels as individual launches     */
+  double graph_time_s;        /* the same work as one CUDA graph with one
+                                 branch per kernel (branches concurrent)    */
+  double graph_serial_time_s; /* the same work as one CUDA graph holding a
+                                 single chain in launch order               */
 } rp_batch_result;
 
 /* Last error on this host thread. */

@@ -62,7 +62,8 @@ class RpResult(ctypes.Structure):
 class RpBatchResult(ctypes.Structure):
     _fields_ = [("kernels", ctypes.c_int32), ("reserved", ctypes.c_int32),
                 ("reps", ctypes.c_int64), ("launches_per_rep", ctypes.c_int64),
-                ("launch_time_s", ctypes.c_double), ("graph_time_s", ctypes.c_double)]
+                ("launch_time_s", ctypes.c_double), ("graph_time_s", ctypes.c_double),
+                ("graph_serial_time_s", ctypes.c_double)]
 
 
 _C_TYPES = {
@@ -205,7 +206,8 @@ def graph_batch(args: list[str]) -> dict:
         raise RuntimeError(f"rp_graph_batch failed ({st}): {lib.rp_last_error().decode()}")
     return {"kernels": out.kernels, "reps": out.reps,
             "launches_per_rep": out.launches_per_rep,
-            "launch_time_s": out.launch_time_s, "graph_time_s": out.graph_time_s}
+            "launch_time_s": out.launch_time_s, "graph_time_s": out.graph_time_s,
+            "graph_serial_time_s": out.graph_serial_time_s}
 
 
 def declared_functions(header: str) -> list[str]:

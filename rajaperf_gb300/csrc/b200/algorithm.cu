@@ -2,14 +2,15 @@
 //
 // SCAN is a single-pass decoupled-lookback scan: every CTA takes the next
 // tile id from a counter (so a CTA only ever waits on tiles already owned by
-// running CTAs), scans its tile in shared memory, publishes the tile
-// aggregate, looks back over its predecessors' aggregates / inclusive
-// prefixes with one warp, then publishes its own inclusive prefix.  Flags
-// carry a launch epoch, so the workspace never needs re-zeroing between calls
-// (and the call can be captured in a CUDA graph): the last CTA to finish
-// resets the tile counter and advances the epoch.  Every wait is bounded; a
-// wait that gives up sets the workspace error word and the call's results are
-// invalid (b200_scan_workspace_error reads it back).
+// running CTAs).  A dedicated lookback warp starts walking its predecessors'
+// aggregates / inclusive prefixes at once, while eight loader warps stage
+// the tile in shared memory, reduce it and publish its aggregate; the
+// lookback warp then publishes the tile's inclusive prefix and the loaders
+// write the tile out.  Flags carry a launch epoch, so the workspace never
+// needs re-zeroing between calls (and the call can be captured in a CUDA
+// graph): the last CTA to finish resets the tile counter and advances the
+// epoch.  Every wait is bounded; a wait that gives up sets the error word of
+// the workspace header (byte offset 16) and the call's results are invalid.
 #include "b200_internal.cuh"
 #include "b200_reduce.cuh"
 
@@ -17,7 +18,8 @@ using namespace b200;
 
 namespace {
 
-constexpr int kScanBlock = 256;
+constexpr int kScanBlock = 256;                         // loader threads
+constexpr int kScanThreads = kScanBlock + 32;           // + the lookback warp
 constexpr int kScanItemsMin = 16;                       // smallest tile: 4096 items
 constexpr int kScanItemsDefault = 32;                   // default tile: 8192 items
 constexpr int kScanTileMin = kScanBlock * kScanItemsMin;
@@ -32,8 +34,6 @@ struct ScanHeader {
   unsigned int pad[59];
 };
 static_assert(sizeof(ScanHeader) == 256, "scan header is 256 bytes");
-
-__device__ __forceinline__ int padded(int i) { return i + (i >> 4); }
 
 __device__ __forceinline__ unsigned long long ld_acquire(const unsigned long long* p) {
   unsigned long long v;
@@ -76,14 +76,28 @@ __device__ __forceinline__ unsigned long long wait_flag(const unsigned long long
   return f;
 }
 
-// Tile = kScanBlock * IT items, staged in dynamic shared memory (padded so
-// the per-thread runs of IT consecutive items are conflict-free).
+__device__ __forceinline__ void named_sync(int id, int count) {
+  asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(count) : "memory");
+}
+__device__ __forceinline__ void named_arrive(int id, int count) {
+  asm volatile("bar.arrive %0, %1;" ::"r"(id), "r"(count) : "memory");
+}
+
+// One CTA per tile of kScanBlock * IT items.  Warp 0 is the lookback warp:
+// it walks the predecessors' flags as soon as the tile id is known, while
+// warps 1..8 (the loaders) stage the tile in shared memory (padded so the
+// per-thread runs of IT consecutive items are conflict-free), reduce it and
+// publish the aggregate.  The lookback warp then publishes the inclusive
+// prefix, and the loaders write the tile out.  Named barriers: 1 = loaders
+// only, 2 = aggregate ready (loaders arrive, lookback warp waits), 3 =
+// exclusive prefix ready (lookback warp arrives, loaders wait).
 template <typename T, int IT>
-__global__ void __launch_bounds__(kScanBlock)
+__global__ void __launch_bounds__(kScanThreads)
 scan_kernel(const T* __restrict__ x, T* __restrict__ y, int64_t n, T init,
             ScanHeader* __restrict__ hdr, unsigned long long* __restrict__ flags,
             T* __restrict__ aggs, T* __restrict__ incs) {
   constexpr int kTile = kScanBlock * IT;
+  constexpr int kPadShift = (IT == 32) ? 5 : 4;
   extern __shared__ __align__(16) unsigned char s_raw[];
   T* s_tile = reinterpret_cast<T*>(s_raw);
   __shared__ T s_warp[kScanBlock / 32];
@@ -92,6 +106,7 @@ scan_kernel(const T* __restrict__ x, T* __restrict__ y, int64_t n, T init,
   __shared__ unsigned int s_tile_id;
   __shared__ unsigned long long s_epoch;
   __shared__ bool s_last;
+  auto pad = [](int i) { return i + (i >> kPadShift); };
 
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   if (tid == 0) {
@@ -104,60 +119,12 @@ scan_kernel(const T* __restrict__ x, T* __restrict__ y, int64_t n, T init,
   const unsigned long long AGG = epoch * 4 + 1, INC = epoch * 4 + 2;
   const int64_t base = static_cast<int64_t>(tile) * kTile;
 
-  // striped, coalesced load into shared memory
-  if (base + kTile <= n) {
-#pragma unroll
-    for (int u = 0; u < IT; ++u) {
-      const int k = u * kScanBlock + tid;
-      s_tile[padded(k)] = __ldcs(x + base + k);
-    }
-  } else {
-#pragma unroll
-    for (int u = 0; u < IT; ++u) {
-      const int k = u * kScanBlock + tid;
-      const int64_t i = base + k;
-      s_tile[padded(k)] = (i < n) ? __ldcs(x + i) : T(0);
-    }
-  }
-  __syncthreads();
-
-  // Each thread sums its IT consecutive items; a block scan of the thread
-  // totals gives every thread its offset inside the tile.
-  T run = T(0);
-#pragma unroll
-  for (int u = 0; u < IT; ++u) run += s_tile[padded(tid * IT + u)];
-  T incl = warp_inclusive_scan(run);
-  if (lane == 31) s_warp[warp] = incl;
-  __syncthreads();
   if (warp == 0) {
-    T w = (lane < kScanBlock / 32) ? s_warp[lane] : T(0);
-    T wi = warp_inclusive_scan(w);
-    if (lane < kScanBlock / 32) s_warp[lane] = wi - w;  // exclusive warp offsets
-    if (lane == kScanBlock / 32 - 1) s_agg = wi;         // tile aggregate
-  }
-  __syncthreads();
-  const T thread_excl = s_warp[warp] + (incl - run);
-  const T agg = s_agg;
-
-  // Warp 0 resolves the tile's prefix (decoupled lookback) while the other
-  // warps turn their items into tile-local exclusive prefixes in place.  One
-  // lookback round examines 32 * kLookbackPerLane predecessors, nearest
-  // first (window slot w = j * 32 + lane is predecessor p_hi - w), so that
-  // the INC frontier keeps up with the rate at which tiles start.
-  if (warp == 0) {
+    // ---- lookback warp ----
+    // One round examines 32 * kLookbackPerLane predecessors, nearest first
+    // (window slot w = j * 32 + lane is predecessor p_hi - w).
     T exclusive = init;
-    if (tile == 0) {
-      if (lane == 0) {
-        incs[0] = init + agg;
-        __threadfence();
-        st_release(&flags[0], INC);
-      }
-    } else {
-      if (lane == 0) {
-        aggs[tile] = agg;
-        __threadfence();
-        st_release(&flags[tile], AGG);
-      }
+    if (tile > 0) {
       T acc = T(0);
       int64_t p_hi = static_cast<int64_t>(tile) - 1;  // nearest unexamined predecessor
       bool done = false;
@@ -194,42 +161,88 @@ scan_kernel(const T* __restrict__ x, T* __restrict__ y, int64_t n, T init,
         p_hi -= 32 * kLookbackPerLane;
       }
       exclusive = acc;
-      if (lane == 0) {
-        incs[tile] = exclusive + agg;
-        __threadfence();
-        st_release(&flags[tile], INC);
+    }
+    named_sync(2, kScanThreads);  // the loaders have the tile aggregate
+    if (lane == 0) {
+      incs[tile] = exclusive + s_agg;
+      __threadfence();
+      st_release(&flags[tile], INC);
+      s_excl = exclusive;
+    }
+    named_arrive(3, kScanThreads);
+  } else {
+    // ---- loaders ----
+    const int ltid = tid - 32, lwarp = warp - 1;
+    if (base + kTile <= n) {
+#pragma unroll
+      for (int u = 0; u < IT; ++u) {
+        const int k = u * kScanBlock + ltid;
+        s_tile[pad(k)] = __ldcs(x + base + k);
+      }
+    } else {
+#pragma unroll
+      for (int u = 0; u < IT; ++u) {
+        const int k = u * kScanBlock + ltid;
+        const int64_t i = base + k;
+        s_tile[pad(k)] = (i < n) ? __ldcs(x + i) : T(0);
       }
     }
-    if (lane == 0) s_excl = exclusive;
-  }
-  {
-    T r = thread_excl;
+    named_sync(1, kScanBlock);
+    // Each thread sums its IT consecutive items; a scan of the thread totals
+    // gives every thread its offset inside the tile.
+    T run = T(0);
 #pragma unroll
-    for (int u = 0; u < IT; ++u) {
-      const int k = padded(tid * IT + u);
-      const T xv = s_tile[k];
-      s_tile[k] = r;
-      r += xv;
+    for (int u = 0; u < IT; ++u) run += s_tile[pad(ltid * IT + u)];
+    const T incl = warp_inclusive_scan(run);
+    if (lane == 31) s_warp[lwarp] = incl;
+    named_sync(1, kScanBlock);
+    if (lwarp == 0) {
+      const T w = (lane < kScanBlock / 32) ? s_warp[lane] : T(0);
+      const T wi = warp_inclusive_scan(w);
+      if (lane < kScanBlock / 32) s_warp[lane] = wi - w;  // exclusive warp offsets
+      if (lane == kScanBlock / 32 - 1) {
+        s_agg = wi;                                       // tile aggregate
+        if (tile > 0) {
+          aggs[tile] = wi;
+          __threadfence();
+          st_release(&flags[tile], AGG);
+        }
+      }
     }
-  }
-  __syncthreads();
-  const T prefix = s_excl;
-  if (base + kTile <= n) {
+    named_sync(1, kScanBlock);
+    named_arrive(2, kScanThreads);
+    // tile-local exclusive prefixes, in place
+    {
+      T r = s_warp[lwarp] + (incl - run);
 #pragma unroll
-    for (int u = 0; u < IT; ++u) {
-      const int k = u * kScanBlock + tid;
-      __stcs(y + base + k, prefix + s_tile[padded(k)]);
+      for (int u = 0; u < IT; ++u) {
+        const int k = pad(ltid * IT + u);
+        const T xv = s_tile[k];
+        s_tile[k] = r;
+        r += xv;
+      }
     }
-  } else {
+    named_sync(1, kScanBlock);
+    named_sync(3, kScanThreads);  // the lookback warp has the exclusive prefix
+    const T prefix = s_excl;
+    if (base + kTile <= n) {
 #pragma unroll
-    for (int u = 0; u < IT; ++u) {
-      const int k = u * kScanBlock + tid;
-      const int64_t i = base + k;
-      if (i < n) __stcs(y + i, prefix + s_tile[padded(k)]);
+      for (int u = 0; u < IT; ++u) {
+        const int k = u * kScanBlock + ltid;
+        __stcs(y + base + k, prefix + s_tile[pad(k)]);
+      }
+    } else {
+#pragma unroll
+      for (int u = 0; u < IT; ++u) {
+        const int k = u * kScanBlock + ltid;
+        const int64_t i = base + k;
+        if (i < n) __stcs(y + i, prefix + s_tile[pad(k)]);
+      }
     }
   }
 
   // the last CTA to finish prepares the workspace for the next call
+  __syncthreads();
   if (tid == 0) {
     __threadfence();
     unsigned int prev = atomicAdd(&hdr->done_counter, 1u);
@@ -250,7 +263,7 @@ int64_t scan_tiles_max(int64_t n) { return ceil_div(n > 0 ? n : 1, kScanTileMin)
 template <typename T, int IT>
 int launch_scan_it(const T* x, T* y, int64_t n, T init, char* w, cudaStream_t st) {
   constexpr int kTile = kScanBlock * IT;
-  constexpr size_t kSmem = static_cast<size_t>(kTile + kTile / 16) * sizeof(T);
+  constexpr size_t kSmem = static_cast<size_t>(kTile + kTile / IT) * sizeof(T);
   const cudaError_t attr = cudaFuncSetAttribute(
       scan_kernel<T, IT>, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(kSmem));
   if (attr != cudaSuccess) {
@@ -263,7 +276,7 @@ int launch_scan_it(const T* x, T* y, int64_t n, T init, char* w, cudaStream_t st
   unsigned long long* flags = reinterpret_cast<unsigned long long*>(w + 256);
   T* aggs = reinterpret_cast<T*>(w + 256 + slots * 8);
   T* incs = reinterpret_cast<T*>(w + 256 + slots * 16);
-  scan_kernel<T, IT><<<static_cast<int>(tiles), kScanBlock, kSmem, st>>>(x, y, n, init, hdr,
+  scan_kernel<T, IT><<<static_cast<int>(tiles), kScanThreads, kSmem, st>>>(x, y, n, init, hdr,
                                                                           flags, aggs, incs);
   return B200_OK;
 }

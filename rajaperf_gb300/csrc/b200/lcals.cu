@@ -62,27 +62,45 @@ struct DiffPredict {
   double* px;
   const double* __restrict__ cx;
   int64_t o;
+  // The suite reads each plane of px before overwriting it and never reads
+  // it again, and for o = n >= 1 the planes are disjoint: so all ten loads
+  // are issued first (independent, in flight together) and the ten stores
+  // follow.  The same differences, in the same order, as the macro.
   __device__ void operator()(int64_t i) const {
+    double p[9];  // planes 4..12 before the update
+#pragma unroll
+    for (int k = 0; k < 9; ++k) p[k] = px[i + o * (4 + k)];
     double ar, br, cr;
+    double q4, q5, q6, q7, q8, q9, q10, q11, q12, q13;
     ar = ld(cx + i + o * 4);
-    br = ar - px[i + o * 4];
-    px[i + o * 4] = ar;
-    cr = br - px[i + o * 5];
-    px[i + o * 5] = br;
-    ar = cr - px[i + o * 6];
-    px[i + o * 6] = cr;
-    br = ar - px[i + o * 7];
-    px[i + o * 7] = ar;
-    cr = br - px[i + o * 8];
-    px[i + o * 8] = br;
-    ar = cr - px[i + o * 9];
-    px[i + o * 9] = cr;
-    br = ar - px[i + o * 10];
-    px[i + o * 10] = ar;
-    cr = br - px[i + o * 11];
-    px[i + o * 11] = br;
-    px[i + o * 13] = cr - px[i + o * 12];
-    px[i + o * 12] = cr;
+    br = ar - p[0];
+    q4 = ar;
+    cr = br - p[1];
+    q5 = br;
+    ar = cr - p[2];
+    q6 = cr;
+    br = ar - p[3];
+    q7 = ar;
+    cr = br - p[4];
+    q8 = br;
+    ar = cr - p[5];
+    q9 = cr;
+    br = ar - p[6];
+    q10 = ar;
+    cr = br - p[7];
+    q11 = br;
+    q13 = cr - p[8];
+    q12 = cr;
+    px[i + o * 4] = q4;
+    px[i + o * 5] = q5;
+    px[i + o * 6] = q6;
+    px[i + o * 7] = q7;
+    px[i + o * 8] = q8;
+    px[i + o * 9] = q9;
+    px[i + o * 10] = q10;
+    px[i + o * 11] = q11;
+    px[i + o * 12] = q12;
+    px[i + o * 13] = q13;
   }
 };
 
@@ -151,7 +169,7 @@ hydro2d_body23(const double* __restrict__ za, const double* __restrict__ zb,
 // result is the smallest index holding the minimum (or initloc when the
 // initial value is not beaten).  Compares run on order-preserving integer keys
 // (order_key), which order exactly as '<' on the doubles.
-template <int BS, int IT>
+template <int BS, int IT, bool VEC>
 __global__ void __launch_bounds__(BS)
 first_min_kernel(const double* __restrict__ x, int64_t n, double xmin_init,
                  int64_t initloc, int64_t* __restrict__ minloc_out,
@@ -166,19 +184,48 @@ first_min_kernel(const double* __restrict__ x, int64_t n, double xmin_init,
                                      : order_key(__double_as_longlong(xmin_init)),
                     initloc};
   KeyLoc m = init;
-  for (int64_t t0 = static_cast<int64_t>(blockIdx.x) * (BS * IT); t0 < n;
-       t0 += static_cast<int64_t>(gridDim.x) * (BS * IT)) {
-    long long v[IT];
+  if (VEC) {
+    // 16-byte loads of element pairs; a thread still meets its indices in
+    // increasing order, so strict '<' keeps the first minimum it sees.
+    const longlong2* xv = reinterpret_cast<const longlong2*>(x);
+    const int64_t nv = n >> 1;
+    for (int64_t t0 = static_cast<int64_t>(blockIdx.x) * (BS * IT); t0 < nv;
+         t0 += static_cast<int64_t>(gridDim.x) * (BS * IT)) {
+      longlong2 v[IT];
 #pragma unroll
-    for (int u = 0; u < IT; ++u) {
-      int64_t i = t0 + u * BS + threadIdx.x;
-      v[u] = (i < n) ? __ldg(xb + i) : 0LL;
+      for (int u = 0; u < IT; ++u) {
+        const int64_t iv = t0 + u * BS + threadIdx.x;
+        v[u] = (iv < nv) ? __ldg(xv + iv) : make_longlong2(0LL, 0LL);
+      }
+#pragma unroll
+      for (int u = 0; u < IT; ++u) {
+        const int64_t iv = t0 + u * BS + threadIdx.x;
+        if (iv < nv) {
+          const long long k0 = order_key(v[u].x), k1 = order_key(v[u].y);
+          if (k0 < m.key) { m.key = k0; m.loc = 2 * iv; }
+          if (k1 < m.key) { m.key = k1; m.loc = 2 * iv + 1; }
+        }
+      }
     }
+    if ((n & 1) && blockIdx.x == 0 && threadIdx.x == 0) {  // odd tail element
+      const long long k = order_key(__ldg(xb + n - 1));
+      if (k < m.key) { m.key = k; m.loc = n - 1; }
+    }
+  } else {
+    for (int64_t t0 = static_cast<int64_t>(blockIdx.x) * (BS * IT); t0 < n;
+         t0 += static_cast<int64_t>(gridDim.x) * (BS * IT)) {
+      long long v[IT];
 #pragma unroll
-    for (int u = 0; u < IT; ++u) {
-      int64_t i = t0 + u * BS + threadIdx.x;
-      long long k = order_key(v[u]);
-      if (i < n && k < m.key) { m.key = k; m.loc = i; }
+      for (int u = 0; u < IT; ++u) {
+        int64_t i = t0 + u * BS + threadIdx.x;
+        v[u] = (i < n) ? __ldg(xb + i) : 0LL;
+      }
+#pragma unroll
+      for (int u = 0; u < IT; ++u) {
+        int64_t i = t0 + u * BS + threadIdx.x;
+        long long k = order_key(v[u]);
+        if (i < n && k < m.key) { m.key = k; m.loc = i; }
+      }
     }
   }
   m = block_keyloc<BS>(m, smem);
@@ -289,7 +336,9 @@ int b200_lcals_first_min(const double* x, int64_t n, double xmin_init, int64_t i
   int block = (tune && tune->block_size) ? tune->block_size : 256;
   int items = (tune && tune->items) ? tune->items : 8;
   if (!valid_block(block)) return invalid("b200_lcals_first_min: bad block size %d", block);
-  int grid = reduce_grid(n, tune, block, items);
+  // 16-byte pair loads when x is aligned (tune->vec == 1 forces 8-byte loads)
+  const bool vec = aligned16(x) && !(tune && tune->vec == 1) && n >= 2;
+  int grid = reduce_grid(vec ? (n + 1) / 2 : n, tune, block, items);
   size_t need = reduce_ws_bytes_for_grid(grid);
   if (!workspace || workspace_bytes < need) {
     set_error("b200_lcals_first_min: workspace %zu bytes, need %zu", workspace_bytes, need);
@@ -298,9 +347,15 @@ int b200_lcals_first_min(const double* x, int64_t n, double xmin_init, int64_t i
   unsigned int* counter = static_cast<unsigned int*>(workspace);
   KeyLoc* partials = reinterpret_cast<KeyLoc*>(static_cast<char*>(workspace) + 256);
   cudaStream_t st = as_stream(stream);
-  B200_DISPATCH_BLOCK(block, BS, B200_DISPATCH_ITEMS(items, IT,
-    first_min_kernel<BS, IT><<<grid, BS, 0, st>>>(x, n, xmin_init, initloc, minloc, minval,
-                                                  partials, counter)));
+  if (vec) {
+    B200_DISPATCH_BLOCK(block, BS, B200_DISPATCH_ITEMS(items, IT,
+      first_min_kernel<BS, IT, true><<<grid, BS, 0, st>>>(x, n, xmin_init, initloc, minloc,
+                                                          minval, partials, counter)));
+  } else {
+    B200_DISPATCH_BLOCK(block, BS, B200_DISPATCH_ITEMS(items, IT,
+      first_min_kernel<BS, IT, false><<<grid, BS, 0, st>>>(x, n, xmin_init, initloc, minloc,
+                                                           minval, partials, counter)));
+  }
   return after_launch("b200_lcals_first_min");
 }
 

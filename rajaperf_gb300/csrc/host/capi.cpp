@@ -92,6 +92,7 @@ int rp_graph_batch(int argc, const char* const* argv, rp_batch_result* out) {
     out->launches_per_rep = b.launches_per_rep;
     out->launch_time_s = b.launch_time;
     out->graph_time_s = b.graph_time;
+    out->graph_serial_time_s = b.graph_serial_time;
     if (!b.error.empty()) {
       g_error = b.error;
       return RP_ERR_RUN;

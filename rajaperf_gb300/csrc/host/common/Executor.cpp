@@ -211,16 +211,30 @@ void Executor::runGraphBatch() {
     auto t1 = std::chrono::steady_clock::now();
     batch_.launch_time = std::chrono::duration<double>(t1 - t0).count();
 
-    GraphRepRunner runner(reps);
-    runner.capture(reps, [&](b200_stream_t s) {
-      for (const auto& b : bodies) b(s);
-    });
-    checkCuda(cudaDeviceSynchronize(), "sync");
-    auto g0 = std::chrono::steady_clock::now();
-    runner.launch();
-    runner.synchronize();
-    auto g1 = std::chrono::steady_clock::now();
-    batch_.graph_time = std::chrono::duration<double>(g1 - g0).count();
+    // one chain: every rep of every kernel in launch order
+    {
+      GraphRepRunner runner(reps);
+      runner.capture(reps, [&](b200_stream_t s) {
+        for (const auto& b : bodies) b(s);
+      });
+      checkCuda(cudaDeviceSynchronize(), "sync");
+      auto g0 = std::chrono::steady_clock::now();
+      runner.launch();
+      runner.synchronize();
+      auto g1 = std::chrono::steady_clock::now();
+      batch_.graph_serial_time = std::chrono::duration<double>(g1 - g0).count();
+    }
+    // one branch per kernel: the kernels share no data, so only each
+    // kernel's own reps stay ordered and the branches run concurrently
+    {
+      ParallelGraph graph(bodies, reps);
+      checkCuda(cudaDeviceSynchronize(), "sync");
+      auto g0 = std::chrono::steady_clock::now();
+      graph.launch();
+      graph.synchronize();
+      auto g1 = std::chrono::steady_clock::now();
+      batch_.graph_time = std::chrono::duration<double>(g1 - g0).count();
+    }
     batch_.kernels = static_cast<int>(kernels_.size());
     batch_.reps = reps;
   } catch (const std::exception& e) {
@@ -245,7 +259,8 @@ void Executor::outputRunData() {
     f << "{\"kernels\": " << batch_.kernels << ", \"reps\": " << batch_.reps
       << ", \"launches_per_rep\": " << batch_.launches_per_rep
       << ", \"launch_time_s\": " << std::setprecision(9) << batch_.launch_time
-      << ", \"graph_time_s\": " << batch_.graph_time << ", \"error\": \""
+      << ", \"graph_time_s\": " << batch_.graph_time
+      << ", \"graph_serial_time_s\": " << batch_.graph_serial_time << ", \"error\": \""
       << batch_.error << "\"}\n";
     return;
   }

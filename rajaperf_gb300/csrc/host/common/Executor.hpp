@@ -46,7 +46,8 @@ struct GraphBatchResult {
   long long reps = 0;
   long long launches_per_rep = 0;  // library launches of one rep of the group
   double launch_time = 0.0;        // seconds, individual launches
-  double graph_time = 0.0;         // seconds, one captured graph
+  double graph_serial_time = 0.0;  // seconds, one graph, all reps in one chain
+  double graph_time = 0.0;         // seconds, one graph, one branch per kernel
   std::string error;
 };
 

@@ -83,4 +83,72 @@ void GraphRepRunner::synchronize() {
             "cudaStreamSynchronize");
 }
 
+ParallelGraph::ParallelGraph(const std::vector<GraphRepRunner::RepBody>& bodies,
+                             int64_t reps) {
+  cudaStream_t main = nullptr;
+  checkCuda(cudaStreamCreateWithFlags(&main, cudaStreamNonBlocking), "cudaStreamCreate");
+  stream_ = main;
+  std::vector<cudaStream_t> branch(bodies.size(), nullptr);
+  std::vector<cudaEvent_t> done(bodies.size(), nullptr);
+  cudaEvent_t fork = nullptr;
+  cudaGraph_t graph = nullptr;
+  auto cleanup = [&]() {
+    for (cudaStream_t b : branch)
+      if (b) cudaStreamDestroy(b);
+    for (cudaEvent_t e : done)
+      if (e) cudaEventDestroy(e);
+    if (fork) cudaEventDestroy(fork);
+    if (graph) cudaGraphDestroy(graph);
+  };
+  try {
+    checkCuda(cudaEventCreateWithFlags(&fork, cudaEventDisableTiming), "cudaEventCreate");
+    for (size_t i = 0; i < bodies.size(); ++i) {
+      checkCuda(cudaStreamCreateWithFlags(&branch[i], cudaStreamNonBlocking),
+                "cudaStreamCreate");
+      checkCuda(cudaEventCreateWithFlags(&done[i], cudaEventDisableTiming), "cudaEventCreate");
+    }
+    checkCuda(cudaStreamBeginCapture(main, cudaStreamCaptureModeThreadLocal),
+              "cudaStreamBeginCapture");
+    try {
+      checkCuda(cudaEventRecord(fork, main), "cudaEventRecord");
+      for (size_t i = 0; i < bodies.size(); ++i) {
+        checkCuda(cudaStreamWaitEvent(branch[i], fork, 0), "cudaStreamWaitEvent");
+        for (int64_t r = 0; r < reps; ++r) bodies[i](reinterpret_cast<b200_stream_t>(branch[i]));
+        checkCuda(cudaEventRecord(done[i], branch[i]), "cudaEventRecord");
+        checkCuda(cudaStreamWaitEvent(main, done[i], 0), "cudaStreamWaitEvent");
+      }
+    } catch (...) {
+      cudaGraph_t g = nullptr;
+      cudaStreamEndCapture(main, &g);
+      if (g) cudaGraphDestroy(g);
+      throw;
+    }
+    checkCuda(cudaStreamEndCapture(main, &graph), "cudaStreamEndCapture");
+    cudaGraphExec_t exec = nullptr;
+    checkCuda(cudaGraphInstantiate(&exec, graph, 0), "cudaGraphInstantiate");
+    exec_ = exec;
+  } catch (...) {
+    cleanup();
+    cudaStreamDestroy(main);
+    stream_ = nullptr;
+    throw;
+  }
+  cleanup();
+}
+
+ParallelGraph::~ParallelGraph() {
+  if (exec_) cudaGraphExecDestroy(static_cast<cudaGraphExec_t>(exec_));
+  if (stream_) cudaStreamDestroy(static_cast<cudaStream_t>(stream_));
+}
+
+void ParallelGraph::launch() {
+  checkCuda(cudaGraphLaunch(static_cast<cudaGraphExec_t>(exec_),
+                            static_cast<cudaStream_t>(stream_)),
+            "cudaGraphLaunch");
+}
+
+void ParallelGraph::synchronize() {
+  checkCuda(cudaStreamSynchronize(static_cast<cudaStream_t>(stream_)), "cudaStreamSynchronize");
+}
+
 }  // namespace rajaperf

@@ -13,6 +13,7 @@
 
 #include <cstdint>
 #include <functional>
+#include <vector>
 
 namespace rajaperf {
 
@@ -46,6 +47,25 @@ class GraphRepRunner {
   b200_stream_t stream_ = nullptr;
   void* chunk_graph_ = nullptr;     // cudaGraphExec_t of `chunk_` reps
   void* tail_graph_ = nullptr;      // cudaGraphExec_t of the remainder
+};
+
+// One CUDA graph over several independent rep bodies: capture forks from a
+// capture stream into one stream per body, records that body's `reps` reps
+// there (so they stay in order) and joins every branch back.  The bodies must
+// share no device data; the branches then run concurrently on the GPU.
+class ParallelGraph {
+ public:
+  ParallelGraph(const std::vector<GraphRepRunner::RepBody>& bodies, int64_t reps);
+  ~ParallelGraph();
+  ParallelGraph(const ParallelGraph&) = delete;
+  ParallelGraph& operator=(const ParallelGraph&) = delete;
+
+  void launch();
+  void synchronize();
+
+ private:
+  void* stream_ = nullptr;  // cudaStream_t the graph is launched on
+  void* exec_ = nullptr;    // cudaGraphExec_t
 };
 
 }  // namespace rajaperf
