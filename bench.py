@@ -233,6 +233,7 @@ def _bandwidth_cases():
             self.bytes_per_rep = (8 * (4 * n + 4 * n + 4 * (kn - 2) * (jn - 2)) +
                                   8 * 6 * (kn - 2) * (jn - 2))
             self.flops_per_rep = 44 * (kn - 2) * (jn - 2)
+            self.fp64_instr_per_rep = None  # BODY1 28 per point; BODY2+3 not counted
 
         def inputs(self):
             return self.arr[2:9]
@@ -254,6 +255,7 @@ def _bandwidth_cases():
             self.y, self.z, self.u = (self.uniform(n + 7) for _ in range(3))
             self.bytes_per_rep = 16 * n + 8 * (n + 7) + 8 * n
             self.flops_per_rep = 16 * n
+            self.fp64_instr_per_rep = 8 * n
 
         def inputs(self):
             return [self.y, self.z, self.u]
@@ -276,6 +278,7 @@ def _bandwidth_cases():
             self.y = self.uniform(n + 1)
             self.bytes_per_rep = 8 * (n + 1) + 8 * n
             self.flops_per_rep = n
+            self.fp64_instr_per_rep = n
 
         def inputs(self):
             return [self.y]
@@ -301,6 +304,7 @@ def _bandwidth_cases():
             self.ws = self.zeros(self.ws_bytes, dtype=torch.uint8)
             self.bytes_per_rep = 8 + 8 + 8 * n + 8 + 8
             self.flops_per_rep = 0
+            self.fp64_instr_per_rep = 0
 
         def inputs(self):
             return [self.x]
@@ -328,6 +332,7 @@ def _bandwidth_cases():
             self.div = self.zeros(nn)
             self.bytes_per_rep = 8 * self.nz + 4 * 8 * n_real_nodes + 8 * self.nz
             self.flops_per_rep = 54 * self.nz
+            self.fp64_instr_per_rep = 59 * self.nz
 
         def inputs(self):
             return [self.x, self.y, self.xdot, self.ydot, self.zones]
@@ -352,6 +357,7 @@ def _bandwidth_cases():
             self.A, self.B = self.uniform(N * N), self.uniform(N * N)
             self.bytes_per_rep = (8 * (N * N - 4) * 2 + 8 * (N - 2) * (N - 2) * 2) * tsteps
             self.flops_per_rep = tsteps * 10 * (N - 2) * (N - 2)
+            self.fp64_instr_per_rep = tsteps * 10 * (N - 2) * (N - 2)
 
         def inputs(self):
             return [self.A, self.B]
@@ -375,6 +381,7 @@ def _bandwidth_cases():
             inner = (N - 2) ** 3
             self.bytes_per_rep = (8 * (N ** 3 - 12 * (N - 2) - 8) * 2 + 8 * inner * 2) * tsteps
             self.flops_per_rep = tsteps * 30 * inner
+            self.fp64_instr_per_rep = tsteps * 22 * inner
 
         def inputs(self):
             return [self.A, self.B]
@@ -428,6 +435,7 @@ def _bandwidth_cases():
             self.ws = self.zeros(self.ws_bytes, dtype=torch.uint8)
             self.bytes_per_rep = 16 * n
             self.flops_per_rep = n
+            self.fp64_instr_per_rep = 0
 
         def inputs(self):
             return [self.x]
@@ -784,9 +792,13 @@ def run_gpu(args, rank, world):
         avg_s = sum(ms) / len(ms) / 1e3
         gbs = c.bytes_per_rep / avg_s / 1e9
         gfs = c.flops_per_rep / avg_s / 1e9
+        fi = getattr(c, "fp64_instr_per_rep", None)
         per_kernel.append({"kernel": c.name, "ms": avg_s * 1e3, "gbs": gbs,
                            "frac": gbs / peaks["hbm_gbs"], "bytes": c.bytes_per_rep,
                            "gflops": gfs, "fp64_frac": gfs / fp64["gflops"],
+                           # FP64-pipe instructions (ncu counts) / time / peak rate
+                           "fp64_pipe_frac": (round(fi / avg_s / fp64["fma_per_s"], 4)
+                                              if fi is not None else None),
                            "launches": c.launches})
     step_s = sum(p["ms"] for p in per_kernel) / 1e3
     if dist:
@@ -800,16 +812,20 @@ def run_gpu(args, rank, world):
 
     dom = max(per_kernel, key=lambda p: p["ms"])
     tr = traffic.get(dom["kernel"])
+    # per launch: the rep's algorithmic bytes and time divided by its launches
     roofline = {"bound": "hbm", "kernel": dom["kernel"], "achieved": round(dom["gbs"], 1),
                 "peak": peaks["hbm_gbs"], "unit": "GB/s",
                 "frac": round(dom["gbs"] / peaks["hbm_gbs"], 4),
-                "traffic": (tr["bytes_per_rep"] if tr else None),
-                "algorithmic_bytes": dom["bytes"],
+                "traffic": (tr["bytes_per_launch"] if tr else None),
+                "algorithmic_bytes_per_launch": dom["bytes"] // dom["launches"],
+                "launch_ms": round(dom["ms"] / dom["launches"], 4),
+                "traffic_source": (tr["source"] if tr else None),
                 "peak_source": f"{peaks['source']} (MEASURED_PEAKS.json copy peak)"
                                if peaks["source"] == "measured" else "fallback",
                 "fp64": {"achieved_gflops": round(dom["gflops"], 1),
                          "peak_gflops": round(fp64["gflops"], 1),
                          "frac": round(dom["fp64_frac"], 4),
+                         "pipe_frac": dom.get("fp64_pipe_frac"),
                          "peak_source": "measured in this run: max of the DFMA probe and "
                                         "native FP64 GEMM 2048^3 (FMA = 2 flops)",
                          "probe_gflops": fp64["probe_gflops"],
