@@ -35,14 +35,48 @@ struct ScanHeader {
 };
 static_assert(sizeof(ScanHeader) == 256, "scan header is 256 bytes");
 
-__device__ __forceinline__ unsigned long long ld_acquire(const unsigned long long* p) {
-  unsigned long long v;
-  asm volatile("ld.acquire.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
-  return v;
+// A tile's descriptor: {status, value} in one 16-byte word, read and written
+// as single 128-bit accesses (PTX .b128), so a reader that sees a status also
+// sees the value published with it; no other data is ordered by a
+// descriptor, so relaxed accesses suffice and a lane's loads of several
+// descriptors are in flight together.  status = epoch * 4 + (AGG 1 | INC 2).
+struct alignas(16) TileDesc {
+  unsigned long long status;
+  unsigned long long value;  // the T's bits
+};
+
+__device__ __forceinline__ void desc_load(const TileDesc* d, unsigned long long& status,
+                                          unsigned long long& value) {
+  asm volatile(
+      "{\n\t.reg .b128 t;\n\t"
+      "ld.relaxed.gpu.global.b128 t, [%2];\n\t"
+      "mov.b128 {%0, %1}, t;\n\t}"
+      : "=l"(status), "=l"(value)
+      : "l"(d)
+      : "memory");
 }
 
-__device__ __forceinline__ void st_release(unsigned long long* p, unsigned long long v) {
-  asm volatile("st.release.gpu.global.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
+__device__ __forceinline__ void desc_store(TileDesc* d, unsigned long long status,
+                                           unsigned long long value) {
+  asm volatile(
+      "{\n\t.reg .b128 t;\n\t"
+      "mov.b128 t, {%1, %2};\n\t"
+      "st.relaxed.gpu.global.b128 [%0], t;\n\t}" ::"l"(d),
+      "l"(status), "l"(value)
+      : "memory");
+}
+
+template <typename T>
+__device__ __forceinline__ unsigned long long to_bits(T v) {
+  unsigned long long b;
+  memcpy(&b, &v, sizeof(b));
+  return b;
+}
+template <typename T>
+__device__ __forceinline__ T from_bits(unsigned long long b) {
+  T v;
+  memcpy(&v, &b, sizeof(v));
+  return v;
 }
 
 template <typename T>
@@ -57,23 +91,26 @@ __device__ __forceinline__ T warp_inclusive_scan(T v) {
 }
 
 // Waits (bounded) until predecessor p has published at least its aggregate
-// for this launch; returns the flag.  A wait that gives up records the error
-// and reports an inclusive prefix so the lookback terminates.
-__device__ __forceinline__ unsigned long long wait_flag(const unsigned long long* flags,
-                                                        int64_t p, unsigned long long AGG,
+// for this launch; returns its status and value.  A wait that gives up
+// records the error and reports an inclusive prefix so the lookback ends.
+__device__ __forceinline__ unsigned long long wait_desc(const TileDesc* descs, int64_t p,
+                                                        unsigned long long AGG,
                                                         unsigned long long INC,
-                                                        ScanHeader* hdr) {
-  unsigned long long f = ld_acquire(&flags[p]);
+                                                        ScanHeader* hdr,
+                                                        unsigned long long& value) {
+  unsigned long long st;
+  desc_load(descs + p, st, value);
   long long spins = 0;
-  while (f < AGG) {
+  while (st < AGG) {
     if (++spins > kSpinLimit) {
       atomicExch(&hdr->error, 1u);
+      value = 0ull;
       return INC;
     }
     if (spins > 64) __nanosleep(64);
-    f = ld_acquire(&flags[p]);
+    desc_load(descs + p, st, value);
   }
-  return f;
+  return st;
 }
 
 __device__ __forceinline__ void named_sync(int id, int count) {
@@ -94,8 +131,7 @@ __device__ __forceinline__ void named_arrive(int id, int count) {
 template <typename T, int IT>
 __global__ void __launch_bounds__(kScanThreads)
 scan_kernel(const T* __restrict__ x, T* __restrict__ y, int64_t n, T init,
-            ScanHeader* __restrict__ hdr, unsigned long long* __restrict__ flags,
-            T* __restrict__ aggs, T* __restrict__ incs) {
+            ScanHeader* __restrict__ hdr, TileDesc* __restrict__ descs) {
   constexpr int kTile = kScanBlock * IT;
   constexpr int kPadShift = (IT == 32) ? 5 : 4;
   extern __shared__ __align__(16) unsigned char s_raw[];
@@ -130,17 +166,20 @@ scan_kernel(const T* __restrict__ x, T* __restrict__ y, int64_t n, T init,
       bool done = false;
       while (!done) {
         unsigned long long f[kLookbackPerLane];
-#pragma unroll
-        for (int j = 0; j < kLookbackPerLane; ++j) {
-          const int64_t p = p_hi - (j * 32 + lane);
-          f[j] = (p >= 0) ? wait_flag(flags, p, AGG, INC, hdr) : INC;  // p < 0: terminator
-        }
         T v[kLookbackPerLane];
+        unsigned long long bits[kLookbackPerLane];
 #pragma unroll
-        for (int j = 0; j < kLookbackPerLane; ++j) {
+        for (int j = 0; j < kLookbackPerLane; ++j) {  // all loads first
           const int64_t p = p_hi - (j * 32 + lane);
-          // L1-bypassing loads: the values were written by other SMs.
-          v[j] = (p < 0) ? T(0) : (f[j] == INC) ? __ldcg(incs + p) : __ldcg(aggs + p);
+          f[j] = INC;                                  // p < 0: end of the lookback
+          bits[j] = 0ull;
+          if (p >= 0) desc_load(descs + p, f[j], bits[j]);
+        }
+#pragma unroll
+        for (int j = 0; j < kLookbackPerLane; ++j) {  // then wait for the late ones
+          const int64_t p = p_hi - (j * 32 + lane);
+          if (p >= 0 && f[j] < AGG) f[j] = wait_desc(descs, p, AGG, INC, hdr, bits[j]);
+          v[j] = from_bits<T>(bits[j]);
         }
         // nearest window slot holding an inclusive prefix
         int stop = 32 * kLookbackPerLane;
@@ -164,9 +203,7 @@ scan_kernel(const T* __restrict__ x, T* __restrict__ y, int64_t n, T init,
     }
     named_sync(2, kScanThreads);  // the loaders have the tile aggregate
     if (lane == 0) {
-      incs[tile] = exclusive + s_agg;
-      __threadfence();
-      st_release(&flags[tile], INC);
+      desc_store(descs + tile, INC, to_bits<T>(exclusive + s_agg));
       s_excl = exclusive;
     }
     named_arrive(3, kScanThreads);
@@ -202,11 +239,7 @@ scan_kernel(const T* __restrict__ x, T* __restrict__ y, int64_t n, T init,
       if (lane < kScanBlock / 32) s_warp[lane] = wi - w;  // exclusive warp offsets
       if (lane == kScanBlock / 32 - 1) {
         s_agg = wi;                                       // tile aggregate
-        if (tile > 0) {
-          aggs[tile] = wi;
-          __threadfence();
-          st_release(&flags[tile], AGG);
-        }
+        if (tile > 0) desc_store(descs + tile, AGG, to_bits<T>(wi));
       }
     }
     named_sync(1, kScanBlock);
@@ -271,13 +304,10 @@ int launch_scan_it(const T* x, T* y, int64_t n, T init, char* w, cudaStream_t st
     return B200_ERR_LAUNCH;
   }
   const int64_t tiles = ceil_div(n, kTile);
-  const int64_t slots = scan_tiles_max(n);
   ScanHeader* hdr = reinterpret_cast<ScanHeader*>(w);
-  unsigned long long* flags = reinterpret_cast<unsigned long long*>(w + 256);
-  T* aggs = reinterpret_cast<T*>(w + 256 + slots * 8);
-  T* incs = reinterpret_cast<T*>(w + 256 + slots * 16);
+  TileDesc* descs = reinterpret_cast<TileDesc*>(w + 256);
   scan_kernel<T, IT><<<static_cast<int>(tiles), kScanThreads, kSmem, st>>>(x, y, n, init, hdr,
-                                                                          flags, aggs, incs);
+                                                                          descs);
   return B200_OK;
 }
 
@@ -292,7 +322,8 @@ int launch_scan(const char* name, const T* x, T* y, int64_t n, T init, void* ws,
     return invalid("%s: block size %d (only %d)", name, tune->block_size, kScanBlock);
   const int items = (tune && tune->items) ? tune->items : kScanItemsDefault;
   if (items != 16 && items != 32) return invalid("%s: items %d (16 or 32)", name, items);
-  size_t need = 256 + static_cast<size_t>(slots) * 24;
+  size_t need = 256 + static_cast<size_t>(slots) * sizeof(TileDesc);
+  if (ws && !aligned16(ws)) return invalid("%s: workspace not 16-byte aligned", name);
   if (!ws || ws_bytes < need) {
     set_error("%s: workspace %zu bytes, need %zu", name, ws_bytes, need);
     return B200_ERR_WORKSPACE;
@@ -343,7 +374,7 @@ reduce_sum_kernel(const double* __restrict__ x, int64_t n, double init,
 extern "C" {
 
 size_t b200_scan_workspace_bytes(int64_t n) {
-  return 256 + static_cast<size_t>(scan_tiles_max(n)) * 24;
+  return 256 + static_cast<size_t>(scan_tiles_max(n)) * sizeof(TileDesc);
 }
 
 int b200_algorithm_scan(const double* x, double* y, int64_t n, double init,
