@@ -471,7 +471,8 @@ BW27 = {
     "Lcals_EOS": (32, 8), "Lcals_FIRST_DIFF": (16, 1), "Lcals_INT_PREDICT": (88, 10),
     "Lcals_FIRST_MIN": (8, 0), "Lcals_DIFF_PREDICT": (160, 9), "Lcals_PLANCKIAN": (40, 32),
     "Apps_PRESSURE": (48, 6), "Apps_ENERGY": (216, 29), "Algorithm_SCAN": (16, 0),
-    "Algorithm_REDUCE_SUM": (8, 1),
+    "Algorithm_REDUCE_SUM": (8, 1), "Algorithm_MEMSET": (8, 0), "Algorithm_MEMCPY": (16, 0),
+    "Basic_INDEXLIST": (10, 0), "Algorithm_HISTOGRAM": (8, 0), "Basic_MULTI_REDUCE": (16, 1),
 }
 
 
@@ -570,6 +571,35 @@ def bw27_run(torch, rp, name, n, seed):
         ws = z(wb, torch.uint8)
         return (lambda s: L.b200_algorithm_reduce_sum(P(x), n, 0.0, P(out), P(ws), wb, None,
                                                       s)), [x, out, ws]
+    if name == "Algorithm_MEMSET":
+        x = z(n)
+        return (lambda s: L.b200_algorithm_memset(P(x), 0.0, n, None, s)), [x]
+    if name == "Algorithm_MEMCPY":
+        x, y = u(n), z(n)
+        return (lambda s: L.b200_algorithm_memcpy(P(x), P(y), n, None, s)), [x, y]
+    if name == "Basic_INDEXLIST":
+        x = u(n)
+        x.sub_(1.0)  # uniform [-0.5, 0.5): about half the items selected
+        lst = z(n, torch.int32)
+        ln = z(1, torch.int64)
+        wb = L.b200_indexlist_workspace_bytes(n)
+        ws = z(wb, torch.uint8)
+        return (lambda s: L.b200_basic_indexlist(P(x), P(lst), n, P(ln), P(ws), wb, None, s)), \
+            [x, lst, ln, ws]
+    if name in ("Algorithm_HISTOGRAM", "Basic_MULTI_REDUCE"):
+        nb = 10
+        bins = torch.empty(n, dtype=torch.int64, device="cuda")
+        rp.check(L.b200_init_uniform_i64(P(bins), n, seed, 7, 0, nb, None))
+        if name == "Algorithm_HISTOGRAM":
+            cinit, cnt = z(nb, torch.int64), z(nb, torch.int64)
+            return (lambda s: L.b200_algorithm_histogram(P(bins), n, nb, P(cinit), P(cnt), None,
+                                                         s)), [bins, cinit, cnt]
+        data, vinit, vals = u(n), z(nb), z(nb)
+        wb = L.b200_multi_reduce_workspace_bytes(n, nb)
+        ws = z(wb, torch.uint8)
+        return (lambda s: L.b200_basic_multi_reduce(P(bins), P(data), n, nb, P(vinit), P(vals),
+                                                    P(ws), wb, None, s)), \
+            [bins, data, vinit, vals, ws]
     raise KeyError(name)
 
 

@@ -370,6 +370,51 @@ int b200_algorithm_scan_i64(const int64_t* x, int64_t* y, int64_t n,
                             size_t workspace_bytes, const b200_tune* tune,
                             b200_stream_t stream);
 
+/* y[i] = x[i]  -- algorithm/MEMCPY.hpp:27-28, MEMCPY-Cuda.cpp:26.  The Stream
+ * COPY kernel (16-byte vectors).                                            */
+int b200_algorithm_memcpy(const double* x, double* y, int64_t n,
+                          const b200_tune* tune, b200_stream_t stream);
+
+/* x[i] = val  -- algorithm/MEMSET.hpp:27-28, MEMSET-Cuda.cpp:26.            */
+int b200_algorithm_memset(double* x, double val, int64_t n,
+                          const b200_tune* tune, b200_stream_t stream);
+
+/* counts[b] = counts_init[b] + #{i : bins[i] == b}, b in [0, num_bins);
+ * items with a bin outside the range are skipped.  Exact (integer counts)
+ *   -- algorithm/HISTOGRAM.hpp:37-64, HISTOGRAM-Cuda.cpp:31.  Two launches. */
+int b200_algorithm_histogram(const int64_t* bins, int64_t n, int64_t num_bins,
+                             const unsigned long long* counts_init,
+                             unsigned long long* counts, const b200_tune* tune,
+                             b200_stream_t stream);
+
+/* ---- Basic: index lists and multi-reductions ----------------------------- */
+
+/* Workspace for b200_basic_indexlist on n items (zero it before first use;
+ * calls leave it ready for the next; word at byte 16 = wait-gave-up flag). */
+size_t b200_indexlist_workspace_bytes(int64_t n);
+
+/* list[count++] = i for every i (in order) with x[i] < 0; *len = count.
+ * n <= 2^31 - 1 (the list is int32, the suite's Int_type).  One launch,
+ * single-pass compaction on a decoupled lookback
+ *   -- basic/INDEXLIST.hpp:28-34, INDEXLIST-Cuda.cpp:33; also the list and
+ *   count of basic/INDEXLIST_3LOOP.hpp:39-45, INDEXLIST_3LOOP-Cuda.cpp:34-56. */
+int b200_basic_indexlist(const double* x, int32_t* list, int64_t n, int64_t* len,
+                         void* workspace, size_t workspace_bytes,
+                         const b200_tune* tune, b200_stream_t stream);
+
+/* Workspace for b200_basic_multi_reduce (n items, num_bins bins).          */
+size_t b200_multi_reduce_workspace_bytes(int64_t n, int64_t num_bins);
+
+/* values[b] = values_init[b] + sum of data[i] over i with bins[i] == b.
+ * Deterministic for num_bins <= 96 (fixed-order sums); more bins use FP64
+ * atomics.  Items with a bin outside [0, num_bins) are skipped
+ *   -- basic/MULTI_REDUCE.hpp:38-65, MULTI_REDUCE-Cuda.cpp:28.              */
+int b200_basic_multi_reduce(const int64_t* bins, const double* data, int64_t n,
+                            int64_t num_bins, const double* values_init,
+                            double* values, void* workspace,
+                            size_t workspace_bytes, const b200_tune* tune,
+                            b200_stream_t stream);
+
 /* *sum = sum_init + sum_i x[i], fixed-shape tree (deterministic)
  *   -- algorithm/REDUCE_SUM.hpp:25-32, REDUCE_SUM-Seq.cpp:34-48             */
 int b200_algorithm_reduce_sum(const double* x, int64_t n, double sum_init,

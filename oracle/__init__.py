@@ -31,7 +31,8 @@ class OracleOpts(ctypes.Structure):
                 ("init_mode", ctypes.c_int), ("threads", ctypes.c_int),
                 ("seed", ctypes.c_ulonglong), ("lo", ctypes.c_double),
                 ("hi", ctypes.c_double), ("tsteps", ctypes.c_long),
-                ("variant", ctypes.c_int), ("skip_checksum", ctypes.c_int)]
+                ("variant", ctypes.c_int), ("skip_checksum", ctypes.c_int),
+                ("num_bins", ctypes.c_long), ("bin_algo", ctypes.c_int)]
 
 
 class OracleResult(ctypes.Structure):
@@ -108,13 +109,16 @@ def lib() -> ctypes.CDLL:
 
 def run(kernel: str, size: float = -1, reps: int = 1, init: str = "reference",
         seed: int = 4793, lo: float = 0.5, hi: float = 1.5, tsteps: int = -1,
-        threads: int = 0, variant: int = 0, skip_checksum: bool = False) -> dict:
+        threads: int = 0, variant: int = 0, skip_checksum: bool = False,
+        num_bins: int = 10, bin_algo: str = "RunsRandomSizes") -> dict:
     """Runs one kernel with the suite's Base_Seq (threads=0) or Base_OpenMP
     semantics and returns its checksum, sizes and rep-loop time."""
+    algos = ["Random", "RunsRandomSizes", "RunsEvenSizes", "Single"]
     o = OracleOpts(size=float(size), reps=int(reps),
                    init_mode=1 if init == "uniform" else 0, threads=int(threads),
                    seed=int(seed), lo=float(lo), hi=float(hi), tsteps=int(tsteps),
-                   variant=int(variant), skip_checksum=1 if skip_checksum else 0)
+                   variant=int(variant), skip_checksum=1 if skip_checksum else 0,
+                   num_bins=int(num_bins), bin_algo=algos.index(bin_algo))
     r = OracleResult()
     st = lib().oracle_run(kernel.encode(), ctypes.byref(o), ctypes.byref(r))
     if st != 0:
@@ -135,10 +139,11 @@ def checksum(arr, scale: float = 1.0) -> float:
     return lib().oracle_checksum(a.ctypes.data, a.size, scale, None)
 
 
-def run_ref(kernel: str, size: int, reps: int) -> dict:
-    """Runs the suite's own Base_Seq code (oracle/_ref) for one kernel."""
-    out = subprocess.run([REF_EXE, kernel, str(size), str(reps)], check=True,
-                         capture_output=True, text=True).stdout
+def run_ref(kernel: str, size: int, reps: int, extra=()) -> dict:
+    """Runs the suite's own Base_Seq code (oracle/_ref) for one kernel;
+    `extra` are further suite options (e.g. --multi_reduce_num_bins 100)."""
+    out = subprocess.run([REF_EXE, kernel, str(size), str(reps), *map(str, extra)],
+                         check=True, capture_output=True, text=True).stdout
     line = [ln for ln in out.splitlines() if ln.startswith("{")][-1]
     return json.loads(line)
 

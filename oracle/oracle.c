@@ -110,6 +110,93 @@ static double* alloc_randvalue(ctx* c, int64_t n) {
   return p;
 }
 
+/* allocAndInitDataRandSign (DataUtils.cpp:542-555), or the uniform mode */
+static double* alloc_randsign(ctx* c, int64_t n) {
+  if (c->o->init_mode == 1) return alloc_init(c, n);
+  double* p = alloc_raw(n);
+  if (!p) return NULL;
+  double factor = (c->count % 2 ? 0.1 : 0.2);
+  srand(4793);
+  for (int64_t i = 0; i < n; ++i) {
+    double s = (double)rand() / RAND_MAX;
+    s = (s < 0.5 ? -1.0 : 1.0);
+    p[i] = s * factor * (i + 1.1) / (i + 1.12345);
+  }
+  c->count++;
+  return p;
+}
+
+/* allocAndInitData(Int_ptr) (DataUtils.cpp:477-497), in either mode; an
+ * index equal to n (rand() == RAND_MAX) is skipped. */
+static int* alloc_int(ctx* c, int64_t n) {
+  int* p = (int*)malloc(sizeof(int) * (size_t)(n > 0 ? n : 1));
+  if (!p) return NULL;
+  srand(4793);
+  for (int64_t i = 0; i < n; ++i) p[i] = ((double)rand() / RAND_MAX < 0.5 ? -1 : 1);
+  double f = (double)rand() / RAND_MAX;
+  size_t ilo = (size_t)(n * f);
+  if ((int64_t)ilo < n) p[ilo] = -58;
+  f = (double)rand() / RAND_MAX;
+  size_t ihi = (size_t)(n * f);
+  if ((int64_t)ihi < n) p[ihi] = 19;
+  c->count++;
+  return p;
+}
+
+/* rand()/RAND_MAX values (DataUtils.cpp:560-569) in either mode; bumps the
+ * init count like allocAndInitDataRandValue. */
+static double* rand_values(ctx* c, int64_t n) {
+  double* p = alloc_raw(n);
+  if (!p) return NULL;
+  srand(4793);
+  for (int64_t i = 0; i < n; ++i) p[i] = (double)rand() / RAND_MAX;
+  c->count++;
+  return p;
+}
+
+static int cmp_double(const void* a, const void* b) {
+  double x = *(const double*)a, y = *(const double*)b;
+  return (x > y) - (x < y);
+}
+
+/* The bins of HISTOGRAM / MULTI_REDUCE (algorithm/HISTOGRAM.cpp:73-131,
+ * basic/MULTI_REDUCE.cpp:74-133). */
+static int64_t* assign_bins(ctx* c, int64_t n, int64_t num_bins, int algo) {
+  int64_t* bins = (int64_t*)malloc(sizeof(int64_t) * (size_t)(n > 0 ? n : 1));
+  if (!bins) return NULL;
+  if (algo == 0) {
+    double* d = rand_values(c, n);
+    if (!d) { free(bins); return NULL; }
+    for (int64_t i = 0; i < n; ++i) {
+      int64_t b = (int64_t)(d[i] * num_bins);
+      if (b >= num_bins) b = num_bins - 1;
+      if (b < 0) b = 0;
+      bins[i] = b;
+    }
+    free(d);
+    return bins;
+  }
+  double* bounds;
+  if (algo == 1) {
+    bounds = rand_values(c, num_bins);
+    if (!bounds) { free(bins); return NULL; }
+    qsort(bounds, (size_t)num_bins, sizeof(double), cmp_double);
+  } else {
+    bounds = alloc_raw(num_bins);
+    if (!bounds) { free(bins); return NULL; }
+    for (int64_t b = 0; b < num_bins; ++b)
+      bounds[b] = (algo == 2) ? (double)(b + 1) / num_bins : 0.0;
+  }
+  int64_t bin = 0;
+  for (int64_t i = 0; i < n; ++i) {
+    double pos = (double)i / n;
+    while (bin + 1 < num_bins && pos >= bounds[bin]) bin += 1;
+    bins[i] = bin;
+  }
+  free(bounds);
+  return bins;
+}
+
 /* initData(Real_type&) (DataUtils.cpp:589-595) */
 static double init_scalar(ctx* c) {
   double factor = (c->count % 2 ? 0.1 : 0.2);
@@ -151,6 +238,34 @@ static long double checksum_ld_i64(const int64_t* p, int64_t n, double scale) {
   }
   tchk *= scale;
   return tchk;
+}
+
+static long double checksum_ld_int(const int* p, int64_t n, double scale) {
+  if (g_skip_checksum) return 0.0L;
+  long double tchk = 0.0, ckahan = 0.0;
+  for (int64_t j = 0; j < n; ++j) {
+    long double x = (fabs(sin(j + 1.0)) + 0.5) * (long double)p[j];
+    long double y = x - ckahan;
+    volatile long double t = tchk + y;
+    volatile long double z = t - tchk;
+    ckahan = z - y;
+    tchk = t;
+  }
+  return tchk * scale;
+}
+
+static long double checksum_ld_u64(const unsigned long long* p, int64_t n, double scale) {
+  if (g_skip_checksum) return 0.0L;
+  long double tchk = 0.0, ckahan = 0.0;
+  for (int64_t j = 0; j < n; ++j) {
+    long double x = (fabs(sin(j + 1.0)) + 0.5) * (long double)p[j];
+    long double y = x - ckahan;
+    volatile long double t = tchk + y;
+    volatile long double z = t - tchk;
+    ckahan = z - y;
+    tchk = t;
+  }
+  return tchk * scale;
 }
 
 double oracle_checksum(const double* p, int64_t n, double scale, double* residual) {
@@ -1471,6 +1586,133 @@ done:
 }
 
 /* ------------------------------------------------------------------------ */
+/* Algorithm MEMSET / MEMCPY / HISTOGRAM, Basic INDEXLIST / MULTI_REDUCE      */
+/* ------------------------------------------------------------------------ */
+
+/* MEMSET.cpp:22-75, MEMSET.hpp:27-28 */
+static void run_memset(ctx* c, oracle_result* r) {
+  idx_t n = target_size(c, 1000000), reps = c->o->reps;
+  double* x = alloc_const(c, n, -1.234567e89);
+  double val = 0.0, t0;
+  CHECK_ALLOC(x);
+  t0 = now_s();
+  for (idx_t irep = 0; irep < reps; ++irep) {
+    OMP_FOR
+    for (idx_t i = 0; i < n; ++i) x[i] = val;
+  }
+  set_result(r, checksum_ld(x, n, 1.0), n, reps, n, 1, 8 * n, 0, now_s() - t0);
+done:
+  free(x);
+}
+
+/* MEMCPY.cpp:22-75, MEMCPY.hpp:27-28 */
+static void run_memcpy(ctx* c, oracle_result* r) {
+  idx_t n = target_size(c, 1000000), reps = c->o->reps;
+  double *x = alloc_const(c, n, 0.0), *y = alloc_const(c, n, -1.234567e89), t0;
+  CHECK_ALLOC(x); CHECK_ALLOC(y);
+  t0 = now_s();
+  for (idx_t irep = 0; irep < reps; ++irep) {
+    OMP_FOR
+    for (idx_t i = 0; i < n; ++i) y[i] = x[i];
+  }
+  set_result(r, checksum_ld(y, n, 1.0), n, reps, n, 1, 16 * n, 0, now_s() - t0);
+done:
+  free(x); free(y);
+}
+
+/* INDEXLIST.cpp:22-80, INDEXLIST.hpp:28-34, INDEXLIST-Seq.cpp; with
+ * three_loop, INDEXLIST_3LOOP.cpp:22-92 (counts, their exclusive scan and the
+ * list from count changes: the same list and length). */
+static void run_indexlist_any(ctx* c, oracle_result* r, int three_loop) {
+  idx_t n = target_size(c, 1000000), reps = c->o->reps;
+  double* x = alloc_randsign(c, n);
+  int* list = alloc_int(c, n);
+  idx_t* counts = (idx_t*)malloc(sizeof(idx_t) * (size_t)(n + 1));
+  idx_t len = -1;
+  double t0;
+  CHECK_ALLOC(x); CHECK_ALLOC(list); CHECK_ALLOC(counts);
+  t0 = now_s();
+  for (idx_t irep = 0; irep < reps; ++irep) {
+    if (!three_loop) {
+      idx_t count = 0;
+      for (idx_t i = 0; i < n; ++i)
+        if (x[i] < 0.0) list[count++] = (int)i;
+      len = count;
+    } else {
+      for (idx_t i = 0; i < n; ++i) counts[i] = (x[i] < 0.0) ? 1 : 0;
+      idx_t count = 0;
+      for (idx_t i = 0; i < n + 1; ++i) {
+        idx_t inc = (i < n) ? counts[i] : 0;
+        counts[i] = count;
+        count += inc;
+      }
+      for (idx_t i = 0; i < n; ++i)
+        if (counts[i] != counts[i + 1]) list[counts[i]] = (int)i;
+      len = counts[n];
+    }
+  }
+  t0 = now_s() - t0;
+  if (!three_loop) {
+    set_result(r, checksum_ld_int(list, n, 1.0) + (long double)len, n, reps, n, 1,
+               8 + 8 * n + 8 + 4 * n / 2, 0, t0);
+  } else {
+    set_result(r, checksum_ld_int(list, n, 1.0) + (long double)len, n, reps, 3 * n + 1, 3,
+               8 * n + 8 + 8 * (n + 1) + 8 * (n + 1) +
+                   (8 * n + 8 + 8 * (n + 1) + 4 * (n + 1) / 2),
+               0, t0);
+  }
+done:
+  free(x); free(list); free(counts);
+}
+
+static void run_indexlist(ctx* c, oracle_result* r) { run_indexlist_any(c, r, 0); }
+static void run_indexlist_3loop(ctx* c, oracle_result* r) { run_indexlist_any(c, r, 1); }
+
+static int64_t bins_of(const ctx* c) { return c->o->num_bins > 0 ? c->o->num_bins : 10; }
+static int bin_algo_of(const ctx* c) {
+  return (c->o->bin_algo >= 0 && c->o->bin_algo <= 3) ? c->o->bin_algo : 1;
+}
+
+/* HISTOGRAM.cpp:24-149, HISTOGRAM.hpp:37-64, HISTOGRAM-Seq.cpp */
+static void run_histogram(ctx* c, oracle_result* r) {
+  idx_t n = target_size(c, 1000000), reps = c->o->reps;
+  int64_t nb = bins_of(c);
+  int64_t* bins = assign_bins(c, n, nb, bin_algo_of(c));
+  unsigned long long* counts = (unsigned long long*)calloc((size_t)nb, sizeof(unsigned long long));
+  double t0;
+  CHECK_ALLOC(bins); CHECK_ALLOC(counts);
+  t0 = now_s();
+  for (idx_t irep = 0; irep < reps; ++irep) {
+    for (int64_t b = 0; b < nb; ++b) counts[b] = 0ull;  /* counts_init */
+    for (idx_t i = 0; i < n; ++i) counts[bins[i]] += 1ull;
+  }
+  set_result(r, checksum_ld_u64(counts, nb, 1.0), n, reps, n, 1, 8 * nb + 8 * n + 8 * nb, n,
+             now_s() - t0);
+done:
+  free(bins); free(counts);
+}
+
+/* MULTI_REDUCE.cpp:24-153, MULTI_REDUCE.hpp:38-65, MULTI_REDUCE-Seq.cpp */
+static void run_multi_reduce(ctx* c, oracle_result* r) {
+  idx_t n = target_size(c, 1000000), reps = c->o->reps;
+  int64_t nb = bins_of(c);
+  double* data = alloc_randvalue(c, n);
+  int64_t* bins = assign_bins(c, n, nb, bin_algo_of(c));
+  double* values = (double*)calloc((size_t)nb, sizeof(double));
+  double t0;
+  CHECK_ALLOC(data); CHECK_ALLOC(bins); CHECK_ALLOC(values);
+  t0 = now_s();
+  for (idx_t irep = 0; irep < reps; ++irep) {
+    for (int64_t b = 0; b < nb; ++b) values[b] = 0.0;  /* values_init */
+    for (idx_t i = 0; i < n; ++i) values[bins[i]] += data[i];
+  }
+  set_result(r, checksum_ld(values, nb, 1.0), n, reps, n, 1, 8 * nb + 8 * n + 8 * n + 8 * nb,
+             n, now_s() - t0);
+done:
+  free(data); free(bins); free(values);
+}
+
+/* ------------------------------------------------------------------------ */
 
 typedef void (*runner_fn)(ctx*, oracle_result*);
 
@@ -1491,7 +1733,10 @@ static const struct {
     {"Polybench_JACOBI_2D", run_jacobi_2d}, {"Polybench_HEAT_3D", run_heat_3d},
     {"Polybench_FDTD_2D", run_fdtd_2d}, {"Polybench_GEMM", run_gemm},
     {"Polybench_3MM", run_3mm},        {"Algorithm_SCAN", run_scan},
-    {"Algorithm_REDUCE_SUM", run_reduce_sum},
+    {"Algorithm_REDUCE_SUM", run_reduce_sum}, {"Algorithm_MEMSET", run_memset},
+    {"Algorithm_MEMCPY", run_memcpy},   {"Algorithm_HISTOGRAM", run_histogram},
+    {"Basic_INDEXLIST", run_indexlist}, {"Basic_INDEXLIST_3LOOP", run_indexlist_3loop},
+    {"Basic_MULTI_REDUCE", run_multi_reduce},
 };
 
 int oracle_run(const char* kernel, const oracle_opts* opts, oracle_result* out) {

@@ -32,6 +32,8 @@ typedef struct oracle_opts {
   long tsteps;             /* Polybench time-step override; < 0 = default   */
   int variant;             /* kernel-specific: SCAN 1 = int64 values         */
   int skip_checksum;       /* 1: time the rep loop only (checksum = 0)      */
+  long num_bins;           /* HISTOGRAM / MULTI_REDUCE bins; <= 0 = 10       */
+  int bin_algo;            /* 0 Random, 1 RunsRandomSizes (default), 2 RunsEvenSizes, 3 Single */
 } oracle_opts;
 
 typedef struct oracle_result {

@@ -2,10 +2,11 @@
 // the suite's own KernelBase::execute (common/KernelBase.cpp:359-377) and
 // prints one JSON line with the checksum and timing.
 //
-//   rajaperf_ref <Group_KERNEL> <size> <reps>
+//   rajaperf_ref <Group_KERNEL> <size> <reps> [suite options ...]
 //
 // Sizes and reps are passed through the suite's RunParams as
-// "--size <size> --checkrun <reps>".
+// "--size <size> --checkrun <reps>"; further arguments (e.g.
+// "--multi_reduce_num_bins 100") are appended to that command line.
 #include "common/RAJAPerfSuite.hpp"
 #include "common/KernelBase.hpp"
 #include "common/RunParams.hpp"
@@ -27,6 +28,7 @@ int main(int argc, char** argv) {
                                    "--checkrun", argv[3],
                                    "--disable-warmup",
                                    "-k", kname, "-v", "Base_Seq"};
+  for (int a = 4; a < argc; ++a) args.push_back(argv[a]);
   std::vector<char*> cargs;
   for (auto& a : args) cargs.push_back(&a[0]);
   RunParams params(static_cast<int>(cargs.size()), cargs.data());

@@ -34,6 +34,12 @@
 #include "basic/DAXPY.hpp"
 #include "basic/INIT3.hpp"
 #include "basic/MULADDSUB.hpp"
+#include "basic/INDEXLIST.hpp"
+#include "basic/INDEXLIST_3LOOP.hpp"
+#include "basic/MULTI_REDUCE.hpp"
+#include "algorithm/MEMSET.hpp"
+#include "algorithm/MEMCPY.hpp"
+#include "algorithm/HISTOGRAM.hpp"
 
 #include <iostream>
 #include <string>
@@ -72,6 +78,11 @@ const std::vector<KName>& kernelNames() {
     {Algorithm_REDUCE_SUM, "Algorithm_REDUCE_SUM"},
     {Basic_DAXPY, "Basic_DAXPY"}, {Basic_INIT3, "Basic_INIT3"},
     {Basic_MULADDSUB, "Basic_MULADDSUB"},
+    {Basic_INDEXLIST, "Basic_INDEXLIST"},
+    {Basic_INDEXLIST_3LOOP, "Basic_INDEXLIST_3LOOP"},
+    {Basic_MULTI_REDUCE, "Basic_MULTI_REDUCE"},
+    {Algorithm_MEMSET, "Algorithm_MEMSET"}, {Algorithm_MEMCPY, "Algorithm_MEMCPY"},
+    {Algorithm_HISTOGRAM, "Algorithm_HISTOGRAM"},
   };
   return names;
 }
@@ -184,6 +195,12 @@ KernelBase* getKernelObject(KernelID kid, const RunParams& rp) {
     case Basic_DAXPY: return new basic::DAXPY(rp);
     case Basic_INIT3: return new basic::INIT3(rp);
     case Basic_MULADDSUB: return new basic::MULADDSUB(rp);
+    case Basic_INDEXLIST: return new basic::INDEXLIST(rp);
+    case Basic_INDEXLIST_3LOOP: return new basic::INDEXLIST_3LOOP(rp);
+    case Basic_MULTI_REDUCE: return new basic::MULTI_REDUCE(rp);
+    case Algorithm_MEMSET: return new algorithm::MEMSET(rp);
+    case Algorithm_MEMCPY: return new algorithm::MEMCPY(rp);
+    case Algorithm_HISTOGRAM: return new algorithm::HISTOGRAM(rp);
     default: return nullptr;
   }
 }

@@ -7,4 +7,8 @@
 #include "RAJA/util/macros.hpp"
 #include "RAJA/util/Timer.hpp"
 #include "RAJA/internal/MemUtils_CPU.hpp"
+// RAJA's headers bring in the C string and algorithm headers that some
+// kernels' Seq files use without including them (std::memcpy, std::sort).
+#include <algorithm>
+#include <cstring>
 #endif

@@ -12,6 +12,7 @@
 // epoch.  Every wait is bounded; a wait that gives up sets the error word of
 // the workspace header (byte offset 16) and the call's results are invalid.
 #include "b200_internal.cuh"
+#include "b200_lookback.cuh"
 #include "b200_reduce.cuh"
 
 using namespace b200;
@@ -23,96 +24,6 @@ constexpr int kScanThreads = kScanBlock + 32;           // + the lookback warp
 constexpr int kScanItemsMin = 16;                       // smallest tile: 4096 items
 constexpr int kScanItemsDefault = 32;                   // default tile: 8192 items
 constexpr int kScanTileMin = kScanBlock * kScanItemsMin;
-constexpr int kLookbackPerLane = 4;                     // 128 predecessors per round
-constexpr long long kSpinLimit = 1LL << 22;
-
-struct ScanHeader {
-  unsigned long long epoch;
-  unsigned int tile_counter;
-  unsigned int done_counter;
-  unsigned int error;
-  unsigned int pad[59];
-};
-static_assert(sizeof(ScanHeader) == 256, "scan header is 256 bytes");
-
-// A tile's descriptor: {status, value} in one 16-byte word, read and written
-// as single 128-bit accesses (PTX .b128), so a reader that sees a status also
-// sees the value published with it; no other data is ordered by a
-// descriptor, so relaxed accesses suffice and a lane's loads of several
-// descriptors are in flight together.  status = epoch * 4 + (AGG 1 | INC 2).
-struct alignas(16) TileDesc {
-  unsigned long long status;
-  unsigned long long value;  // the T's bits
-};
-
-__device__ __forceinline__ void desc_load(const TileDesc* d, unsigned long long& status,
-                                          unsigned long long& value) {
-  asm volatile(
-      "{\n\t.reg .b128 t;\n\t"
-      "ld.relaxed.gpu.global.b128 t, [%2];\n\t"
-      "mov.b128 {%0, %1}, t;\n\t}"
-      : "=l"(status), "=l"(value)
-      : "l"(d)
-      : "memory");
-}
-
-__device__ __forceinline__ void desc_store(TileDesc* d, unsigned long long status,
-                                           unsigned long long value) {
-  asm volatile(
-      "{\n\t.reg .b128 t;\n\t"
-      "mov.b128 t, {%1, %2};\n\t"
-      "st.relaxed.gpu.global.b128 [%0], t;\n\t}" ::"l"(d),
-      "l"(status), "l"(value)
-      : "memory");
-}
-
-template <typename T>
-__device__ __forceinline__ unsigned long long to_bits(T v) {
-  unsigned long long b;
-  memcpy(&b, &v, sizeof(b));
-  return b;
-}
-template <typename T>
-__device__ __forceinline__ T from_bits(unsigned long long b) {
-  T v;
-  memcpy(&v, &b, sizeof(v));
-  return v;
-}
-
-template <typename T>
-__device__ __forceinline__ T warp_inclusive_scan(T v) {
-  const int lane = threadIdx.x & 31;
-#pragma unroll
-  for (int off = 1; off < 32; off <<= 1) {
-    T o = __shfl_up_sync(0xffffffffu, v, off);
-    if (lane >= off) v += o;
-  }
-  return v;
-}
-
-// Waits (bounded) until predecessor p has published at least its aggregate
-// for this launch; returns its status and value.  A wait that gives up
-// records the error and reports an inclusive prefix so the lookback ends.
-__device__ __forceinline__ unsigned long long wait_desc(const TileDesc* descs, int64_t p,
-                                                        unsigned long long AGG,
-                                                        unsigned long long INC,
-                                                        ScanHeader* hdr,
-                                                        unsigned long long& value) {
-  unsigned long long st;
-  desc_load(descs + p, st, value);
-  long long spins = 0;
-  while (st < AGG) {
-    if (++spins > kSpinLimit) {
-      atomicExch(&hdr->error, 1u);
-      value = 0ull;
-      return INC;
-    }
-    if (spins > 64) __nanosleep(64);
-    desc_load(descs + p, st, value);
-  }
-  return st;
-}
-
 __device__ __forceinline__ void named_sync(int id, int count) {
   asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(count) : "memory");
 }
@@ -128,10 +39,16 @@ __device__ __forceinline__ void named_arrive(int id, int count) {
 // prefix, and the loaders write the tile out.  Named barriers: 1 = loaders
 // only, 2 = aggregate ready (loaders arrive, lookback warp waits), 3 =
 // exclusive prefix ready (lookback warp arrives, loaders wait).
-template <typename T, int IT>
-__global__ void __launch_bounds__(kScanThreads)
+// 16-byte vector of two T (double2 / longlong2).
+template <typename T> struct Vec2;
+template <> struct Vec2<double> { using type = double2; };
+template <> struct Vec2<long long> { using type = longlong2; };
+
+template <typename T, int IT, bool VEC>
+__global__ void __launch_bounds__(kScanThreads, 3)
 scan_kernel(const T* __restrict__ x, T* __restrict__ y, int64_t n, T init,
             ScanHeader* __restrict__ hdr, TileDesc* __restrict__ descs) {
+  using V2 = typename Vec2<T>::type;
   constexpr int kTile = kScanBlock * IT;
   constexpr int kPadShift = (IT == 32) ? 5 : 4;
   extern __shared__ __align__(16) unsigned char s_raw[];
@@ -145,11 +62,7 @@ scan_kernel(const T* __restrict__ x, T* __restrict__ y, int64_t n, T init,
   auto pad = [](int i) { return i + (i >> kPadShift); };
 
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  if (tid == 0) {
-    s_epoch = *reinterpret_cast<volatile unsigned long long*>(&hdr->epoch);
-    s_tile_id = atomicAdd(&hdr->tile_counter, 1u);
-  }
-  __syncthreads();
+  take_tile(hdr, &s_tile_id, &s_epoch);
   const unsigned int tile = s_tile_id;
   const unsigned long long epoch = s_epoch;
   const unsigned long long AGG = epoch * 4 + 1, INC = epoch * 4 + 2;
@@ -159,48 +72,8 @@ scan_kernel(const T* __restrict__ x, T* __restrict__ y, int64_t n, T init,
     // ---- lookback warp ----
     // One round examines 32 * kLookbackPerLane predecessors, nearest first
     // (window slot w = j * 32 + lane is predecessor p_hi - w).
-    T exclusive = init;
-    if (tile > 0) {
-      T acc = T(0);
-      int64_t p_hi = static_cast<int64_t>(tile) - 1;  // nearest unexamined predecessor
-      bool done = false;
-      while (!done) {
-        unsigned long long f[kLookbackPerLane];
-        T v[kLookbackPerLane];
-        unsigned long long bits[kLookbackPerLane];
-#pragma unroll
-        for (int j = 0; j < kLookbackPerLane; ++j) {  // all loads first
-          const int64_t p = p_hi - (j * 32 + lane);
-          f[j] = INC;                                  // p < 0: end of the lookback
-          bits[j] = 0ull;
-          if (p >= 0) desc_load(descs + p, f[j], bits[j]);
-        }
-#pragma unroll
-        for (int j = 0; j < kLookbackPerLane; ++j) {  // then wait for the late ones
-          const int64_t p = p_hi - (j * 32 + lane);
-          if (p >= 0 && f[j] < AGG) f[j] = wait_desc(descs, p, AGG, INC, hdr, bits[j]);
-          v[j] = from_bits<T>(bits[j]);
-        }
-        // nearest window slot holding an inclusive prefix
-        int stop = 32 * kLookbackPerLane;
-#pragma unroll
-        for (int j = kLookbackPerLane - 1; j >= 0; --j) {
-          const unsigned int m = __ballot_sync(0xffffffffu, f[j] == INC);
-          if (m) stop = j * 32 + __ffs(m) - 1;
-        }
-        // fixed order: slots j = 0.. summed per lane, then a fixed lane tree
-        T val = T(0);
-#pragma unroll
-        for (int j = 0; j < kLookbackPerLane; ++j)
-          if (j * 32 + lane <= stop) val += v[j];
-#pragma unroll
-        for (int off = 16; off > 0; off >>= 1) val += __shfl_down_sync(0xffffffffu, val, off);
-        acc += __shfl_sync(0xffffffffu, val, 0);
-        if (stop < 32 * kLookbackPerLane) done = true;
-        p_hi -= 32 * kLookbackPerLane;
-      }
-      exclusive = acc;
-    }
+    const T exclusive =
+        (tile > 0) ? lookback_exclusive<T>(descs, tile, AGG, INC, hdr) : init;
     named_sync(2, kScanThreads);  // the loaders have the tile aggregate
     if (lane == 0) {
       desc_store(descs + tile, INC, to_bits<T>(exclusive + s_agg));
@@ -210,7 +83,17 @@ scan_kernel(const T* __restrict__ x, T* __restrict__ y, int64_t n, T init,
   } else {
     // ---- loaders ----
     const int ltid = tid - 32, lwarp = warp - 1;
-    if (base + kTile <= n) {
+    if (VEC && base + kTile <= n) {
+      // 16-byte loads of item pairs (x 16-byte aligned, tiles start even)
+      const V2* xv = reinterpret_cast<const V2*>(x + base);
+#pragma unroll
+      for (int u = 0; u < IT / 2; ++u) {
+        const int k2 = u * kScanBlock + ltid;
+        const V2 v = __ldcs(xv + k2);
+        s_tile[pad(2 * k2)] = v.x;
+        s_tile[pad(2 * k2 + 1)] = v.y;
+      }
+    } else if (base + kTile <= n) {
 #pragma unroll
       for (int u = 0; u < IT; ++u) {
         const int k = u * kScanBlock + ltid;
@@ -258,7 +141,17 @@ scan_kernel(const T* __restrict__ x, T* __restrict__ y, int64_t n, T init,
     named_sync(1, kScanBlock);
     named_sync(3, kScanThreads);  // the lookback warp has the exclusive prefix
     const T prefix = s_excl;
-    if (base + kTile <= n) {
+    if (VEC && base + kTile <= n) {
+      V2* yv = reinterpret_cast<V2*>(y + base);
+#pragma unroll
+      for (int u = 0; u < IT / 2; ++u) {
+        const int k2 = u * kScanBlock + ltid;
+        V2 v;
+        v.x = prefix + s_tile[pad(2 * k2)];
+        v.y = prefix + s_tile[pad(2 * k2 + 1)];
+        __stcs(yv + k2, v);
+      }
+    } else if (base + kTile <= n) {
 #pragma unroll
       for (int u = 0; u < IT; ++u) {
         const int k = u * kScanBlock + ltid;
@@ -274,31 +167,20 @@ scan_kernel(const T* __restrict__ x, T* __restrict__ y, int64_t n, T init,
     }
   }
 
-  // the last CTA to finish prepares the workspace for the next call
   __syncthreads();
-  if (tid == 0) {
-    __threadfence();
-    unsigned int prev = atomicAdd(&hdr->done_counter, 1u);
-    s_last = (prev == gridDim.x - 1);
-  }
-  __syncthreads();
-  if (s_last && tid == 0) {
-    hdr->tile_counter = 0u;
-    hdr->done_counter = 0u;
-    __threadfence();
-    *reinterpret_cast<volatile unsigned long long*>(&hdr->epoch) = epoch + 1;
-  }
+  finish_launch(hdr, epoch, &s_last);
 }
 
 // The workspace is sized for the smallest tile, so it serves every tile size.
 int64_t scan_tiles_max(int64_t n) { return ceil_div(n > 0 ? n : 1, kScanTileMin); }
 
-template <typename T, int IT>
+template <typename T, int IT, bool VEC>
 int launch_scan_it(const T* x, T* y, int64_t n, T init, char* w, cudaStream_t st) {
   constexpr int kTile = kScanBlock * IT;
   constexpr size_t kSmem = static_cast<size_t>(kTile + kTile / IT) * sizeof(T);
   const cudaError_t attr = cudaFuncSetAttribute(
-      scan_kernel<T, IT>, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(kSmem));
+      scan_kernel<T, IT, VEC>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+      static_cast<int>(kSmem));
   if (attr != cudaSuccess) {
     set_error("scan: shared memory attribute: %s", cudaGetErrorString(attr));
     return B200_ERR_LAUNCH;
@@ -306,8 +188,8 @@ int launch_scan_it(const T* x, T* y, int64_t n, T init, char* w, cudaStream_t st
   const int64_t tiles = ceil_div(n, kTile);
   ScanHeader* hdr = reinterpret_cast<ScanHeader*>(w);
   TileDesc* descs = reinterpret_cast<TileDesc*>(w + 256);
-  scan_kernel<T, IT><<<static_cast<int>(tiles), kScanThreads, kSmem, st>>>(x, y, n, init, hdr,
-                                                                          descs);
+  scan_kernel<T, IT, VEC><<<static_cast<int>(tiles), kScanThreads, kSmem, st>>>(
+      x, y, n, init, hdr, descs);
   return B200_OK;
 }
 
@@ -329,8 +211,11 @@ int launch_scan(const char* name, const T* x, T* y, int64_t n, T init, void* ws,
     return B200_ERR_WORKSPACE;
   }
   char* w = static_cast<char*>(ws);
-  const int rc = (items == 16) ? launch_scan_it<T, 16>(x, y, n, init, w, st)
-                               : launch_scan_it<T, 32>(x, y, n, init, w, st);
+  const bool vec = aligned16(x) && aligned16(y) && !(tune && tune->vec == 1);
+  const int rc = (items == 16) ? (vec ? launch_scan_it<T, 16, true>(x, y, n, init, w, st)
+                                      : launch_scan_it<T, 16, false>(x, y, n, init, w, st))
+                               : (vec ? launch_scan_it<T, 32, true>(x, y, n, init, w, st)
+                                      : launch_scan_it<T, 32, false>(x, y, n, init, w, st));
   if (rc != B200_OK) return rc;
   return after_launch(name);
 }

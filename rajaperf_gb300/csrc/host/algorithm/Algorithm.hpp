@@ -1,7 +1,10 @@
-// Algorithm group kernels (suite src/algorithm): SCAN and REDUCE_SUM.
+// Algorithm group kernels (suite src/algorithm): SCAN, REDUCE_SUM, MEMSET,
+// MEMCPY and HISTOGRAM.
 #pragma once
 
 #include "common/KernelDecl.hpp"
+
+#include <vector>
 
 namespace rajaperf {
 namespace algorithm {
@@ -29,6 +32,26 @@ RAJAPERF_GB300_KERNEL(REDUCE_SUM,
   Real_ptr m_dsum = nullptr;
   void* m_ws = nullptr;
   size_t m_ws_bytes = 0;)
+
+RAJAPERF_GB300_KERNEL(MEMSET,
+ private:
+  Real_ptr m_x = nullptr;
+  Real_type m_val = 0.0;)
+
+RAJAPERF_GB300_KERNEL(MEMCPY,
+ private:
+  Real_ptr m_x = nullptr;
+  Real_ptr m_y = nullptr;)
+
+RAJAPERF_GB300_KERNEL(HISTOGRAM,
+ public:
+  void finishRun(size_t tune_idx) override;
+ private:
+  Index_type m_num_bins = 0;
+  Index_type* m_bins = nullptr;
+  unsigned long long* m_counts_init = nullptr;  // device copies of the suite's vectors
+  unsigned long long* m_counts = nullptr;
+  std::vector<unsigned long long> m_counts_final;)
 
 }  // namespace algorithm
 }  // namespace rajaperf

@@ -1,5 +1,7 @@
 #include "DataUtils.hpp"
 
+#include <algorithm>
+
 #include "b200.h"
 
 #include <cuda_runtime.h>
@@ -146,6 +148,65 @@ void initDeviceDataRandValue(const RunParams& rp, Real_ptr d, Size_type len) {
   detail::incDataInitCount();
 }
 
+void initDeviceDataInt(Int_ptr d, Size_type len) {
+  std::vector<Int_type> h(len);
+  std::srand(4793);
+  for (Size_type i = 0; i < len; ++i) {
+    const Real_type signfact = Real_type(std::rand()) / RAND_MAX;
+    h[i] = (signfact < 0.5 ? -1 : 1);
+  }
+  // (rand() == RAND_MAX would put the index at len: skipped here, written
+  // out of bounds by the suite)
+  Real_type signfact = Real_type(std::rand()) / RAND_MAX;
+  const Size_type ilo = static_cast<Size_type>(len * signfact);
+  if (ilo < len) h[ilo] = -58;
+  signfact = Real_type(std::rand()) / RAND_MAX;
+  const Size_type ihi = static_cast<Size_type>(len * signfact);
+  if (ihi < len) h[ihi] = 19;
+  copyToDevice(d, h.data(), len * sizeof(Int_type));
+  detail::incDataInitCount();
+}
+
+std::vector<Real_type> hostRandValues(Size_type len) {
+  std::vector<Real_type> h(len);
+  std::srand(4793);
+  for (Size_type i = 0; i < len; ++i) h[i] = Real_type(std::rand()) / RAND_MAX;
+  detail::incDataInitCount();
+  return h;
+}
+
+std::vector<Index_type> hostBinAssignment(Size_type len, Index_type num_bins,
+                                          RunParams::BinAssignmentAlgorithm algo) {
+  using A = RunParams::BinAssignmentAlgorithm;
+  std::vector<Index_type> bins(len);
+  if (algo == A::Random) {
+    const std::vector<Real_type> data = hostRandValues(len);
+    for (Size_type i = 0; i < len; ++i) {
+      Index_type b = static_cast<Index_type>(data[i] * num_bins);
+      if (b >= num_bins) b = num_bins - 1;
+      if (b < 0) b = 0;
+      bins[i] = b;
+    }
+    return bins;
+  }
+  std::vector<Real_type> bounds;
+  if (algo == A::RunsRandomSizes) {
+    bounds = hostRandValues(static_cast<Size_type>(num_bins));
+    std::sort(bounds.begin(), bounds.end());
+  } else {
+    bounds.resize(static_cast<Size_type>(num_bins));
+    for (Index_type b = 0; b < num_bins; ++b)
+      bounds[b] = (algo == A::RunsEvenSizes) ? static_cast<Real_type>(b + 1) / num_bins : 0.0;
+  }
+  Index_type bin = 0;
+  for (Size_type i = 0; i < len; ++i) {
+    const Real_type pos = static_cast<Real_type>(i) / len;
+    while (bin + 1 < num_bins && pos >= bounds[bin]) bin += 1;
+    bins[i] = bin;
+  }
+  return bins;
+}
+
 namespace {
 
 template <typename Getter>
@@ -183,6 +244,19 @@ long double calcChecksumDevice(const Real_type* d, Size_type len,
   std::vector<Real_type> h(len);
   copyToHost(h.data(), d, len * sizeof(Real_type));
   return calcChecksumHost(h.data(), len, scale_factor);
+}
+
+long double calcChecksumDevice(const Int_type* d, Size_type len, Real_type scale_factor) {
+  std::vector<Int_type> h(len);
+  copyToHost(h.data(), d, len * sizeof(Int_type));
+  return kahanChecksum([&h](Size_type j) { return static_cast<long double>(h[j]); }, len,
+                       scale_factor);
+}
+
+long double calcChecksumHost(const unsigned long long* h, Size_type len,
+                             Real_type scale_factor) {
+  return kahanChecksum([h](Size_type j) { return static_cast<long double>(h[j]); }, len,
+                       scale_factor);
 }
 
 long double calcChecksumDevice(const Index_type* d, Size_type len,

@@ -16,6 +16,7 @@
 #include "RunParams.hpp"
 
 #include <cstdint>
+#include <vector>
 
 namespace rajaperf {
 namespace detail {
@@ -40,6 +41,17 @@ void initDeviceDataConst(Real_ptr d, Size_type len, Real_type val);
 void initDeviceDataConst(Index_type* d, Size_type len, Index_type val);
 void initDeviceDataRandSign(const RunParams& rp, Real_ptr d, Size_type len);
 void initDeviceDataRandValue(const RunParams& rp, Real_ptr d, Size_type len);
+// Int_type arrays: +-1 by the C library generator, then -58 and 19 at two
+// generated positions (DataUtils.cpp:477-497), in either init mode.
+void initDeviceDataInt(Int_ptr d, Size_type len);
+// rand()/RAND_MAX values seeded as the suite seeds them (DataUtils.cpp:560-569),
+// on the host; bumps the data-init counter.
+std::vector<Real_type> hostRandValues(Size_type len);
+// The bin of every item for HISTOGRAM / MULTI_REDUCE, as their setUp assigns
+// them (algorithm/HISTOGRAM.cpp:73-131): runs whose boundaries are sorted
+// random values, even runs, one bin, or a random bin per item.
+std::vector<Index_type> hostBinAssignment(Size_type len, Index_type num_bins,
+                                          RunParams::BinAssignmentAlgorithm algo);
 
 // Host <-> device copies (synchronous).
 void copyToDevice(void* d, const void* h, Size_type nbytes);
@@ -52,10 +64,13 @@ long double calcChecksumDevice(const Real_type* d, Size_type len,
                                Real_type scale_factor);
 long double calcChecksumDevice(const Index_type* d, Size_type len,
                                Real_type scale_factor);
+long double calcChecksumDevice(const Int_type* d, Size_type len, Real_type scale_factor);
 // ... and of host data.
 long double calcChecksumHost(const Real_type* h, Size_type len,
                              Real_type scale_factor);
 long double calcChecksumHost(const long long* h, Size_type len,
+                             Real_type scale_factor);
+long double calcChecksumHost(const unsigned long long* h, Size_type len,
                              Real_type scale_factor);
 
 // Counter-based uniform value of the uniform input mode (identical to the

@@ -16,7 +16,8 @@ const std::array<std::string, NumGroups>& groupNames() {
 
 const std::array<std::string, NumKernels>& kernelNames() {
   static const std::array<std::string, NumKernels> names = {
-      "Basic_DAXPY",        "Basic_INIT3",         "Basic_MULADDSUB",
+      "Basic_DAXPY",        "Basic_INDEXLIST",     "Basic_INDEXLIST_3LOOP",
+      "Basic_INIT3",        "Basic_MULADDSUB",     "Basic_MULTI_REDUCE",
       "Lcals_DIFF_PREDICT", "Lcals_EOS",           "Lcals_FIRST_DIFF",
       "Lcals_FIRST_MIN",    "Lcals_HYDRO_1D",      "Lcals_HYDRO_2D",
       "Lcals_INT_PREDICT",  "Lcals_PLANCKIAN",     "Polybench_3MM",
@@ -24,7 +25,8 @@ const std::array<std::string, NumKernels>& kernelNames() {
       "Polybench_JACOBI_2D", "Stream_ADD",         "Stream_COPY",
       "Stream_DOT",         "Stream_MUL",          "Stream_TRIAD",
       "Apps_DEL_DOT_VEC_2D", "Apps_ENERGY",        "Apps_PRESSURE",
-      "Apps_VOL3D",         "Algorithm_SCAN",      "Algorithm_REDUCE_SUM"};
+      "Apps_VOL3D",         "Algorithm_SCAN",      "Algorithm_REDUCE_SUM",
+      "Algorithm_MEMSET",   "Algorithm_MEMCPY",    "Algorithm_HISTOGRAM"};
   return names;
 }
 

@@ -29,8 +29,11 @@ enum GroupID {
 
 enum KernelID {
   Basic_DAXPY = 0,
+  Basic_INDEXLIST,
+  Basic_INDEXLIST_3LOOP,
   Basic_INIT3,
   Basic_MULADDSUB,
+  Basic_MULTI_REDUCE,
 
   Lcals_DIFF_PREDICT,
   Lcals_EOS,
@@ -60,6 +63,9 @@ enum KernelID {
 
   Algorithm_SCAN,
   Algorithm_REDUCE_SUM,
+  Algorithm_MEMSET,
+  Algorithm_MEMCPY,
+  Algorithm_HISTOGRAM,
 
   NumKernels
 };

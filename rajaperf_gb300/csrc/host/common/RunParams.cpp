@@ -123,6 +123,19 @@ RunParams::RunParams(int argc, const char* const* argv) {
       long long v;
       if (!parseLong(takeValue(i, opt), v) || v < 0) fail("bad --polybench_tsteps");
       polybench_tsteps = static_cast<long>(v);
+    } else if (opt == "--multi_reduce_num_bins") {
+      long long v;
+      if (!parseLong(takeValue(i, opt), v) || v < 1) fail("bad --multi_reduce_num_bins");
+      multi_reduce_num_bins = static_cast<long>(v);
+    } else if (opt == "--multi_reduce_bin_assignment_algorithm") {
+      std::string v = takeValue(i, opt);
+      if (v == "Random") multi_reduce_bin_assignment = BinAssignmentAlgorithm::Random;
+      else if (v == "RunsRandomSizes")
+        multi_reduce_bin_assignment = BinAssignmentAlgorithm::RunsRandomSizes;
+      else if (v == "RunsEvenSizes")
+        multi_reduce_bin_assignment = BinAssignmentAlgorithm::RunsEvenSizes;
+      else if (v == "Single") multi_reduce_bin_assignment = BinAssignmentAlgorithm::Single;
+      else fail("bad --multi_reduce_bin_assignment_algorithm " + v);
     } else if (opt == "--size-map") {
       std::vector<std::string> items;
       takeList(i, items);
@@ -249,6 +262,9 @@ std::string RunParams::usage() {
       "  --init reference|uniform     array contents (default reference)\n"
       "  --seed S --init-range LO HI  seed and range of the uniform mode\n"
       "  --polybench_tsteps T         override Polybench time steps\n"
+      "  --multi_reduce_num_bins B    HISTOGRAM / MULTI_REDUCE bins (10)\n"
+      "  --multi_reduce_bin_assignment_algorithm Random|RunsRandomSizes|\n"
+      "                               RunsEvenSizes|Single (RunsRandomSizes)\n"
       "  --size-map K=N,...           per-kernel sizes\n"
       "  --tuning-table FILE          tuning table (kernel size-bucket params)\n"
       "  --autotune FILE              measure launch shapes for the selected\n"

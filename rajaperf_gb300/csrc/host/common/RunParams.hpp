@@ -47,6 +47,13 @@ class RunParams {
   // -1 when the kernel's own time-step count applies.
   long getPolybenchTsteps() const { return polybench_tsteps; }
 
+  // HISTOGRAM / MULTI_REDUCE bins (RunParams.hpp:107-135 of the suite).
+  enum struct BinAssignmentAlgorithm : int { Random, RunsRandomSizes, RunsEvenSizes, Single };
+  long getMultiReduceNumBins() const { return multi_reduce_num_bins; }
+  BinAssignmentAlgorithm getMultiReduceBinAssignmentAlgorithm() const {
+    return multi_reduce_bin_assignment;
+  }
+
   // Per-kernel target size from --size-map, or -1.
   double getKernelSize(KernelID kid) const;
 
@@ -86,6 +93,8 @@ class RunParams {
   double init_lo = 0.5;
   double init_hi = 1.5;
   long polybench_tsteps = -1;
+  long multi_reduce_num_bins = 10;
+  BinAssignmentAlgorithm multi_reduce_bin_assignment = BinAssignmentAlgorithm::RunsRandomSizes;
 
   std::map<KernelID, double> size_map;
   std::string tuning_table_file;

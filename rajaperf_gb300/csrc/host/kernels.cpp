@@ -20,6 +20,9 @@ KernelBase* getKernelObject(KernelID kid, const RunParams& rp) {
     case Basic_DAXPY: return new basic::DAXPY(rp);
     case Basic_INIT3: return new basic::INIT3(rp);
     case Basic_MULADDSUB: return new basic::MULADDSUB(rp);
+    case Basic_INDEXLIST: return new basic::INDEXLIST(rp);
+    case Basic_INDEXLIST_3LOOP: return new basic::INDEXLIST_3LOOP(rp);
+    case Basic_MULTI_REDUCE: return new basic::MULTI_REDUCE(rp);
     case Lcals_HYDRO_1D: return new lcals::HYDRO_1D(rp);
     case Lcals_HYDRO_2D: return new lcals::HYDRO_2D(rp);
     case Lcals_EOS: return new lcals::EOS(rp);
@@ -39,6 +42,9 @@ KernelBase* getKernelObject(KernelID kid, const RunParams& rp) {
     case Polybench_3MM: return new polybench::POLYBENCH_3MM(rp);
     case Algorithm_SCAN: return new algorithm::SCAN(rp);
     case Algorithm_REDUCE_SUM: return new algorithm::REDUCE_SUM(rp);
+    case Algorithm_MEMSET: return new algorithm::MEMSET(rp);
+    case Algorithm_MEMCPY: return new algorithm::MEMCPY(rp);
+    case Algorithm_HISTOGRAM: return new algorithm::HISTOGRAM(rp);
     default: return nullptr;
   }
 }

@@ -26,12 +26,25 @@ KERNELS = [
     "Polybench_JACOBI_2D", "Polybench_HEAT_3D", "Polybench_FDTD_2D",
     "Polybench_GEMM", "Polybench_3MM",
     "Algorithm_SCAN", "Algorithm_REDUCE_SUM",
+    "Basic_INDEXLIST", "Basic_INDEXLIST_3LOOP", "Basic_MULTI_REDUCE",
+    "Algorithm_MEMSET", "Algorithm_MEMCPY", "Algorithm_HISTOGRAM",
 ]
 CASES = [(1, 1), (31, 2), (1000, 3), (10000, 2), (65537, 1)]
 EXTRA = {
     # the suite's own CPU-runnable Stream case: N = 1e6
     "Stream_TRIAD": [(1000000, 5)],
     "Stream_DOT": [(1000000, 5)],
+}
+# further suite options per record: the bin counts and layouts of HISTOGRAM
+# and MULTI_REDUCE (--multi_reduce_num_bins, --multi_reduce_bin_assignment_algorithm)
+BIN_CASES = [(nb, algo, size) for nb, algo in ((1, "Single"), (7, "Random"), (100, "RunsEvenSizes"),
+                                               (100, "Random"), (3000, "RunsRandomSizes"))
+             for size in (1000, 65537)]
+OPTION_CASES = {
+    k: [(size, 2, ["--multi_reduce_num_bins", str(nb),
+                   "--multi_reduce_bin_assignment_algorithm", algo])
+        for nb, algo, size in BIN_CASES]
+    for k in ("Algorithm_HISTOGRAM", "Basic_MULTI_REDUCE")
 }
 
 
@@ -47,6 +60,12 @@ def main() -> None:
                 continue
             r = oracle.run_ref(k, size, reps)
             records.append({"kernel": k, "size": size, "reps": reps,
+                            "checksum": r["checksum"], "actual_size": r["actual_size"],
+                            "bytes_per_rep": r["bytes_per_rep"],
+                            "flops_per_rep": r["flops_per_rep"]})
+        for size, reps, args in OPTION_CASES.get(k, []):
+            r = oracle.run_ref(k, size, reps, args)
+            records.append({"kernel": k, "size": size, "reps": reps, "args": args,
                             "checksum": r["checksum"], "actual_size": r["actual_size"],
                             "bytes_per_rep": r["bytes_per_rep"],
                             "flops_per_rep": r["flops_per_rep"]})

@@ -192,6 +192,25 @@ def test_scan_f64_and_i64(n, items):
     assert hdr[4] == 0, "lookback wait gave up"
 
 
+@pytest.mark.parametrize("n", [8192 * 3 + 5, 1 << 20])
+def test_scan_misaligned_pointers(n):
+    """x and y one element past a 16-byte boundary: the 8-byte load/store
+    path; results must match the vector path's exactly (int64)."""
+    torch = gu.torch_cuda()
+    rng = np.random.default_rng(n)
+    xi = rng.integers(0, 100, n + 1).astype(np.int64)
+    dx = dev(xi)
+    dy = torch.zeros(n + 1, dtype=torch.int64, device="cuda")
+    wsb = lib().b200_scan_workspace_bytes(n)
+    w = ws(wsb)
+    rp.check(lib().b200_algorithm_scan_i64(dx.data_ptr() + 8, dy.data_ptr() + 8, n, 3,
+                                           w.data_ptr(), wsb, None, gu.stream()))
+    want = 3 + np.concatenate([[0], np.cumsum(xi[1:])[:-1]])
+    got = gu.host(dy)[1:]
+    assert np.array_equal(got, want)
+    assert gu.host(dy)[0] == 0  # nothing written before y
+
+
 @pytest.mark.parametrize("case", ["planted", "ties", "first", "last", "negzero", "tiny",
                                   "nan", "inf"])
 def test_first_min_exact(case):

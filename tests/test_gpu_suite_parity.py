@@ -19,7 +19,7 @@ pytestmark = pytest.mark.gpu
 
 RECORDS = json.load(open(gu.GOLDEN))["records"]
 KERNELS = sorted({r["kernel"] for r in RECORDS})
-SUMS = {"Stream_DOT", "Algorithm_REDUCE_SUM", "Algorithm_SCAN"}
+SUMS = {"Stream_DOT", "Algorithm_REDUCE_SUM", "Algorithm_SCAN", "Basic_MULTI_REDUCE"}
 
 
 def _check(kernel, rec, got):
@@ -42,7 +42,8 @@ def _check(kernel, rec, got):
 def test_kernel_matches_suite_base_seq(kernel):
     for rec in [r for r in RECORDS if r["kernel"] == kernel]:
         res = rp.run_suite(["--size", rec["size"], "--checkrun", rec["reps"], "-k", kernel,
-                            "-t", "default", "graph", "--disable-warmup"])
+                            "-t", "default", "graph", "--disable-warmup",
+                            *rec.get("args", [])])
         assert {r["tuning"] for r in res} == {"default", "graph"}, res
         for r in res:
             _check(kernel, rec, r)

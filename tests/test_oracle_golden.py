@@ -16,9 +16,25 @@ GOLDEN = os.path.join(os.path.dirname(__file__), "golden", "ref_checksums.json")
 RECORDS = json.load(open(GOLDEN))["records"]
 
 
-@pytest.mark.parametrize("rec", RECORDS, ids=lambda r: f"{r['kernel']}-{r['size']}x{r['reps']}")
+def option_kwargs(args):
+    """oracle.run keywords for a record's further suite options."""
+    kw = {}
+    for opt, val in zip(args[::2], args[1::2]):
+        if opt == "--multi_reduce_num_bins":
+            kw["num_bins"] = int(val)
+        elif opt == "--multi_reduce_bin_assignment_algorithm":
+            kw["bin_algo"] = val
+        else:
+            raise KeyError(opt)
+    return kw
+
+
+@pytest.mark.parametrize("rec", RECORDS,
+                         ids=lambda r: f"{r['kernel']}-{r['size']}x{r['reps']}"
+                                       + ("-" + "-".join(r["args"][1::2]) if "args" in r else ""))
 def test_oracle_matches_suite_base_seq(rec):
-    r = oracle.run(rec["kernel"], size=rec["size"], reps=rec["reps"])
+    r = oracle.run(rec["kernel"], size=rec["size"], reps=rec["reps"],
+                   **option_kwargs(rec.get("args", [])))
     assert r["actual_size"] == rec["actual_size"]
     assert r["bytes_per_rep"] == rec["bytes_per_rep"]
     assert r["flops_per_rep"] == rec["flops_per_rep"]
