@@ -415,6 +415,30 @@ int b200_basic_multi_reduce(const int64_t* bins, const double* data, int64_t n,
                             size_t workspace_bytes, const b200_tune* tune,
                             b200_stream_t stream);
 
+/* ---- Comm: halo packing (one process) ----------------------------------- */
+
+/* One (neighbour, variable) piece of a halo exchange: `len` entries of the
+ * int32 index `list` into `var`, packed into / unpacked from `buffer`.  All
+ * pointers are device addresses. */
+typedef struct b200_halo_seg {
+  double* var;
+  const int32_t* list;
+  double* buffer;
+  int64_t len;
+} b200_halo_seg;
+
+/* buffer[i] = var[list[i]] for every segment of `pack` (HALO_PACK_BODY), then
+ * var[list[i]] = buffer[i] for every segment of `unpack` (HALO_UNPACK_BODY),
+ * in that order; at most 256 segments per direction, tables in host memory.
+ * Unpack segments run concurrently: two of them writing the same element
+ * land in unspecified order (halo lists never overlap).
+ * Two launches, where the suite launches one kernel per segment
+ *   -- comm/HALO_base.hpp:25-29, HALO_PACKING-Cuda.cpp,
+ *      HALO_PACKING_FUSED-Cuda.cpp.                                         */
+int b200_comm_halo_packing(const b200_halo_seg* pack, int32_t n_pack,
+                           const b200_halo_seg* unpack, int32_t n_unpack,
+                           const b200_tune* tune, b200_stream_t stream);
+
 /* *sum = sum_init + sum_i x[i], fixed-shape tree (deterministic)
  *   -- algorithm/REDUCE_SUM.hpp:25-32, REDUCE_SUM-Seq.cpp:34-48             */
 int b200_algorithm_reduce_sum(const double* x, int64_t n, double sum_init,

@@ -32,7 +32,8 @@ class OracleOpts(ctypes.Structure):
                 ("seed", ctypes.c_ulonglong), ("lo", ctypes.c_double),
                 ("hi", ctypes.c_double), ("tsteps", ctypes.c_long),
                 ("variant", ctypes.c_int), ("skip_checksum", ctypes.c_int),
-                ("num_bins", ctypes.c_long), ("bin_algo", ctypes.c_int)]
+                ("num_bins", ctypes.c_long), ("bin_algo", ctypes.c_int),
+                ("halo_width", ctypes.c_long), ("halo_num_vars", ctypes.c_long)]
 
 
 class OracleResult(ctypes.Structure):
@@ -110,7 +111,8 @@ def lib() -> ctypes.CDLL:
 def run(kernel: str, size: float = -1, reps: int = 1, init: str = "reference",
         seed: int = 4793, lo: float = 0.5, hi: float = 1.5, tsteps: int = -1,
         threads: int = 0, variant: int = 0, skip_checksum: bool = False,
-        num_bins: int = 10, bin_algo: str = "RunsRandomSizes") -> dict:
+        num_bins: int = 10, bin_algo: str = "RunsRandomSizes", halo_width: int = 1,
+        halo_num_vars: int = 3) -> dict:
     """Runs one kernel with the suite's Base_Seq (threads=0) or Base_OpenMP
     semantics and returns its checksum, sizes and rep-loop time."""
     algos = ["Random", "RunsRandomSizes", "RunsEvenSizes", "Single"]
@@ -118,7 +120,8 @@ def run(kernel: str, size: float = -1, reps: int = 1, init: str = "reference",
                    init_mode=1 if init == "uniform" else 0, threads=int(threads),
                    seed=int(seed), lo=float(lo), hi=float(hi), tsteps=int(tsteps),
                    variant=int(variant), skip_checksum=1 if skip_checksum else 0,
-                   num_bins=int(num_bins), bin_algo=algos.index(bin_algo))
+                   num_bins=int(num_bins), bin_algo=algos.index(bin_algo),
+                   halo_width=int(halo_width), halo_num_vars=int(halo_num_vars))
     r = OracleResult()
     st = lib().oracle_run(kernel.encode(), ctypes.byref(o), ctypes.byref(r))
     if st != 0:

@@ -1713,6 +1713,110 @@ done:
 }
 
 /* ------------------------------------------------------------------------ */
+/* Comm HALO_PACKING / HALO_PACKING_FUSED (one rank)                           */
+/* ------------------------------------------------------------------------ */
+
+/* comm/HALO_base.cpp:80-116 */
+static const int kHaloOffsets[26][3] = {
+    {-1, 0, 0},   {1, 0, 0},   {0, -1, 0},  {0, 1, 0},   {0, 0, -1},  {0, 0, 1},
+    {-1, -1, 0},  {-1, 1, 0},  {1, -1, 0},  {1, 1, 0},   {-1, 0, -1}, {-1, 0, 1},
+    {1, 0, -1},   {1, 0, 1},   {0, -1, -1}, {0, -1, 1},  {0, 1, -1},  {0, 1, 1},
+    {-1, -1, -1}, {-1, -1, 1}, {-1, 1, -1}, {-1, 1, 1},  {1, -1, -1}, {1, -1, 1},
+    {1, 1, -1},   {1, 1, 1}};
+
+/* comm/HALO_base.cpp:118-162 (send: the boundary layer; recv: the halo) */
+static void halo_bounds(int off, int send, idx_t w, idx_t dim, idx_t* lo, idx_t* hi) {
+  if (off == -1) { *lo = send ? w : 0; *hi = send ? 2 * w : w; }
+  else if (off == 0) { *lo = w; *hi = w + dim; }
+  else { *lo = send ? dim : w + dim; *hi = send ? w + dim : w + dim + w; }
+}
+
+/* comm/HALO_base.cpp:164-276: the list of one neighbour and direction */
+static int* halo_list(const idx_t* gd, idx_t w, int l, int send, idx_t* len) {
+  idx_t lo[3], hi[3];
+  for (int d = 0; d < 3; ++d) halo_bounds(kHaloOffsets[l][d], send, w, gd[d], &lo[d], &hi[d]);
+  idx_t js = gd[0] + 2 * w, ks = js * (gd[1] + 2 * w);
+  *len = (hi[0] - lo[0]) * (hi[1] - lo[1]) * (hi[2] - lo[2]);
+  int* list = (int*)malloc(sizeof(int) * (size_t)(*len > 0 ? *len : 1));
+  if (!list) return NULL;
+  idx_t k = 0;
+  for (idx_t kk = lo[2]; kk < hi[2]; ++kk)
+    for (idx_t jj = lo[1]; jj < hi[1]; ++jj)
+      for (idx_t ii = lo[0]; ii < hi[0]; ++ii) list[k++] = (int)(ii + jj * js + kk * ks);
+  return list;
+}
+
+/* HALO_PACKING.cpp:18-170, HALO_PACKING-Seq.cpp (Base_Seq, one rank, pack
+ * and unpack buffers in the same space: no separate send/recv copies);
+ * HALO_PACKING_FUSED only differs in its kernel count. */
+static void run_halo_packing_any(ctx* c, oracle_result* r, int fused) {
+  idx_t reps = c->o->reps;
+  double target = c->o->size >= 0 ? c->o->size : 1000000.0;
+  idx_t w = c->o->halo_width > 0 ? c->o->halo_width : 1;
+  idx_t nv = c->o->halo_num_vars > 0 ? c->o->halo_num_vars : 3;
+  double cbrt_run = cbrt(target) + cbrt(3.0) - 1.0;
+  idx_t gd[3] = {(idx_t)cbrt_run, (idx_t)cbrt_run, (idx_t)cbrt_run};
+  idx_t var_size = (gd[0] + 2 * w) * (gd[1] + 2 * w) * (gd[2] + 2 * w);
+  idx_t actual = gd[0] * gd[1] * gd[1];
+  int* plist[26] = {0};
+  int* ulist[26] = {0};
+  idx_t plen[26], ulen[26];
+  double* vars[16] = {0};
+  double* pbuf[26] = {0};
+  double* ubuf[26] = {0};
+  long double ck = 0.0L;
+  double t0;
+  int ok = nv <= 16;
+  for (int l = 0; ok && l < 26; ++l) {
+    plist[l] = halo_list(gd, w, l, 1, &plen[l]);
+    c->count++;  /* allocAndInitData of the list, then overwritten */
+    ulist[l] = halo_list(gd, w, l, 0, &ulen[l]);
+    c->count++;
+    ok = plist[l] && ulist[l];
+  }
+  for (idx_t v = 0; ok && v < nv; ++v) {
+    vars[v] = alloc_raw(var_size);
+    c->count++;  /* allocAndInitData, then var[i] = i + v */
+    ok = vars[v] != NULL;
+    for (idx_t i = 0; ok && i < var_size; ++i) vars[v][i] = (double)(i + v);
+  }
+  for (int l = 0; ok && l < 26; ++l) ok = (pbuf[l] = alloc_init(c, nv * plen[l])) != NULL;
+  for (int l = 0; ok && l < 26; ++l) ok = (ubuf[l] = alloc_init(c, nv * ulen[l])) != NULL;
+  if (!ok) { r->status = 3; goto done; }
+  t0 = now_s();
+  for (idx_t irep = 0; irep < reps; ++irep) {
+    for (int l = 0; l < 26; ++l) {
+      double* buffer = pbuf[l];
+      for (idx_t v = 0; v < nv; ++v) {
+        for (idx_t i = 0; i < plen[l]; ++i) buffer[i] = vars[v][plist[l][i]];
+        buffer += plen[l];
+      }
+    }
+    for (int l = 0; l < 26; ++l) {
+      double* buffer = ubuf[l];
+      for (idx_t v = 0; v < nv; ++v) {
+        for (idx_t i = 0; i < ulen[l]; ++i) vars[v][ulist[l][i]] = buffer[i];
+        buffer += ulen[l];
+      }
+    }
+  }
+  t0 = now_s() - t0;
+  for (idx_t v = 0; v < nv; ++v) ck += checksum_ld(vars[v], var_size, 1.0);
+  for (int l = 0; l < 26; ++l) ck += checksum_ld(pbuf[l], nv * plen[l], 1.0);
+  {
+    idx_t its = nv * (var_size - actual);
+    set_result(r, ck, actual, reps, its, fused ? 2 : 2 * 26 * nv, 4 * its + 8 * its + 4 * its +
+               8 * its + 8 * its + 8 * its, 0, t0);
+  }
+done:
+  for (int l = 0; l < 26; ++l) { free(plist[l]); free(ulist[l]); free(pbuf[l]); free(ubuf[l]); }
+  for (int v = 0; v < 16; ++v) free(vars[v]);
+}
+
+static void run_halo_packing(ctx* c, oracle_result* r) { run_halo_packing_any(c, r, 0); }
+static void run_halo_packing_fused(ctx* c, oracle_result* r) { run_halo_packing_any(c, r, 1); }
+
+/* ------------------------------------------------------------------------ */
 
 typedef void (*runner_fn)(ctx*, oracle_result*);
 
@@ -1737,6 +1841,7 @@ static const struct {
     {"Algorithm_MEMCPY", run_memcpy},   {"Algorithm_HISTOGRAM", run_histogram},
     {"Basic_INDEXLIST", run_indexlist}, {"Basic_INDEXLIST_3LOOP", run_indexlist_3loop},
     {"Basic_MULTI_REDUCE", run_multi_reduce},
+    {"Comm_HALO_PACKING", run_halo_packing}, {"Comm_HALO_PACKING_FUSED", run_halo_packing_fused},
 };
 
 int oracle_run(const char* kernel, const oracle_opts* opts, oracle_result* out) {

@@ -34,6 +34,8 @@ typedef struct oracle_opts {
   int skip_checksum;       /* 1: time the rep loop only (checksum = 0)      */
   long num_bins;           /* HISTOGRAM / MULTI_REDUCE bins; <= 0 = 10       */
   int bin_algo;            /* 0 Random, 1 RunsRandomSizes (default), 2 RunsEvenSizes, 3 Single */
+  long halo_width;         /* HALO_PACKING halo width; <= 0 = 1             */
+  long halo_num_vars;      /* HALO_PACKING variables; <= 0 = 3              */
 } oracle_opts;
 
 typedef struct oracle_result {

@@ -40,6 +40,8 @@
 #include "algorithm/MEMSET.hpp"
 #include "algorithm/MEMCPY.hpp"
 #include "algorithm/HISTOGRAM.hpp"
+#include "comm/HALO_PACKING.hpp"
+#include "comm/HALO_PACKING_FUSED.hpp"
 
 #include <iostream>
 #include <string>
@@ -83,6 +85,8 @@ const std::vector<KName>& kernelNames() {
     {Basic_MULTI_REDUCE, "Basic_MULTI_REDUCE"},
     {Algorithm_MEMSET, "Algorithm_MEMSET"}, {Algorithm_MEMCPY, "Algorithm_MEMCPY"},
     {Algorithm_HISTOGRAM, "Algorithm_HISTOGRAM"},
+    {Comm_HALO_PACKING, "Comm_HALO_PACKING"},
+    {Comm_HALO_PACKING_FUSED, "Comm_HALO_PACKING_FUSED"},
   };
   return names;
 }
@@ -201,6 +205,8 @@ KernelBase* getKernelObject(KernelID kid, const RunParams& rp) {
     case Algorithm_MEMSET: return new algorithm::MEMSET(rp);
     case Algorithm_MEMCPY: return new algorithm::MEMCPY(rp);
     case Algorithm_HISTOGRAM: return new algorithm::HISTOGRAM(rp);
+    case Comm_HALO_PACKING: return new comm::HALO_PACKING(rp);
+    case Comm_HALO_PACKING_FUSED: return new comm::HALO_PACKING_FUSED(rp);
     default: return nullptr;
   }
 }

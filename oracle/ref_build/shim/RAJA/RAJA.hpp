@@ -11,4 +11,11 @@
 // kernels' Seq files use without including them (std::memcpy, std::sort).
 #include <algorithm>
 #include <cstring>
+// Workgroup dispatch policy names that comm/HALO_base.hpp refers to in its
+// RAJA-variant helpers (never instantiated by the Base_Seq code built here).
+namespace RAJA {
+template <typename... Ts> struct direct_dispatch {};
+struct indirect_function_call_dispatch {};
+struct indirect_virtual_function_dispatch {};
+}  // namespace RAJA
 #endif

@@ -10,7 +10,7 @@ namespace {
 
 const std::array<std::string, NumGroups>& groupNames() {
   static const std::array<std::string, NumGroups> names = {
-      "Basic", "Lcals", "Polybench", "Stream", "Apps", "Algorithm"};
+      "Basic", "Lcals", "Polybench", "Stream", "Apps", "Algorithm", "Comm"};
   return names;
 }
 
@@ -26,7 +26,8 @@ const std::array<std::string, NumKernels>& kernelNames() {
       "Stream_DOT",         "Stream_MUL",          "Stream_TRIAD",
       "Apps_DEL_DOT_VEC_2D", "Apps_ENERGY",        "Apps_PRESSURE",
       "Apps_VOL3D",         "Algorithm_SCAN",      "Algorithm_REDUCE_SUM",
-      "Algorithm_MEMSET",   "Algorithm_MEMCPY",    "Algorithm_HISTOGRAM"};
+      "Algorithm_MEMSET",   "Algorithm_MEMCPY",    "Algorithm_HISTOGRAM",
+      "Comm_HALO_PACKING",  "Comm_HALO_PACKING_FUSED"};
   return names;
 }
 

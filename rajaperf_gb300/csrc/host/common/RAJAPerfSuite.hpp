@@ -24,6 +24,7 @@ enum GroupID {
   Stream,
   Apps,
   Algorithm,
+  Comm,
   NumGroups
 };
 
@@ -66,6 +67,9 @@ enum KernelID {
   Algorithm_MEMSET,
   Algorithm_MEMCPY,
   Algorithm_HISTOGRAM,
+
+  Comm_HALO_PACKING,
+  Comm_HALO_PACKING_FUSED,
 
   NumKernels
 };

@@ -136,6 +136,14 @@ RunParams::RunParams(int argc, const char* const* argv) {
         multi_reduce_bin_assignment = BinAssignmentAlgorithm::RunsEvenSizes;
       else if (v == "Single") multi_reduce_bin_assignment = BinAssignmentAlgorithm::Single;
       else fail("bad --multi_reduce_bin_assignment_algorithm " + v);
+    } else if (opt == "--halo_width") {
+      long long v;
+      if (!parseLong(takeValue(i, opt), v) || v < 1) fail("bad --halo_width");
+      halo_width = static_cast<long>(v);
+    } else if (opt == "--halo_num_vars") {
+      long long v;
+      if (!parseLong(takeValue(i, opt), v) || v < 1 || v > 9) fail("bad --halo_num_vars (1-9)");
+      halo_num_vars = static_cast<long>(v);
     } else if (opt == "--size-map") {
       std::vector<std::string> items;
       takeList(i, items);
@@ -265,6 +273,7 @@ std::string RunParams::usage() {
       "  --multi_reduce_num_bins B    HISTOGRAM / MULTI_REDUCE bins (10)\n"
       "  --multi_reduce_bin_assignment_algorithm Random|RunsRandomSizes|\n"
       "                               RunsEvenSizes|Single (RunsRandomSizes)\n"
+      "  --halo_width W --halo_num_vars V  HALO_PACKING halo (1) and variables (3)\n"
       "  --size-map K=N,...           per-kernel sizes\n"
       "  --tuning-table FILE          tuning table (kernel size-bucket params)\n"
       "  --autotune FILE              measure launch shapes for the selected\n"

@@ -50,6 +50,9 @@ class RunParams {
   // HISTOGRAM / MULTI_REDUCE bins (RunParams.hpp:107-135 of the suite).
   enum struct BinAssignmentAlgorithm : int { Random, RunsRandomSizes, RunsEvenSizes, Single };
   long getMultiReduceNumBins() const { return multi_reduce_num_bins; }
+  // HALO_PACKING halo width and variable count (suite defaults 1 and 3).
+  long getHaloWidth() const { return halo_width; }
+  long getHaloNumVars() const { return halo_num_vars; }
   BinAssignmentAlgorithm getMultiReduceBinAssignmentAlgorithm() const {
     return multi_reduce_bin_assignment;
   }
@@ -94,6 +97,8 @@ class RunParams {
   double init_hi = 1.5;
   long polybench_tsteps = -1;
   long multi_reduce_num_bins = 10;
+  long halo_width = 1;
+  long halo_num_vars = 3;
   BinAssignmentAlgorithm multi_reduce_bin_assignment = BinAssignmentAlgorithm::RunsRandomSizes;
 
   std::map<KernelID, double> size_map;

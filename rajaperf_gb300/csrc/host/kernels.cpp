@@ -4,6 +4,7 @@
 #include "algorithm/Algorithm.hpp"
 #include "apps/Apps.hpp"
 #include "basic/Basic.hpp"
+#include "comm/Comm.hpp"
 #include "lcals/Lcals.hpp"
 #include "polybench/Polybench.hpp"
 #include "stream/Stream.hpp"
@@ -45,6 +46,8 @@ KernelBase* getKernelObject(KernelID kid, const RunParams& rp) {
     case Algorithm_MEMSET: return new algorithm::MEMSET(rp);
     case Algorithm_MEMCPY: return new algorithm::MEMCPY(rp);
     case Algorithm_HISTOGRAM: return new algorithm::HISTOGRAM(rp);
+    case Comm_HALO_PACKING: return new comm::HALO_PACKING(rp);
+    case Comm_HALO_PACKING_FUSED: return new comm::HALO_PACKING_FUSED(rp);
     default: return nullptr;
   }
 }

@@ -28,6 +28,7 @@ KERNELS = [
     "Algorithm_SCAN", "Algorithm_REDUCE_SUM",
     "Basic_INDEXLIST", "Basic_INDEXLIST_3LOOP", "Basic_MULTI_REDUCE",
     "Algorithm_MEMSET", "Algorithm_MEMCPY", "Algorithm_HISTOGRAM",
+    "Comm_HALO_PACKING", "Comm_HALO_PACKING_FUSED",
 ]
 CASES = [(1, 1), (31, 2), (1000, 3), (10000, 2), (65537, 1)]
 EXTRA = {
@@ -46,6 +47,10 @@ OPTION_CASES = {
         for nb, algo, size in BIN_CASES]
     for k in ("Algorithm_HISTOGRAM", "Basic_MULTI_REDUCE")
 }
+# halo width and variable count of HALO_PACKING(_FUSED)
+for _k in ("Comm_HALO_PACKING", "Comm_HALO_PACKING_FUSED"):
+    OPTION_CASES[_k] = [(size, 2, ["--halo_width", str(w), "--halo_num_vars", str(nv)])
+                        for w, nv in ((2, 1), (3, 4)) for size in (1000, 65537)]
 
 
 def main() -> None:

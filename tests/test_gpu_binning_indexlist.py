@@ -134,3 +134,51 @@ def test_bad_args_rejected():
                                       x.data_ptr(), 1 << 20, None, None) == rp.B200_ERR_INVALID_ARG
     assert lib().b200_basic_indexlist(x.data_ptr(), x.data_ptr(), 100, x.data_ptr(),
                                       x.data_ptr(), 8, None, None) == rp.B200_ERR_WORKSPACE
+
+
+class HaloSeg(ctypes.Structure):
+    _fields_ = [("var", ctypes.c_void_p), ("list", ctypes.c_void_p),
+                ("buffer", ctypes.c_void_p), ("len", ctypes.c_int64)]
+
+
+def test_halo_packing_segments():
+    """Packs read the variables before any unpack of the same call writes
+    them; empty segments are skipped; the largest segment tables work."""
+    torch = gu.torch_cuda()
+    rng = np.random.default_rng(9)
+    nvar, size = 3, 5000
+    var_h = [rng.uniform(-1, 1, size) for _ in range(nvar)]
+    var_d = [gu.dev(v.copy()) for v in var_h]
+    lens = [0, 1, 17, 1000, 3000]
+    pack, unpack, keep, expect_buf = [], [], [], []
+    cells = rng.permutation(size)  # disjoint unpack targets
+    pos = 0
+    for k, n in enumerate(lens * 40):  # 200 segments per direction
+        v = k % nvar
+        plist = rng.integers(0, size, n).astype(np.int32)
+        ulist = cells[pos:pos + min(n, 20)].astype(np.int32)
+        pos = (pos + len(ulist)) % (size - 20)
+        pl, ul = gu.dev(plist), gu.dev(ulist)
+        pb = torch.zeros(max(n, 1), dtype=torch.float64, device="cuda")
+        ub = gu.dev(rng.uniform(5, 6, max(len(ulist), 1)))
+        keep += [pl, ul, pb, ub]
+        pack.append(HaloSeg(var_d[v].data_ptr(), pl.data_ptr(), pb.data_ptr(), n))
+        unpack.append(HaloSeg(var_d[v].data_ptr(), ul.data_ptr(), ub.data_ptr(), len(ulist)))
+        expect_buf.append((pb, var_h[v][plist]))
+    P = (HaloSeg * len(pack))(*pack)
+    U = (HaloSeg * len(unpack))(*unpack)
+    rp.check(lib().b200_comm_halo_packing(ctypes.addressof(P), len(pack), ctypes.addressof(U),
+                                          len(unpack), None, gu.stream()))
+    for pb, want in expect_buf:  # packed from the values before the unpacks
+        assert np.array_equal(gu.host(pb)[:want.size], want)
+    want_vars = [v.copy() for v in var_h]
+    for k, seg in enumerate(unpack):
+        if seg.len:
+            ul = gu.host(keep[4 * k + 1])[:seg.len]
+            ub = gu.host(keep[4 * k + 3])[:seg.len]
+            want_vars[k % nvar][ul] = ub
+    for v in range(nvar):
+        assert np.array_equal(gu.host(var_d[v]), want_vars[v])
+    too_many = (HaloSeg * 257)()
+    assert lib().b200_comm_halo_packing(ctypes.addressof(too_many), 257, None, 0, None,
+                                        None) == rp.B200_ERR_INVALID_ARG

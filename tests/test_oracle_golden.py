@@ -24,6 +24,10 @@ def option_kwargs(args):
             kw["num_bins"] = int(val)
         elif opt == "--multi_reduce_bin_assignment_algorithm":
             kw["bin_algo"] = val
+        elif opt == "--halo_width":
+            kw["halo_width"] = int(val)
+        elif opt == "--halo_num_vars":
+            kw["halo_num_vars"] = int(val)
         else:
             raise KeyError(opt)
     return kw
