@@ -1,10 +1,12 @@
 // HISTOGRAM (counts[bins[i]] += 1) and MULTI_REDUCE (values[bins[i]] +=
 // data[i]): per-bin reductions over a bin index per item.
 //
-// HISTOGRAM: a CTA counts into a shared-memory histogram, lanes of a warp that
-// hit the same bin combined first (__match_any_sync, one shared atomic per
-// bin per warp row: the suite's default bin layout is long runs of one bin),
-// then adds its counts to the global counters with 64-bit atomics.  Integer
+// HISTOGRAM: up to 16 bins (the suite's default is 10), each thread counts in
+// packed 8-bit register counters; up to 16384 bins, a CTA counts into a
+// shared-memory histogram, lanes of a warp that hit the same bin combined
+// first (__match_any_sync: the suite's default bin layout is long runs of
+// one bin); the CTA then adds its counts to the global counters with 64-bit
+// atomics.  Integer
 // sums do not depend on order, so the counts are exact.  The global counters
 // start from counts_init (one small copy kernel).
 //
@@ -71,6 +73,65 @@ histogram_shared_kernel(const int64_t* __restrict__ bins, int64_t n, int64_t num
   __syncthreads();
   for (int64_t b = threadIdx.x; b < num_bins; b += kBlock)
     if (s_cnt[b]) atomicAdd(&counts[b], static_cast<unsigned long long>(s_cnt[b]));
+}
+
+// Up to 16 bins: every thread counts in two 64-bit words of 8-bit counters
+// (bin b adds 1 << 8*(b mod 8) to word b / 8: a shift and an add per item),
+// unpacked into 32-bit totals before any byte can overflow; warp and CTA
+// sums follow, and one 64-bit atomic per bin and CTA.
+constexpr int64_t kRegisterBins = 16;
+
+__global__ void __launch_bounds__(kBlock)
+histogram_register_kernel(const int64_t* __restrict__ bins, int64_t n, int num_bins,
+                          unsigned long long* __restrict__ counts) {
+  __shared__ unsigned int s_tot[kBlock / 32][kRegisterBins];
+  unsigned int acc[kRegisterBins];
+#pragma unroll
+  for (int k = 0; k < kRegisterBins; ++k) acc[k] = 0u;
+  unsigned long long lo = 0ull, hi = 0ull;
+  int pending = 0;
+  auto flush = [&]() {
+#pragma unroll
+    for (int k = 0; k < 8; ++k) {
+      acc[k] += static_cast<unsigned int>((lo >> (8 * k)) & 0xffull);
+      acc[8 + k] += static_cast<unsigned int>((hi >> (8 * k)) & 0xffull);
+    }
+    lo = hi = 0ull;
+    pending = 0;
+  };
+  for (int64_t t0 = static_cast<int64_t>(blockIdx.x) * (kBlock * kItems); t0 < n;
+       t0 += static_cast<int64_t>(gridDim.x) * (kBlock * kItems)) {
+    int64_t b[kItems];
+#pragma unroll
+    for (int u = 0; u < kItems; ++u) {
+      const int64_t i = t0 + u * kBlock + threadIdx.x;
+      b[u] = (i < n) ? __ldcs(bins + i) : -1;
+    }
+#pragma unroll
+    for (int u = 0; u < kItems; ++u) {
+      const bool ok = b[u] >= 0 && b[u] < num_bins;
+      const unsigned long long one = ok ? (1ull << (8 * (b[u] & 7))) : 0ull;
+      if (b[u] < 8) lo += one; else hi += one;
+    }
+    pending += kItems;
+    if (pending > 255 - kItems) flush();
+  }
+  flush();
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+#pragma unroll
+  for (int k = 0; k < kRegisterBins; ++k) {
+    unsigned int v = acc[k];
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) v += __shfl_down_sync(0xffffffffu, v, off);
+    if (lane == 0) s_tot[warp][k] = v;
+  }
+  __syncthreads();
+  if (threadIdx.x < num_bins) {
+    unsigned long long t = 0ull;
+#pragma unroll
+    for (int w = 0; w < kBlock / 32; ++w) t += s_tot[w][threadIdx.x];
+    if (t) atomicAdd(&counts[threadIdx.x], t);
+  }
 }
 
 __global__ void histogram_global_kernel(const int64_t* __restrict__ bins, int64_t n,
@@ -171,7 +232,11 @@ int b200_algorithm_histogram(const int64_t* bins, int64_t n, int64_t num_bins,
   copy_u64_kernel<<<small_grid(num_bins), 256, 0, st>>>(counts_init, counts, num_bins);
   int launches = 1;
   if (n > 0) {
-    if (num_bins <= kSharedBins) {
+    if (num_bins <= kRegisterBins) {
+      histogram_register_kernel<<<bin_grid(n), kBlock, 0, st>>>(bins, n,
+                                                               static_cast<int>(num_bins),
+                                                               counts);
+    } else if (num_bins <= kSharedBins) {
       const size_t smem = static_cast<size_t>(num_bins) * sizeof(unsigned int);
       if (smem > 48 * 1024) {
         const cudaError_t e = cudaFuncSetAttribute(histogram_shared_kernel,
