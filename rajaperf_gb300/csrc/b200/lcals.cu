@@ -184,6 +184,15 @@ first_min_kernel(const double* __restrict__ x, int64_t n, double xmin_init,
                                      : order_key(__double_as_longlong(xmin_init)),
                     initloc};
   KeyLoc m = init;
+  // Cheap filter: the order key of an element's high 32 bits never exceeds
+  // the high word of its full key (exact for normal values; -0 and NaNs map
+  // lower), so an element whose filter key is above the running minimum's
+  // high word cannot be smaller and skips the full 64-bit key.
+  int mh = static_cast<int>(m.key >> 32);
+  auto maybe = [&](long long bits) {
+    const int h = static_cast<int>(bits >> 32);
+    return (h ^ ((h >> 31) & 0x7fffffff)) <= mh;
+  };
   if (VEC) {
     // 16-byte loads of element pairs; a thread still meets its indices in
     // increasing order, so strict '<' keeps the first minimum it sees.
@@ -200,10 +209,11 @@ first_min_kernel(const double* __restrict__ x, int64_t n, double xmin_init,
 #pragma unroll
       for (int u = 0; u < IT; ++u) {
         const int64_t iv = t0 + u * BS + threadIdx.x;
-        if (iv < nv) {
+        if (iv < nv && (maybe(v[u].x) || maybe(v[u].y))) {
           const long long k0 = order_key(v[u].x), k1 = order_key(v[u].y);
           if (k0 < m.key) { m.key = k0; m.loc = 2 * iv; }
           if (k1 < m.key) { m.key = k1; m.loc = 2 * iv + 1; }
+          mh = static_cast<int>(m.key >> 32);
         }
       }
     }
@@ -223,8 +233,11 @@ first_min_kernel(const double* __restrict__ x, int64_t n, double xmin_init,
 #pragma unroll
       for (int u = 0; u < IT; ++u) {
         int64_t i = t0 + u * BS + threadIdx.x;
-        long long k = order_key(v[u]);
-        if (i < n && k < m.key) { m.key = k; m.loc = i; }
+        if (i < n && maybe(v[u])) {
+          long long k = order_key(v[u]);
+          if (k < m.key) { m.key = k; m.loc = i; }
+          mh = static_cast<int>(m.key >> 32);
+        }
       }
     }
   }
