@@ -83,7 +83,7 @@ constexpr int64_t kRegisterBins = 16;
 
 __global__ void __launch_bounds__(kBlock)
 histogram_register_kernel(const int64_t* __restrict__ bins, int64_t n, int num_bins,
-                          unsigned long long* __restrict__ counts) {
+                          bool vec, unsigned long long* __restrict__ counts) {
   __shared__ unsigned int s_tot[kBlock / 32][kRegisterBins];
   unsigned int acc[kRegisterBins];
 #pragma unroll
@@ -99,23 +99,35 @@ histogram_register_kernel(const int64_t* __restrict__ bins, int64_t n, int num_b
     lo = hi = 0ull;
     pending = 0;
   };
-  for (int64_t t0 = static_cast<int64_t>(blockIdx.x) * (kBlock * kItems); t0 < n;
+  auto count = [&](int64_t b) {
+    const bool ok = b >= 0 && b < num_bins;
+    const unsigned long long one = ok ? (1ull << (8 * (b & 7))) : 0ull;
+    if (b < 8) lo += one; else hi += one;
+  };
+  // item pairs with 16-byte loads (bins is 16-byte aligned when `vec`)
+  const int64_t units = vec ? (n >> 1) : n;
+  for (int64_t t0 = static_cast<int64_t>(blockIdx.x) * (kBlock * kItems); t0 < units;
        t0 += static_cast<int64_t>(gridDim.x) * (kBlock * kItems)) {
-    int64_t b[kItems];
+    longlong2 b[kItems];
 #pragma unroll
     for (int u = 0; u < kItems; ++u) {
       const int64_t i = t0 + u * kBlock + threadIdx.x;
-      b[u] = (i < n) ? __ldcs(bins + i) : -1;
+      if (vec) {
+        b[u] = (i < units) ? __ldcs(reinterpret_cast<const longlong2*>(bins) + i)
+                           : make_longlong2(-1, -1);
+      } else {
+        b[u] = make_longlong2((i < units) ? __ldcs(bins + i) : -1, -1);
+      }
     }
 #pragma unroll
     for (int u = 0; u < kItems; ++u) {
-      const bool ok = b[u] >= 0 && b[u] < num_bins;
-      const unsigned long long one = ok ? (1ull << (8 * (b[u] & 7))) : 0ull;
-      if (b[u] < 8) lo += one; else hi += one;
+      count(b[u].x);
+      count(b[u].y);
     }
-    pending += kItems;
-    if (pending > 255 - kItems) flush();
+    pending += 2 * kItems;
+    if (pending > 255 - 2 * kItems) flush();
   }
+  if (vec && (n & 1) && blockIdx.x == 0 && threadIdx.x == 0) count(__ldcs(bins + n - 1));
   flush();
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
 #pragma unroll
@@ -233,9 +245,8 @@ int b200_algorithm_histogram(const int64_t* bins, int64_t n, int64_t num_bins,
   int launches = 1;
   if (n > 0) {
     if (num_bins <= kRegisterBins) {
-      histogram_register_kernel<<<bin_grid(n), kBlock, 0, st>>>(bins, n,
-                                                               static_cast<int>(num_bins),
-                                                               counts);
+      histogram_register_kernel<<<bin_grid(n), kBlock, 0, st>>>(
+          bins, n, static_cast<int>(num_bins), aligned16(bins), counts);
     } else if (num_bins <= kSharedBins) {
       const size_t smem = static_cast<size_t>(num_bins) * sizeof(unsigned int);
       if (smem > 48 * 1024) {
