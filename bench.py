@@ -763,6 +763,17 @@ class ClockSampler:
 # GPU arm
 # --------------------------------------------------------------------------
 
+def combine_ranks(dist, step_s, value, device):
+    """Whole-job figures of N replicas: the slowest rank's step time and the
+    sum of the per-rank metric (every rank ran the full workload)."""
+    import torch
+    t = torch.tensor([step_s], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    v = torch.tensor([value], dtype=torch.float64, device=device)
+    dist.all_reduce(v, op=dist.ReduceOp.SUM)
+    return float(t.item()), float(v.item())
+
+
 def geomean(xs):
     xs = [x for x in xs if x > 0]
     return math.exp(sum(math.log(x) for x in xs) / len(xs)) if xs else 0.0
@@ -831,10 +842,6 @@ def run_gpu(args, rank, world):
                                               if fi is not None else None),
                            "launches": c.launches})
     step_s = sum(p["ms"] for p in per_kernel) / 1e3
-    if dist:
-        t = torch.tensor([step_s], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        step_s = float(t.item())
     value = 100.0 * geomean([p["frac"] for p in per_kernel])
 
     # e2e through the C ABI with host buffers
@@ -1099,13 +1106,14 @@ def main():
     ap.add_argument("--kernels", type=lambda s: s.split(","), default=None,
                     help="comma list: run only these kernels of the workload")
     ap.add_argument("--gemm", choices=["auto", "on", "off"], default="auto",
-                    help="split-precision vs native FP64 GEMM leg (auto: on for the "
-                         "default workload without --kernels)")
+                    help="split-precision vs native FP64 GEMM leg (auto: on for one "
+                         "rank and the default workload without --kernels)")
     ap.add_argument("--gemm-sizes", type=lambda s: [int(x) for x in s.split(",")],
                     default=[1024, 4096, 8192], help="square sizes of the GEMM leg")
     ap.add_argument("--extras", choices=["auto", "on", "off", "bw", "batch"], default="auto",
                     help="every 1-D kernel at 2^27 elements and the 20-kernel graph batch "
-                         "(auto: on for the default workload without --kernels)")
+                         "(auto: on for one rank and the default workload without "
+                         "--kernels)")
     ap.add_argument("--bw-size", type=int, default=1 << 27,
                     help="element count of the all-kernels bandwidth leg")
     args = ap.parse_args()
@@ -1149,14 +1157,14 @@ def main():
     res = run_gpu(args, rank, world)
     dist = res.pop("dist")
     gemm = None
-    if args.gemm == "on" or (args.gemm == "auto" and not args.kernels and rank == 0):
+    if args.gemm == "on" or (args.gemm == "auto" and not args.kernels and world == 1):
         import torch
         import rajaperf_gb300 as rp
         gemm = measure_gemm(torch, rp, torch.cuda.current_stream(), sizes=args.gemm_sizes)
     bw27 = batch = None
     extras = args.extras
     if extras == "auto":
-        extras = "on" if (not args.kernels and rank == 0) else "off"
+        extras = "on" if (not args.kernels and world == 1) else "off"
     if extras in ("on", "bw") and rank == 0:
         import torch
         import rajaperf_gb300 as rp
@@ -1167,10 +1175,7 @@ def main():
         batch = measure_graph_batch(rp, args.seed)
     value = res["value"]
     if dist:
-        import torch
-        t = torch.tensor([value], device="cuda", dtype=torch.float64)
-        dist.all_reduce(t)
-        value = float(t.item())
+        res["step_s"], value = combine_ranks(dist, res["step_s"], value, "cuda")
     if rank != 0:
         if dist:
             dist.destroy_process_group()
