@@ -353,12 +353,18 @@ int b200_gemm_split(const double* A, const double* B, double* C, int64_t m,
 
 /* Workspace for b200_algorithm_scan / _scan_i64 on n elements.  Zero it
  * once before first use; calls leave it ready for the next call.  The
- * 32-bit word at byte offset 16 becomes nonzero if a bounded wait gave up. */
+ * 32-bit word at byte offset 16 becomes nonzero if a bounded wait gave up;
+ * the results of that call are invalid and the workspace must be zeroed
+ * again before the next call. */
 size_t b200_scan_workspace_bytes(int64_t n);
 
-/* y[i] = init + sum_{j<i} x[j] (exclusive), single-pass decoupled lookback
- * with a dedicated lookback warp per tile; tune->items selects the tile
- * (32: 8192 items, the default; 16: 4096)
+/* y[i] = init + sum_{j<i} x[j] (exclusive), single-pass decoupled lookback.
+ * Default (tune->algo 0, x and y 16-byte aligned): one persistent CTA per SM
+ * streams 4096-item tiles through a ring of shared-memory stages with bulk
+ * copies (TMA), with warps dedicated to loading, tile aggregates, lookback
+ * and the in-place scan.  tune->algo 1 (and unaligned pointers): one CTA per
+ * tile with a dedicated lookback warp; tune->items selects its tile (32:
+ * 8192 items, the default; 16: 4096)
  *   -- algorithm/SCAN.hpp:23-36, SCAN-Cuda.cpp:143-300.  One launch.        */
 int b200_algorithm_scan(const double* x, double* y, int64_t n, double init,
                         void* workspace, size_t workspace_bytes,

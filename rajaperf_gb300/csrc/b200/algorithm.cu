@@ -8,10 +8,11 @@
 // lookback warp then publishes the tile's inclusive prefix and the loaders
 // write the tile out.  Flags carry a launch epoch, so the workspace never
 // needs re-zeroing between calls (and the call can be captured in a CUDA
-// graph): the last CTA to finish resets the tile counter and advances the
-// epoch.  Every wait is bounded; a wait that gives up sets the error word of
+// graph): the CTA that draws the launch's last tile id resets the tile
+// counter and advances the epoch.  Every wait is bounded; a wait that gives up sets the error word of
 // the workspace header (byte offset 16) and the call's results are invalid.
 #include "b200_internal.cuh"
+#include "b200_async.cuh"
 #include "b200_lookback.cuh"
 #include "b200_reduce.cuh"
 
@@ -58,7 +59,6 @@ scan_kernel(const T* __restrict__ x, T* __restrict__ y, int64_t n, T init,
   __shared__ T s_agg;
   __shared__ unsigned int s_tile_id;
   __shared__ unsigned long long s_epoch;
-  __shared__ bool s_last;
   auto pad = [](int i) { return i + (i >> kPadShift); };
 
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
@@ -167,9 +167,318 @@ scan_kernel(const T* __restrict__ x, T* __restrict__ y, int64_t n, T init,
     }
   }
 
-  __syncthreads();
-  finish_launch(hdr, epoch, &s_last);
 }
+
+// ---- pipelined persistent SCAN ---------------------------------------------
+// One CTA per SM walks tiles of 4096 items through a ring of seven
+// shared-memory stages, each role a warp of its own (or four):
+//  * producer (warp 0): once a stage is free, draws the next tile id from the
+//    launch counter and issues one bulk copy (TMA) of the tile.  A tile id is
+//    drawn only when its stage is free: an id held while waiting would delay
+//    that tile's aggregate and stall its successors' lookback;
+//  * aggregator (warp 1): as each tile lands, sums it and publishes the tile
+//    aggregate at once, so a successor's lookback depends only on data
+//    arrival, never on this CTA's earlier tiles;
+//  * lookback (warps 2-3, alternate tiles): starts as soon as the tile id is
+//    drawn, walks back to the nearest inclusive prefix and publishes this
+//    tile's inclusive prefix once the aggregate is in;
+//  * compute (warps 4-7): a thread owns a run of 32 consecutive items (16
+//    item pairs), sums it, scans the run sums across the tile, and when the
+//    tile's exclusive prefix arrives writes every item's prefix in place;
+//  * store (warp 8): writes a finished tile back with one bulk store and
+//    frees the stage when the store has read it.
+// A compute thread visits its pairs rotated by (run mod 16), so every
+// 16-byte shared-memory access of a warp is conflict-free without padding
+// the bulk-copied tile.  mbarriers link the roles per stage: drawn (tile id
+// set), full (data landed), summed (aggregate ready), prefix (exclusive
+// prefix ready), ready (results in place), empty (store has read the stage).
+// Every wait is bounded; one that gives up sets the workspace error word and
+// ends the CTA's work.  Measured on GB300 (int64, 2^26 items, time marks per
+// tile and role): the bare load -> store pipeline runs at the copy peak; what
+// the lookback adds is its L2 round trips under saturated HBM, which the
+// seven stages of loads in flight are there to cover.
+namespace pipe {
+
+constexpr int kTile = 4096;
+constexpr int kStages = 7;
+constexpr int kLookbackWarps = 2;
+constexpr int kComputeWarps = 4;
+constexpr int kFirstCompute = 2 + kLookbackWarps;
+constexpr int kStoreWarp = kFirstCompute + kComputeWarps;
+constexpr int kThreads = 32 * (kStoreWarp + 1);
+constexpr int kRuns = 32 * kComputeWarps;    // 128 runs per tile
+constexpr int kPairs = kTile / kRuns / 2;    // 16 pairs per run
+constexpr int kLookbackLanes = 8;            // 256 predecessors per round
+constexpr unsigned int kEnd = 0xffffffffu;
+constexpr uint64_t kWaitNs = 2000000000ull;  // 2 s
+
+template <typename T>
+struct Smem {
+  T tile[kStages][kTile];
+  T agg[kStages];
+  T excl[kStages];
+  T warp_total[kComputeWarps];
+  unsigned int ticket[kStages];
+  unsigned int phases[kStages];  // full-barrier phases started per stage
+  uint64_t drawn[kStages];
+  uint64_t full[kStages];
+  uint64_t summed[kStages];
+  uint64_t prefix[kStages];
+  uint64_t ready[kStages];
+  uint64_t empty[kStages];
+  unsigned long long epoch;
+  int abort;
+  int fail_loaded;   // compute group: a wait before its first barrier gave up
+  int fail_prefix;   // compute group: a wait before its second barrier gave up
+};
+
+template <typename T>
+constexpr size_t smem_bytes() { return sizeof(Smem<T>) + 128; }
+static_assert(sizeof(Smem<double>) + 128 <= 232448, "shared memory budget");
+
+// Bounded wait by a whole warp; the result is the same in every lane (a lane
+// that gave up fails the warp).  On expiry records the error and stops every
+// role of the CTA.
+template <typename T>
+__device__ __forceinline__ bool wait(Smem<T>& sm, uint64_t* bar, uint32_t parity,
+                                     ScanHeader* hdr) {
+  const bool ok = __all_sync(0xffffffffu, mbar_wait_for(bar, parity, kWaitNs));
+  if (!ok && (threadIdx.x & 31) == 0) {
+    atomicExch(&hdr->error, 1u);
+    *reinterpret_cast<volatile int*>(&sm.abort) = 1;
+  }
+  return ok;
+}
+
+template <typename T>
+__global__ void __launch_bounds__(kThreads, 1)
+scan_pipelined(const T* __restrict__ x, T* __restrict__ y, int64_t n, T init,
+               unsigned int tiles, ScanHeader* __restrict__ hdr,
+               TileDesc* __restrict__ descs) {
+  using V2 = typename Vec2<T>::type;
+  extern __shared__ unsigned char s_raw[];
+  Smem<T>& sm = *reinterpret_cast<Smem<T>*>(
+      (reinterpret_cast<uintptr_t>(s_raw) + 127) & ~static_cast<uintptr_t>(127));
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+
+  if (tid == 0) {
+    for (int s = 0; s < kStages; ++s) {
+      mbar_init(&sm.drawn[s], 1);
+      mbar_init(&sm.full[s], 1);
+      mbar_init(&sm.summed[s], 1);
+      mbar_init(&sm.prefix[s], 1);
+      mbar_init(&sm.ready[s], 1);
+      mbar_init(&sm.empty[s], 1);
+      sm.phases[s] = 0u;
+    }
+    sm.abort = 0;
+    sm.fail_loaded = 0;
+    sm.fail_prefix = 0;
+    mbar_init_fence();
+  }
+  __syncthreads();
+  volatile int* abort_flag = &sm.abort;
+
+  if (warp == 0) {
+    // ---- producer ----
+    const unsigned long long draws = static_cast<unsigned long long>(tiles) + gridDim.x;
+    int ends = 0;
+    for (int k = 0; ends < kLookbackWarps && !__any_sync(0xffffffffu, *abort_flag); ++k) {
+      const int s = k % kStages;
+      if (k >= kStages && !wait(sm, &sm.empty[s], ((k / kStages) - 1) & 1, hdr)) break;
+      unsigned int tile = kEnd;
+      if (ends == 0) {
+        unsigned long long t = 0;
+        if (lane == 0) {
+          t = atomicAdd(&hdr->ticket, 1ull);
+          // the launch's last draw: every CTA has drawn; reset and next epoch
+          if (static_cast<unsigned int>(t) == draws - 1)
+            atomicAdd(&hdr->ticket, (1ull << 32) - draws);
+        }
+        t = __shfl_sync(0xffffffffu, t, 0);
+        if (k == 0 && lane == 0) sm.epoch = t >> 32;
+        if (static_cast<unsigned int>(t) < tiles) tile = static_cast<unsigned int>(t);
+      }
+      if (lane == 0) {
+        sm.ticket[s] = tile;
+        mbar_arrive(&sm.drawn[s]);
+      }
+      if (tile == kEnd) {
+        // one end marker per lookback warp (they take alternate stages)
+        ++ends;
+        __syncwarp();
+        if (lane == 0) {
+          ++sm.phases[s];
+          mbar_arrive(&sm.full[s]);
+        }
+        continue;
+      }
+      const int64_t base = static_cast<int64_t>(tile) * kTile;
+      if (base + kTile <= n) {
+        if (lane == 0) {
+          ++sm.phases[s];
+          mbar_arrive_expect_tx(&sm.full[s], kTile * sizeof(T));
+          bulk_load(sm.tile[s], x + base, kTile * sizeof(T), &sm.full[s]);
+        }
+      } else {
+        // the ragged last tile: plain loads, zero-filled
+        for (int i = lane; i < kTile; i += 32) sm.tile[s][i] = (base + i < n) ? x[base + i] : T(0);
+        __syncwarp();
+        if (lane == 0) {
+          ++sm.phases[s];
+          mbar_arrive(&sm.full[s]);
+        }
+      }
+    }
+  } else if (warp == 1) {
+    // ---- aggregator ----
+    for (int k = 0;; ++k) {
+      const int s = k % kStages;
+      const uint32_t par = (k / kStages) & 1;
+      if (!wait(sm, &sm.full[s], par, hdr)) break;
+      const unsigned int tile = sm.ticket[s];
+      if (tile == kEnd) break;
+      // lane L sums pairs L, L + 32, ... (consecutive lanes: consecutive
+      // 16-byte words, conflict-free)
+      const V2* tv = reinterpret_cast<const V2*>(sm.tile[s]);
+      T total = T(0);
+#pragma unroll 16
+      for (int q = lane; q < kTile / 2; q += 32) {
+        const V2 v = tv[q];
+        total += v.x;
+        total += v.y;
+      }
+#pragma unroll
+      for (int off = 16; off > 0; off >>= 1) total += __shfl_xor_sync(0xffffffffu, total, off);
+      if (lane == 0) {
+        sm.agg[s] = total;
+        if (tile > 0) desc_store(descs + tile, sm.epoch * 4 + 1, to_bits<T>(total));
+      }
+      __syncwarp();
+      if (lane == 0) mbar_arrive(&sm.summed[s]);
+    }
+  } else if (warp < kFirstCompute) {
+    // ---- lookback (alternate tiles) ----
+    for (int k = warp - 2;; k += kLookbackWarps) {
+      const int s = k % kStages;
+      const uint32_t par = (k / kStages) & 1;
+      if (!wait(sm, &sm.drawn[s], par, hdr)) break;
+      const unsigned int tile = sm.ticket[s];
+      if (tile == kEnd) break;
+      const unsigned long long AGG = sm.epoch * 4 + 1, INC = sm.epoch * 4 + 2;
+      const T excl =
+          (tile > 0) ? lookback_exclusive<T, kLookbackLanes>(descs, tile, AGG, INC, hdr) : init;
+      if (!wait(sm, &sm.summed[s], par, hdr)) break;
+      if (lane == 0) {
+        desc_store(descs + tile, INC, to_bits<T>(excl + sm.agg[s]));
+        sm.excl[s] = excl;
+      }
+      __syncwarp();
+      if (lane == 0) mbar_arrive(&sm.prefix[s]);
+    }
+  } else if (warp < kStoreWarp) {
+    // ---- compute ----
+    // The four warps decide together whether to go on: a warp whose wait
+    // gave up sets a flag before the next group barrier and every thread
+    // reads it after that barrier, so no thread is left at a later barrier.
+    // The two barriers of an iteration use separate flags: a failure in the
+    // next iteration can only be recorded after every thread has passed
+    // this iteration's reads of the flag it sets.
+    const int ct = tid - 32 * kFirstCompute, cw = ct >> 5;
+    const int rot = ct & (kPairs - 1);
+    volatile int* fail_loaded = &sm.fail_loaded;
+    volatile int* fail_prefix = &sm.fail_prefix;
+    for (int k = 0;; ++k) {
+      const int s = k % kStages;
+      const uint32_t par = (k / kStages) & 1;
+      const bool loaded = wait(sm, &sm.full[s], par, hdr);
+      const unsigned int tile = sm.ticket[s];
+      if (!loaded) *fail_loaded = 1;
+      V2* tv = reinterpret_cast<V2*>(sm.tile[s]) + ct * kPairs;
+      V2 v[kPairs];
+      T head = T(0), tail = T(0);  // pairs q < rot come first in index order
+      if (loaded && tile != kEnd) {
+#pragma unroll
+        for (int w = 0; w < kPairs; ++w) v[w] = tv[(w + rot) & (kPairs - 1)];
+#pragma unroll
+        for (int w = 0; w < kPairs; ++w) {
+          if (w >= kPairs - rot) {
+            head += v[w].x;
+            head += v[w].y;
+          } else {
+            tail += v[w].x;
+            tail += v[w].y;
+          }
+        }
+      }
+      const T rs = head + tail;
+      const T inc = warp_inclusive_scan(rs);
+      if (lane == 31) sm.warp_total[cw] = inc;
+      named_sync(1, 32 * kComputeWarps);
+      if (*fail_loaded || tile == kEnd) {
+        if (ct == 0 && !*fail_loaded) mbar_arrive(&sm.ready[s]);  // end marker for the store warp
+        break;
+      }
+      T woff = T(0);
+      for (int w = 0; w < cw; ++w) woff += sm.warp_total[w];
+      const bool have_prefix = wait(sm, &sm.prefix[s], par, hdr);
+      if (have_prefix) {
+        const T base = sm.excl[s] + (woff + (inc - rs));
+        T r = base + head;
+#pragma unroll
+        for (int w = 0; w < kPairs; ++w) {
+          if (w == kPairs - rot) r = base;
+          V2 o;
+          o.x = r;
+          r += v[w].x;
+          o.y = r;
+          r += v[w].y;
+          tv[(w + rot) & (kPairs - 1)] = o;
+        }
+        fence_proxy_async_smem();
+      } else {
+        *fail_prefix = 1;
+      }
+      named_sync(2, 32 * kComputeWarps);
+      if (*fail_prefix) break;
+      const int64_t first = static_cast<int64_t>(tile) * kTile;
+      if (first + kTile > n) {
+        // the ragged last tile: plain stores
+        for (int i = ct; first + i < n; i += 32 * kComputeWarps) y[first + i] = sm.tile[s][i];
+      }
+      if (ct == 0) mbar_arrive(&sm.ready[s]);
+    }
+  } else {
+    // ---- store: one bulk store per finished tile ----
+    for (int k = 0;; ++k) {
+      const int s = k % kStages;
+      if (!wait(sm, &sm.ready[s], (k / kStages) & 1, hdr)) break;
+      const unsigned int tile = sm.ticket[s];
+      if (tile == kEnd) break;
+      const int64_t first = static_cast<int64_t>(tile) * kTile;
+      if (lane == 0) {
+        if (first + kTile <= n) {
+          bulk_store(y + first, sm.tile[s], kTile * sizeof(T));
+          bulk_commit();
+          bulk_wait_read<0>();
+        }
+        mbar_arrive(&sm.empty[s]);
+      }
+      __syncwarp();
+    }
+    if (lane == 0) bulk_wait_all();
+  }
+
+  // After an abort, bulk copies may still be landing in shared memory: wait
+  // (bounded) for the last phase started in each stage before the CTA exits.
+  __syncthreads();
+  if (tid == 0 && sm.abort) {
+    for (int s = 0; s < kStages; ++s)
+      if (sm.phases[s] > 0u) mbar_wait_for(&sm.full[s], (sm.phases[s] - 1u) & 1u, kWaitNs);
+  }
+}
+
+}  // namespace pipe
 
 // The workspace is sized for the smallest tile, so it serves every tile size.
 int64_t scan_tiles_max(int64_t n) { return ceil_div(n > 0 ? n : 1, kScanTileMin); }
@@ -194,12 +503,32 @@ int launch_scan_it(const T* x, T* y, int64_t n, T init, char* w, cudaStream_t st
 }
 
 template <typename T>
+int launch_scan_pipelined(const T* x, T* y, int64_t n, T init, char* w, cudaStream_t st) {
+  constexpr size_t kSmem = pipe::smem_bytes<T>();
+  const cudaError_t attr = cudaFuncSetAttribute(
+      pipe::scan_pipelined<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+      static_cast<int>(kSmem));
+  if (attr != cudaSuccess) {
+    set_error("scan: shared memory attribute: %s", cudaGetErrorString(attr));
+    return B200_ERR_LAUNCH;
+  }
+  const int64_t tiles = ceil_div(n, pipe::kTile);
+  const int grid = static_cast<int>(std::min<int64_t>(tiles, device_info().sm_count));
+  pipe::scan_pipelined<T><<<grid, pipe::kThreads, kSmem, st>>>(
+      x, y, n, init, static_cast<unsigned int>(tiles), reinterpret_cast<ScanHeader*>(w),
+      reinterpret_cast<TileDesc*>(w + 256));
+  return B200_OK;
+}
+
+template <typename T>
 int launch_scan(const char* name, const T* x, T* y, int64_t n, T init, void* ws,
                 size_t ws_bytes, const b200_tune* tune, cudaStream_t st) {
   if (n < 0 || (n > 0 && (!x || !y))) return invalid("%s: bad args", name);
   if (n == 0) return B200_OK;
   const int64_t slots = scan_tiles_max(n);
   if (slots > 0x7fffffffLL) return invalid("%s: n too large", name);
+  const int algo = tune ? tune->algo : 0;
+  if (algo != 0 && algo != 1) return invalid("%s: algo %d (0 or 1)", name, algo);
   if (tune && tune->block_size && tune->block_size != kScanBlock)
     return invalid("%s: block size %d (only %d)", name, tune->block_size, kScanBlock);
   const int items = (tune && tune->items) ? tune->items : kScanItemsDefault;
@@ -212,10 +541,14 @@ int launch_scan(const char* name, const T* x, T* y, int64_t n, T init, void* ws,
   }
   char* w = static_cast<char*>(ws);
   const bool vec = aligned16(x) && aligned16(y) && !(tune && tune->vec == 1);
-  const int rc = (items == 16) ? (vec ? launch_scan_it<T, 16, true>(x, y, n, init, w, st)
-                                      : launch_scan_it<T, 16, false>(x, y, n, init, w, st))
-                               : (vec ? launch_scan_it<T, 32, true>(x, y, n, init, w, st)
-                                      : launch_scan_it<T, 32, false>(x, y, n, init, w, st));
+  int rc;
+  if (algo == 0 && vec)
+    rc = launch_scan_pipelined<T>(x, y, n, init, w, st);
+  else
+    rc = (items == 16) ? (vec ? launch_scan_it<T, 16, true>(x, y, n, init, w, st)
+                              : launch_scan_it<T, 16, false>(x, y, n, init, w, st))
+                       : (vec ? launch_scan_it<T, 32, true>(x, y, n, init, w, st)
+                              : launch_scan_it<T, 32, false>(x, y, n, init, w, st));
   if (rc != B200_OK) return rc;
   return after_launch(name);
 }

@@ -5,9 +5,11 @@
 // (AGG) as soon as it has reduced its own items, and its inclusive prefix
 // (INC) once it knows its exclusive prefix; a successor sums predecessors'
 // values back to the nearest INC.  Statuses carry the launch epoch, so the
-// workspace is never re-zeroed between calls: the last CTA of a launch resets
-// the counters and advances the epoch.  Every wait is bounded; one that gives
-// up sets the header's error word and the call's results are invalid.
+// workspace is never re-zeroed between calls: the CTA that draws a launch's
+// last ticket resets the ticket count and advances the epoch.  A status
+// counts only when its epoch equals the launch's (so a wrapped epoch cannot
+// make an old status look new).  Every wait is bounded; one that gives up
+// sets the header's error word and the call's results are invalid.
 #pragma once
 
 #include <cstdint>
@@ -19,9 +21,10 @@ constexpr int kLookbackPerLane = 4;   // a lookback round covers 128 predecessor
 constexpr long long kSpinLimit = 1LL << 22;
 
 struct ScanHeader {
-  unsigned long long epoch;
-  unsigned int tile_counter;
-  unsigned int done_counter;
+  // Low 32 bits: tickets taken in this launch; high 32 bits: the launch
+  // epoch.  One 64-bit atomic hands a CTA its tile and the epoch together.
+  unsigned long long ticket;
+  unsigned long long unused;
   unsigned int error;   // byte offset 16
   unsigned int pad[59];
 };
@@ -31,7 +34,8 @@ static_assert(sizeof(ScanHeader) == 256, "lookback header is 256 bytes");
 // as single 128-bit accesses (PTX .b128), so a reader that sees a status also
 // sees the value published with it; no other data is ordered by a
 // descriptor, so relaxed accesses suffice and a lane's loads of several
-// descriptors are in flight together.  status = epoch * 4 + (AGG 1 | INC 2).
+// descriptors are in flight together.  status = epoch * 4 + (AGG 1 | INC 2),
+// epoch < 2^32.
 struct alignas(16) TileDesc {
   unsigned long long status;
   unsigned long long value;  // the T's bits
@@ -58,6 +62,12 @@ __device__ __forceinline__ void desc_store(TileDesc* d, unsigned long long statu
       : "memory");
 }
 
+// A descriptor status belongs to this launch (AGG or INC of its epoch).
+__device__ __forceinline__ bool published(unsigned long long st, unsigned long long AGG,
+                                          unsigned long long INC) {
+  return st == AGG || st == INC;
+}
+
 template <typename T>
 __device__ __forceinline__ unsigned long long to_bits(T v) {
   unsigned long long b;
@@ -82,64 +92,35 @@ __device__ __forceinline__ T warp_inclusive_scan(T v) {
   return v;
 }
 
-// Waits (bounded) until predecessor p has published at least its aggregate
-// for this launch; returns its status and value.  A wait that gives up
-// records the error and reports an inclusive prefix so the lookback ends.
-__device__ __forceinline__ unsigned long long wait_desc(const TileDesc* descs, int64_t p,
-                                                        unsigned long long AGG,
-                                                        unsigned long long INC,
-                                                        ScanHeader* hdr,
-                                                        unsigned long long& value) {
-  unsigned long long st;
-  desc_load(descs + p, st, value);
-  long long spins = 0;
-  while (st < AGG) {
-    if (++spins > kSpinLimit) {
-      atomicExch(&hdr->error, 1u);
-      value = 0ull;
-      return INC;
-    }
-    if (spins > 64) __nanosleep(64);
-    desc_load(descs + p, st, value);
-  }
-  return st;
-}
-
-
-// Thread 0 takes the CTA's tile id and reads the launch epoch.
+// Thread 0 takes the CTA's tile id and the launch epoch with one atomic.
+// The CTA that draws the launch's last ticket (gridDim.x - 1) knows every
+// other CTA has drawn its own, so it clears the ticket count and advances the
+// epoch in the same word right away; the next launch on the stream starts
+// only after this one has finished.  No CTA has to wait for the others to
+// finish, and no per-call reset of the workspace is needed.
 __device__ __forceinline__ void take_tile(ScanHeader* hdr, unsigned int* s_tile,
                                           unsigned long long* s_epoch) {
   if (threadIdx.x == 0) {
-    *s_epoch = *reinterpret_cast<volatile unsigned long long*>(&hdr->epoch);
-    *s_tile = atomicAdd(&hdr->tile_counter, 1u);
+    const unsigned long long t = atomicAdd(&hdr->ticket, 1ull);
+    const unsigned int tile = static_cast<unsigned int>(t);
+    if (tile == gridDim.x - 1u)
+      atomicAdd(&hdr->ticket, (1ull << 32) - static_cast<unsigned long long>(gridDim.x));
+    *s_tile = tile;
+    *s_epoch = t >> 32;
   }
   __syncthreads();
-}
-
-// Called by every thread of the CTA after its last use of the tile: the last
-// CTA of the launch resets the counters and advances the epoch.
-__device__ __forceinline__ void finish_launch(ScanHeader* hdr, unsigned long long epoch,
-                                              bool* s_last) {
-  if (threadIdx.x == 0) {
-    __threadfence();
-    const unsigned int prev = atomicAdd(&hdr->done_counter, 1u);
-    *s_last = (prev == gridDim.x - 1);
-  }
-  __syncthreads();
-  if (*s_last && threadIdx.x == 0) {
-    hdr->tile_counter = 0u;
-    hdr->done_counter = 0u;
-    __threadfence();
-    *reinterpret_cast<volatile unsigned long long*>(&hdr->epoch) = epoch + 1;
-  }
 }
 
 // Run by one full warp for tile > 0: the sum of the predecessors' values back
-// to (and including) the nearest inclusive prefix.  A round examines
-// 32 * kLookbackPerLane predecessors, nearest first (slot w = j * 32 + lane is
-// predecessor p_hi - w); every lane issues its loads before waiting on any,
-// and values are summed in a fixed order (slots per lane, then a lane tree).
-template <typename T>
+// to (and including) the nearest inclusive prefix.  A round loads the
+// descriptors of 32 * PER_LANE predecessors, nearest first (slot w = j * 32 +
+// lane is predecessor p_hi - w), all at once.  Only slots nearer than the
+// nearest inclusive prefix matter; those still unpublished are re-read
+// together (one memory round trip per retry, however many are late) until
+// every one has at least its aggregate.  Values are summed in a fixed order
+// (slots per lane, then a lane tree).  A slot that stays unpublished past the
+// spin limit records the error and counts as an inclusive prefix of 0.
+template <typename T, int PER_LANE = kLookbackPerLane>
 __device__ T lookback_exclusive(const TileDesc* descs, unsigned int tile,
                                 unsigned long long AGG, unsigned long long INC,
                                 ScanHeader* hdr) {
@@ -147,36 +128,51 @@ __device__ T lookback_exclusive(const TileDesc* descs, unsigned int tile,
   T acc = T(0);
   int64_t p_hi = static_cast<int64_t>(tile) - 1;  // nearest unexamined predecessor
   for (;;) {
-    unsigned long long f[kLookbackPerLane], bits[kLookbackPerLane];
-    T v[kLookbackPerLane];
+    unsigned long long f[PER_LANE], bits[PER_LANE];
 #pragma unroll
-    for (int j = 0; j < kLookbackPerLane; ++j) {  // all loads first
+    for (int j = 0; j < PER_LANE; ++j) {
       const int64_t p = p_hi - (j * 32 + lane);
       f[j] = INC;                                  // p < 0: end of the lookback
       bits[j] = 0ull;
       if (p >= 0) desc_load(descs + p, f[j], bits[j]);
     }
+    int stop;
+    for (long long spins = 0;; ++spins) {
+      stop = 32 * PER_LANE;  // nearest slot holding an inclusive prefix
 #pragma unroll
-    for (int j = 0; j < kLookbackPerLane; ++j) {  // then wait for the late ones
-      const int64_t p = p_hi - (j * 32 + lane);
-      if (p >= 0 && f[j] < AGG) f[j] = wait_desc(descs, p, AGG, INC, hdr, bits[j]);
-      v[j] = from_bits<T>(bits[j]);
-    }
-    int stop = 32 * kLookbackPerLane;  // nearest slot holding an inclusive prefix
+      for (int j = PER_LANE - 1; j >= 0; --j) {
+        const unsigned int m = __ballot_sync(0xffffffffu, f[j] == INC);
+        if (m) stop = j * 32 + __ffs(m) - 1;
+      }
+      bool pending = false;
 #pragma unroll
-    for (int j = kLookbackPerLane - 1; j >= 0; --j) {
-      const unsigned int m = __ballot_sync(0xffffffffu, f[j] == INC);
-      if (m) stop = j * 32 + __ffs(m) - 1;
+      for (int j = 0; j < PER_LANE; ++j)
+        pending |= (j * 32 + lane < stop) && !published(f[j], AGG, INC);
+      if (!__any_sync(0xffffffffu, pending)) break;
+      const bool give_up = spins > kSpinLimit;
+      if (give_up && lane == 0) atomicExch(&hdr->error, 1u);
+      if (spins > 16) __nanosleep(64);
+#pragma unroll
+      for (int j = 0; j < PER_LANE; ++j) {
+        if ((j * 32 + lane < stop) && !published(f[j], AGG, INC)) {
+          if (give_up) {
+            f[j] = INC;
+            bits[j] = 0ull;
+          } else {
+            desc_load(descs + (p_hi - (j * 32 + lane)), f[j], bits[j]);
+          }
+        }
+      }
     }
     T val = T(0);
 #pragma unroll
-    for (int j = 0; j < kLookbackPerLane; ++j)
-      if (j * 32 + lane <= stop) val += v[j];
+    for (int j = 0; j < PER_LANE; ++j)
+      if (j * 32 + lane <= stop) val += from_bits<T>(bits[j]);
 #pragma unroll
     for (int off = 16; off > 0; off >>= 1) val += __shfl_down_sync(0xffffffffu, val, off);
     acc += __shfl_sync(0xffffffffu, val, 0);
-    if (stop < 32 * kLookbackPerLane) return acc;
-    p_hi -= 32 * kLookbackPerLane;
+    if (stop < 32 * PER_LANE) return acc;
+    p_hi -= 32 * PER_LANE;
   }
 }
 

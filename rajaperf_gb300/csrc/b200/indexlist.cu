@@ -37,7 +37,6 @@ indexlist_kernel(const double* __restrict__ x, int32_t* __restrict__ list, int64
   __shared__ long long s_excl;
   __shared__ unsigned int s_tile_id;
   __shared__ unsigned long long s_epoch;
-  __shared__ bool s_last;
 
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   take_tile(hdr, &s_tile_id, &s_epoch);
@@ -114,8 +113,6 @@ indexlist_kernel(const double* __restrict__ x, int32_t* __restrict__ list, int64
   }
   // the tile holding item n-1 knows the total
   if (tid == 0 && static_cast<int64_t>(tile + 1) * kTile >= n) *len = s_excl + s_agg;
-  __syncthreads();
-  finish_launch(hdr, epoch, &s_last);
 }
 
 int64_t tiles_of(int64_t n) { return ceil_div(n > 0 ? n : 1, kTile); }

@@ -73,9 +73,10 @@ double timeGraph(const KernelBase::RepBody& body, int64_t reps) {
 std::vector<b200_tune> autotuneCandidates(KernelID kid) {
   std::vector<b200_tune> out(1, b200_tune{});  // library default
   const Family f = familyOf(kid);
-  if (f == Family::Scan) {
+  if (f == Family::Scan) {  // default: pipelined; algo 1: one tile per CTA
     for (int items : {16, 32}) {
       b200_tune t{};
+      t.algo = 1;
       t.items = items;
       out.push_back(t);
     }

@@ -158,11 +158,17 @@ def test_fdtd_2d(nx, ny, ts):
         close(gu.host(g), w)
 
 
-@pytest.mark.parametrize("n", [1, 2, 4095, 4096, 4097, 8191, 8193, 100003, 1 << 21])
-@pytest.mark.parametrize("items", [0, 16, 32])
-def test_scan_f64_and_i64(n, items):
-    """Default (8192-item) and 4096-item tiles; the calls alternate tile
-    sizes on one workspace, which the epoch-tagged flags must tolerate."""
+SCAN_TUNES = {"pipelined": dict(), "tile4096": dict(algo=1, items=16),
+              "tile8192": dict(algo=1, items=32)}
+
+
+@pytest.mark.parametrize("n", [1, 2, 4095, 4096, 4097, 8191, 8193, 100003, 1 << 21,
+                               152 * 4096 * 3 + 1000])
+@pytest.mark.parametrize("kind", sorted(SCAN_TUNES))
+def test_scan_f64_and_i64(n, kind):
+    """The pipelined persistent kernel and the one-tile-per-CTA kernel with
+    both tile sizes; the calls alternate kernels on one workspace, which the
+    epoch-tagged statuses and the ticket reset must tolerate."""
     rng = np.random.default_rng(n)
     x = rng.uniform(0.0, 1.0, n)
     xi = rng.integers(0, 100, n).astype(np.int64)
@@ -172,8 +178,8 @@ def test_scan_f64_and_i64(n, items):
     dy = torch.zeros(n, dtype=torch.float64, device="cuda")
     dyi = torch.zeros(n, dtype=torch.int64, device="cuda")
     dx, dxi = dev(x), dev(xi)
-    t = rp.Tune(items=items)
-    other = rp.Tune(items=16 if items != 16 else 32)
+    t = rp.Tune(**SCAN_TUNES[kind])
+    other = rp.Tune(algo=1, items=16) if kind == "pipelined" else rp.Tune()
     for rep in range(3):  # the workspace is reused across calls
         rp.check(lib().b200_algorithm_scan(dx.data_ptr(), dy.data_ptr(), n, 0.25,
                                            w.data_ptr(), wsb, ctypes.byref(other), gu.stream()))
@@ -190,6 +196,7 @@ def test_scan_f64_and_i64(n, items):
         assert np.all(np.abs(got - want) <= (n + 64) * gu.U * (np.abs(want) + 0.25))
     hdr = gu.host(w)[:24].view(np.uint32)
     assert hdr[4] == 0, "lookback wait gave up"
+    assert hdr[0] == 0, "ticket count not reset"
 
 
 @pytest.mark.parametrize("n", [8192 * 3 + 5, 1 << 20])

@@ -231,16 +231,16 @@ def test_reductions_and_scan_at_2e27():
     loc = A.z(1, torch.int64)
     rp.check(L.b200_lcals_first_min(P(a), n, 0.5, 0, P(loc), None, P(ws), wb, None, s))
     assert int(gu.host(loc)[0]) == n // 3
-    # int64 scan, exact, with the default and the 4096-item tiles
+    # int64 scan, exact: the pipelined kernel and the one-tile-per-CTA kernel
     x = torch.empty(n, dtype=torch.int64, device="cuda")
     rp.check(L.b200_init_uniform_i64(P(x), n, 28, 0, 0, 100, None))
     y = A.z(n, torch.int64)
     swb = L.b200_scan_workspace_bytes(n)
     sws = A.z(swb, torch.uint8)
     want = torch.cumsum(x, 0) - x
-    for items in (0, 16):
+    for tune in (dict(), dict(algo=1, items=16), dict(algo=1, items=32)):
         y.zero_()
-        t = rp.Tune(items=items)
+        t = rp.Tune(**tune)
         rp.check(L.b200_algorithm_scan_i64(P(x), P(y), n, 0, P(sws), swb, ctypes.byref(t), s))
         assert bool(torch.equal(y, want))
     assert int(gu.host(sws[16:20]).view(np.uint32)[0]) == 0
