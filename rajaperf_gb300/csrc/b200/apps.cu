@@ -6,6 +6,7 @@
 // arithmetic is the suite's, and arrays that only carry values between
 // bodies stay in registers.
 #include "b200_internal.cuh"
+#include "b200_f64emu.cuh"
 #include "b200_map.cuh"
 
 using namespace b200;
@@ -157,6 +158,13 @@ struct Vol3D {
 
 // apps/DEL_DOT_VEC_2D.hpp:65-90 with corners from NDSET2D (AppsData.hpp:
 // v4=v, v1=v4+1, v2=v1+jp, v3=v4+jp); zone index through real_zones.
+// The kernel is bound by the FP64 pipe (59 FP64 instructions per zone).
+// With the suite's half = 0.5 (HALF_POW2) the eight half * (...) products
+// are exact exponent decrements on the integer pipe (f64emu::mul_pow2_fast),
+// which leaves the FP64 pipe 51 instructions per zone and every result bit
+// unchanged; a warp with a zero, subnormal or non-finite half-difference
+// recomputes its zones natively.
+template <bool HALF_POW2>
 struct DelDotVec2D {
   const double* __restrict__ x;
   const double* __restrict__ y;
@@ -166,6 +174,37 @@ struct DelDotVec2D {
   const int64_t* __restrict__ real_zones;
   int64_t jp;
   double ptiny, half;
+  __device__ __forceinline__ double body(double x1, double x2, double x3, double x4,
+                                        double y1, double y2, double y3, double y4,
+                                        double fx1, double fx2, double fx3, double fx4,
+                                        double fy1, double fy2, double fy3, double fy4,
+                                        bool fast, bool& slow) const {
+    double xi, xj, yi, yj, fxi, fxj, fyi, fyj;
+    if (fast) {
+      xi = f64emu::mul_pow2_fast<-1>(x1 + x2 - x3 - x4, slow);
+      xj = f64emu::mul_pow2_fast<-1>(x2 + x3 - x4 - x1, slow);
+      yi = f64emu::mul_pow2_fast<-1>(y1 + y2 - y3 - y4, slow);
+      yj = f64emu::mul_pow2_fast<-1>(y2 + y3 - y4 - y1, slow);
+      fxi = f64emu::mul_pow2_fast<-1>(fx1 + fx2 - fx3 - fx4, slow);
+      fxj = f64emu::mul_pow2_fast<-1>(fx2 + fx3 - fx4 - fx1, slow);
+      fyi = f64emu::mul_pow2_fast<-1>(fy1 + fy2 - fy3 - fy4, slow);
+      fyj = f64emu::mul_pow2_fast<-1>(fy2 + fy3 - fy4 - fy1, slow);
+    } else {
+      xi = half * (x1 + x2 - x3 - x4);
+      xj = half * (x2 + x3 - x4 - x1);
+      yi = half * (y1 + y2 - y3 - y4);
+      yj = half * (y2 + y3 - y4 - y1);
+      fxi = half * (fx1 + fx2 - fx3 - fx4);
+      fxj = half * (fx2 + fx3 - fx4 - fx1);
+      fyi = half * (fy1 + fy2 - fy3 - fy4);
+      fyj = half * (fy2 + fy3 - fy4 - fy1);
+    }
+    const double rarea = 1.0 / (xi * yj - xj * yi + ptiny);
+    const double dfxdx = rarea * (fxi * yj - fxj * yi);
+    const double dfydy = rarea * (fyj * xi - fyi * xj);
+    const double affine = (fy1 + fy2 + fy3 + fy4) / (y1 + y2 + y3 + y4);
+    return dfxdx + dfydy + affine;
+  }
   __device__ void operator()(int64_t ii) const {
     const int64_t i = ld(real_zones + ii);
     const int64_t c1 = i + 1, c2 = i + 1 + jp, c3 = i + jp, c4 = i;
@@ -175,19 +214,14 @@ struct DelDotVec2D {
                  fx4 = ld(xdot + c4);
     const double fy1 = ld(ydot + c1), fy2 = ld(ydot + c2), fy3 = ld(ydot + c3),
                  fy4 = ld(ydot + c4);
-    double xi = half * (x1 + x2 - x3 - x4);
-    double xj = half * (x2 + x3 - x4 - x1);
-    double yi = half * (y1 + y2 - y3 - y4);
-    double yj = half * (y2 + y3 - y4 - y1);
-    double fxi = half * (fx1 + fx2 - fx3 - fx4);
-    double fxj = half * (fx2 + fx3 - fx4 - fx1);
-    double fyi = half * (fy1 + fy2 - fy3 - fy4);
-    double fyj = half * (fy2 + fy3 - fy4 - fy1);
-    double rarea = 1.0 / (xi * yj - xj * yi + ptiny);
-    double dfxdx = rarea * (fxi * yj - fxj * yi);
-    double dfydy = rarea * (fyj * xi - fyi * xj);
-    double affine = (fy1 + fy2 + fy3 + fy4) / (y1 + y2 + y3 + y4);
-    div[i] = dfxdx + dfydy + affine;
+    bool slow = false;
+    double r = body(x1, x2, x3, x4, y1, y2, y3, y4, fx1, fx2, fx3, fx4, fy1, fy2, fy3, fy4,
+                    HALF_POW2, slow);
+    if (HALF_POW2 && __any_sync(__activemask(), slow))
+      if (slow)
+        r = body(x1, x2, x3, x4, y1, y2, y3, y4, fx1, fx2, fx3, fx4, fy1, fy2, fy3, fy4,
+                 false, slow);
+    div[i] = r;
   }
 };
 
@@ -243,8 +277,12 @@ int b200_apps_del_dot_vec_2d(const double* x, const double* y, const double* xdo
   if (n_real_zones < 0 || jp < 0 ||
       (n_real_zones > 0 && (!x || !y || !xdot || !ydot || !div || !real_zones)))
     return invalid("b200_apps_del_dot_vec_2d: bad args");
+  if (half == 0.5)
+    return launch_map1d("b200_apps_del_dot_vec_2d",
+                        DelDotVec2D<true>{x, y, xdot, ydot, div, real_zones, jp, ptiny, half},
+                        n_real_zones, tune, as_stream(stream));
   return launch_map1d("b200_apps_del_dot_vec_2d",
-                      DelDotVec2D{x, y, xdot, ydot, div, real_zones, jp, ptiny, half},
+                      DelDotVec2D<false>{x, y, xdot, ydot, div, real_zones, jp, ptiny, half},
                       n_real_zones, tune, as_stream(stream));
 }
 

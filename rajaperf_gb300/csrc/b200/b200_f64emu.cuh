@@ -125,5 +125,21 @@ __device__ __forceinline__ double scale2(double x, int k) {
   return from_bits(X + (static_cast<uint64_t>(static_cast<int64_t>(k)) << 52));
 }
 
+// x * 2^K for a constant K as an exponent move on the integer pipe.  Exact
+// and equal to the FP64 pipe's x * 2^K while x and the result are normal
+// numbers; `slow` is set for every other input (zeros, subnormals,
+// infinities, NaNs, results leaving the normal range), for which the caller
+// recomputes with the FP64 pipe.
+template <int K>
+__device__ __forceinline__ double mul_pow2_fast(double x, bool& slow) {
+  static_assert(K > -1000 && K < 1000 && K != 0, "small nonzero K");
+  constexpr unsigned kLo = (K < 0) ? 1u - K : 1u;        // smallest exponent kept normal
+  constexpr unsigned kHi = (K > 0) ? 2046u - K : 2046u;  // largest
+  const int hi = __double2hiint(x);
+  const unsigned e = (static_cast<unsigned>(hi) >> 20) & 0x7ffu;
+  slow |= (e - kLo) > (kHi - kLo);
+  return __hiloint2double(hi + K * (1 << 20), __double2loint(x));
+}
+
 }  // namespace f64emu
 }  // namespace b200

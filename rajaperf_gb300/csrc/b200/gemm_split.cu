@@ -35,6 +35,7 @@
 // Every wait of the tcgen05 engine is bounded (1 s); one that gives up sets
 // the error word at the start of the workspace and the CTA winds down.
 #include "b200_internal.cuh"
+#include "b200_async.cuh"
 
 #include <cuda.h>
 #include <cudaTypedefs.h>
@@ -308,35 +309,6 @@ constexpr uint32_t kIdesc = (1u << 4) | (1u << 7) | (1u << 10) |
                             (static_cast<uint32_t>(BM >> 4) << 24);
 static_assert(kSmemBytes <= 232448, "shared memory budget");
 
-__device__ __forceinline__ uint32_t smem_u32(const void* p) {
-  return static_cast<uint32_t>(__cvta_generic_to_shared(p));
-}
-__device__ __forceinline__ uint64_t globaltimer() {
-  uint64_t t;
-  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
-  return t;
-}
-__device__ __forceinline__ void mbar_init(uint64_t* b, uint32_t count) {
-  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(b)), "r"(count) : "memory");
-}
-__device__ __forceinline__ void mbar_arrive(uint64_t* b) {
-  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(b)) : "memory");
-}
-__device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t* b, uint32_t tx) {
-  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(b)), "r"(tx)
-               : "memory");
-}
-__device__ __forceinline__ bool mbar_try_wait(uint64_t* b, uint32_t parity) {
-  uint32_t ok;
-  asm volatile(
-      "{\n\t.reg .pred p;\n\t"
-      "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
-      "selp.u32 %0, 1, 0, p;\n\t}"
-      : "=r"(ok)
-      : "r"(smem_u32(b)), "r"(parity)
-      : "memory");
-  return ok != 0u;
-}
 // Waits for the phase of parity `parity` to complete.  Gives up after 1 s
 // (setting the CTA's abort flag) or when another role has aborted.
 __device__ bool mbar_wait(uint64_t* b, uint32_t parity, volatile int* abort_flag) {
@@ -474,8 +446,7 @@ ozaki_tc_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__
     }
     mbar_init(mma_done, 1);
     *abort_flag = 0;
-    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    mbar_init_fence();
   }
   if (warp == 1) {
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
