@@ -10,7 +10,8 @@ of the suite).  One "step" runs every kernel of the workload once.
                   [--workload bandwidth_stencil|stream]
 
 * value: kernels timed with CUDA events on the launching stream, inputs
-  resident in HBM, L2 flushed (a 256 MiB write) before every kernel.
+  resident in HBM, L2 flushed before every kernel (a 256 MiB write, then a
+  256 MiB read of another buffer so no dirty flush lines remain).
 * e2e: the same metric through the C ABI with host buffers: each step copies
   the kernel's inputs from pinned host memory, runs it and reads the
   result back, all inside the timed region.
@@ -794,12 +795,22 @@ def run_gpu(args, rank, world):
     cases = build_cases(torch, rp, args.workload, args.seed + rank, args.kernels)
     stream = torch.cuda.current_stream()
     s = stream.cuda_stream
-    flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device="cuda")
+    # L2 flush before every kernel: a write of a 256 MiB buffer evicts the
+    # kernel's inputs and outputs, then a read of a second 256 MiB buffer
+    # evicts the flush's own dirty lines, so that their write-back to HBM is
+    # not charged to the timed kernel (at 2^24 elements it would add up to
+    # ~128 MB of writes to a kernel that moves 134-268 MB).
+    flush_w = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device="cuda")
+    flush_r = torch.zeros(L2_FLUSH_BYTES // 4, dtype=torch.float32, device="cuda")
     fp64 = measure_fp64_peak(torch, rp, stream)
+
+    def l2_flush():
+        flush_w.zero_()
+        flush_r.sum()
 
     def one_step(timed_events=None):
         for i, c in enumerate(cases):
-            flush.zero_()
+            l2_flush()
             if timed_events is not None:
                 timed_events[i][0].record(stream)
             rp.check(c.run(s), c.name)
@@ -1124,7 +1135,8 @@ def main():
     desc = WORKLOADS[args.workload]["description"]
     config = {"workload": args.workload, "description": desc,
               "kernels": [k for k, _ in workload_kernels(args.workload, args.kernels)],
-              "l2": "flushed (256 MiB write) before every kernel",
+              "l2": "flushed before every kernel: 256 MiB write, then 256 MiB read of a "
+                    "second buffer (no dirty flush lines left to write back)",
               "init": f"uniform [0.5,1.5) seed {args.seed}"}
     metric = "geomean % of measured HBM copy peak over kernels (suite Bytes/rep)"
 

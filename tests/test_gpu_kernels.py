@@ -347,3 +347,32 @@ def test_heat_mixed_pipes_bit_identical(N, ts, shape):
                                           ctypes.byref(t), gu.stream()))
     assert np.array_equal(gu.host(dA1), gu.host(dA2))
     assert np.array_equal(gu.host(dB1), gu.host(dB2))
+
+
+@pytest.mark.parametrize("case", ["plateau", "subnormal", "mixed"])
+def test_heat_exponent_shift_special_values(case):
+    """The default HEAT_3D kernel scales by 0.125 with an integer exponent move
+    and rewrites a thread's points with FP64 products when a term is zero,
+    subnormal or non-finite; its results must equal the all-FP64-pipe
+    kernel's (algo 1: no emulated warps) bit for bit on such data."""
+    N, ts = 34, 2
+    rng = np.random.default_rng(7)
+    A = np.full(N ** 3, 1.0)
+    B = np.full(N ** 3, 1.0)
+    if case == "plateau":          # exactly zero Laplacian terms almost everywhere
+        A[rng.integers(0, N ** 3, 40)] = 1.5
+    elif case == "subnormal":      # terms and results below the normal range
+        A = rng.uniform(0.5, 1.5, N ** 3) * 1e-308
+        B = rng.uniform(0.5, 1.5, N ** 3) * 1e-308
+    else:
+        A = rng.uniform(0.5, 1.5, N ** 3)
+        A[: N ** 3 // 2] = 0.75
+        A[rng.integers(0, N ** 3, 100)] = 4e-310
+    dA1, dB1, dA2, dB2 = dev(A), dev(B), dev(A), dev(B)
+    rp.check(lib().b200_polybench_heat_3d(dA1.data_ptr(), dB1.data_ptr(), N, ts, None,
+                                          gu.stream()))
+    t = rp.Tune(algo=1)
+    rp.check(lib().b200_polybench_heat_3d(dA2.data_ptr(), dB2.data_ptr(), N, ts,
+                                          ctypes.byref(t), gu.stream()))
+    assert np.array_equal(gu.host(dA1).view(np.int64), gu.host(dA2).view(np.int64))
+    assert np.array_equal(gu.host(dB1).view(np.int64), gu.host(dB2).view(np.int64))
