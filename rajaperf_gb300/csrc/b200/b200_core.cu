@@ -367,11 +367,16 @@ __global__ void f64emu_check_kernel(int64_t n, uint64_t seed, int op,
       bool slow = false;
       got = b200::f64emu::mul_pow2_fast<-1>(a, slow);
       if (slow) got = __dmul_rn(a, 0.5);
-    } else {
+    } else if (op == 4) {
       want = __dmul_rn(a, 0.125);
       bool slow = false;
       got = b200::f64emu::mul_pow2_fast<-3>(a, slow);
       if (slow) got = __dmul_rn(a, 0.125);
+    } else {
+      want = __dmul_rn(a, 2.0);
+      bool slow = false;
+      got = b200::f64emu::mul_pow2_fast<1>(a, slow);
+      if (slow) got = __dmul_rn(a, 2.0);
     }
     const bool same = (__double_as_longlong(want) == __double_as_longlong(got)) ||
                       (isnan(want) && isnan(got));
@@ -384,7 +389,7 @@ __global__ void f64emu_check_kernel(int64_t n, uint64_t seed, int op,
 
 extern "C" int b200_f64emu_selftest(int64_t n, uint64_t seed, int32_t op,
                                     unsigned long long* mismatches, b200_stream_t stream) {
-  if (n < 0 || !mismatches || op < 0 || op > 4) return invalid("b200_f64emu_selftest: bad args");
+  if (n < 0 || !mismatches || op < 0 || op > 5) return invalid("b200_f64emu_selftest: bad args");
   const int blocks = device_info().sm_count * 8;
   f64emu_check_kernel<<<blocks, 256, 0, as_stream(stream)>>>(n, seed, op, mismatches);
   return after_launch("b200_f64emu_selftest");

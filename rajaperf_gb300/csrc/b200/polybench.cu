@@ -43,17 +43,18 @@ heat3d_step(const double* __restrict__ S, double* __restrict__ D, int64_t N) {
   const int64_t j = 1 + static_cast<int64_t>(blockIdx.y) * BY + threadIdx.y;
   if (k >= N - 1 || j >= N - 1) return;
   const int64_t NN = N * N;
-  // 0.125 * v is exact: an exponent decrement on the integer pipe, so the
-  // FP64 pipe keeps only the adds (and the contracted 2.0 * a products).  A
-  // thread that met a zero, subnormal or non-finite term rewrites its points
-  // with the FP64 products after the loop (the same results, bit for bit).
+  // 2.0 * a and 0.125 * v are exact: exponent moves on the integer pipe, so
+  // the FP64 pipe keeps only the 9 adds of a point.  A thread that met a
+  // zero, subnormal or non-finite value rewrites its points with the FP64
+  // products after the loop (the same results, bit for bit).
   bool slow = false;
   for (int64_t i = 1 + blockIdx.z; i < N - 1; i += gridDim.z) {
     const int64_t c = k + N * (j + N * i);
     const double a = ld(S + c);
-    const double ti = f64emu::mul_pow2_fast<-3>(ld(S + c + NN) - 2.0 * a + ld(S + c - NN), slow);
-    const double tj = f64emu::mul_pow2_fast<-3>(ld(S + c + N) - 2.0 * a + ld(S + c - N), slow);
-    const double tk = f64emu::mul_pow2_fast<-3>(ld(S + c + 1) - 2.0 * a + ld(S + c - 1), slow);
+    const double a2 = f64emu::mul_pow2_fast<1>(a, slow);
+    const double ti = f64emu::mul_pow2_fast<-3>(ld(S + c + NN) - a2 + ld(S + c - NN), slow);
+    const double tj = f64emu::mul_pow2_fast<-3>(ld(S + c + N) - a2 + ld(S + c - N), slow);
+    const double tk = f64emu::mul_pow2_fast<-3>(ld(S + c + 1) - a2 + ld(S + c - 1), slow);
     D[c] = ti + tj + tk + a;
   }
   if (__any_sync(__activemask(), slow) && slow) {
