@@ -158,12 +158,13 @@ struct Vol3D {
 
 // apps/DEL_DOT_VEC_2D.hpp:65-90 with corners from NDSET2D (AppsData.hpp:
 // v4=v, v1=v4+1, v2=v1+jp, v3=v4+jp); zone index through real_zones.
-// The kernel is bound by the FP64 pipe (59 FP64 instructions per zone).
-// With the suite's half = 0.5 (HALF_POW2) the eight half * (...) products
-// are exact exponent decrements on the integer pipe (f64emu::mul_pow2_fast),
-// which leaves the FP64 pipe 51 instructions per zone and every result bit
-// unchanged; a warp with a zero, subnormal or non-finite half-difference
-// recomputes its zones natively.
+// The kernel is bound by the FP64 pipe (59 FP64 instructions per zone as
+// written).  With the suite's half = 0.5 (HALF_POW2) the eight half * (...)
+// products are exact exponent decrements on the integer pipe
+// (f64emu::mul_pow2_fast) and the two divisions run on the integer and FP32
+// pipes (f64emu::div_fast, correctly rounded), which leaves the FP64 pipe the
+// adds and multiplies and every result bit unchanged; a warp with a zero,
+// subnormal or non-finite operand recomputes its zones natively.
 template <bool HALF_POW2>
 struct DelDotVec2D {
   const double* __restrict__ x;
@@ -199,10 +200,12 @@ struct DelDotVec2D {
       fyi = half * (fy1 + fy2 - fy3 - fy4);
       fyj = half * (fy2 + fy3 - fy4 - fy1);
     }
-    const double rarea = 1.0 / (xi * yj - xj * yi + ptiny);
+    const double rarea = fast ? f64emu::div_fast(1.0, xi * yj - xj * yi + ptiny, slow)
+                              : 1.0 / (xi * yj - xj * yi + ptiny);
     const double dfxdx = rarea * (fxi * yj - fxj * yi);
     const double dfydy = rarea * (fyj * xi - fyi * xj);
-    const double affine = (fy1 + fy2 + fy3 + fy4) / (y1 + y2 + y3 + y4);
+    const double affine = fast ? f64emu::div_fast(fy1 + fy2 + fy3 + fy4, y1 + y2 + y3 + y4, slow)
+                               : (fy1 + fy2 + fy3 + fy4) / (y1 + y2 + y3 + y4);
     return dfxdx + dfydy + affine;
   }
   __device__ void operator()(int64_t ii) const {

@@ -356,6 +356,28 @@ __global__ void f64emu_check_kernel(int64_t n, uint64_t seed, int op,
         break;
       }
     }
+    if (op == 6) {  // division: three more families that stress rounding
+      const uint64_t bb = (rb & 0x800FFFFFFFFFFFFFULL) | ((((rb >> 52) & 0x7ffu) % 1500u + 270u) << 52);
+      switch ((i >> 3) % 4) {
+        case 1: {  // quotients next to a rounding midpoint: a = RN(b * (1 + odd * 2^-53))
+          const double mid = 1.0 + static_cast<double>((ra >> 12) | 1u) * 0x1.0p-53;
+          B = bb;
+          A = __double_as_longlong(__dmul_rn(__longlong_as_double(static_cast<long long>(B)), mid));
+          break;
+        }
+        case 2: {  // quotients next to 1: a within a few ulps of b
+          B = bb;
+          A = B + static_cast<uint64_t>(static_cast<int64_t>((ra >> 60) % 9u) - 4);
+          break;
+        }
+        case 3: {  // extreme divisor significands: 1.0 or 2 - ulp
+          B = (bb & 0xFFF0000000000000ULL) | (((rb >> 20) & 1u) ? 0x000FFFFFFFFFFFFFULL : 0u);
+          A = (ra & 0x800FFFFFFFFFFFFFULL) | ((((ra >> 52) & 0x7ffu) % 1500u + 270u) << 52);
+          break;
+        }
+        default: break;
+      }
+    }
     const double a = __longlong_as_double(static_cast<long long>(A));
     const double b = __longlong_as_double(static_cast<long long>(B));
     double want, got;
@@ -372,11 +394,16 @@ __global__ void f64emu_check_kernel(int64_t n, uint64_t seed, int op,
       bool slow = false;
       got = b200::f64emu::mul_pow2_fast<-3>(a, slow);
       if (slow) got = __dmul_rn(a, 0.125);
-    } else {
+    } else if (op == 5) {
       want = __dmul_rn(a, 2.0);
       bool slow = false;
       got = b200::f64emu::mul_pow2_fast<1>(a, slow);
       if (slow) got = __dmul_rn(a, 2.0);
+    } else {
+      want = __ddiv_rn(a, b);
+      bool slow = false;
+      got = b200::f64emu::div_fast(a, b, slow);
+      if (slow) got = __ddiv_rn(a, b);
     }
     const bool same = (__double_as_longlong(want) == __double_as_longlong(got)) ||
                       (isnan(want) && isnan(got));
@@ -389,7 +416,7 @@ __global__ void f64emu_check_kernel(int64_t n, uint64_t seed, int op,
 
 extern "C" int b200_f64emu_selftest(int64_t n, uint64_t seed, int32_t op,
                                     unsigned long long* mismatches, b200_stream_t stream) {
-  if (n < 0 || !mismatches || op < 0 || op > 5) return invalid("b200_f64emu_selftest: bad args");
+  if (n < 0 || !mismatches || op < 0 || op > 6) return invalid("b200_f64emu_selftest: bad args");
   const int blocks = device_info().sm_count * 8;
   f64emu_check_kernel<<<blocks, 256, 0, as_stream(stream)>>>(n, seed, op, mismatches);
   return after_launch("b200_f64emu_selftest");

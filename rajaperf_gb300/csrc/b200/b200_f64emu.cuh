@@ -141,5 +141,63 @@ __device__ __forceinline__ double mul_pow2_fast(double x, bool& slow) {
   return __hiloint2double(hi + K * (1 << 20), __double2loint(x));
 }
 
+// One round of the significand long division in div_fast: appends K quotient
+// bits to Q and leaves the exact remainder in R (0 <= R < mb on entry and on
+// exit).  The digit q = floor(R * 2^K / mb) is estimated in FP32 from the top
+// 32 bits of R and the FP32 reciprocal rf of mb's top 32 bits; with K <= 20
+// the estimate is within one of q (relative error of the FP32 product below
+// 2^-22), and the exact remainder R * 2^K - q * mb -- computed modulo 2^64,
+// exact because its true value lies in (-mb, 2 mb) -- corrects it.
+template <int K>
+__device__ __forceinline__ void div_round(uint64_t& Q, uint64_t& R, uint64_t mb, float rf) {
+  static_assert(K >= 1 && K <= 20, "digit size");
+  const float rfk = rf * static_cast<float>(1u << K);  // exact scaling
+  uint32_t q = __float2uint_rz(__uint2float_rn(static_cast<uint32_t>(R >> 21)) * rfk);
+  long long r = static_cast<long long>((R << K) - static_cast<uint64_t>(q) * mb);
+  if (r < 0) {
+    q -= 1u;
+    r += static_cast<long long>(mb);
+  } else if (r >= static_cast<long long>(mb)) {
+    q += 1u;
+    r -= static_cast<long long>(mb);
+  }
+  Q = (Q << K) | q;
+  R = static_cast<uint64_t>(r);
+}
+
+// a / b, correctly rounded (RN-even), without FP64 instructions: integer long
+// division of the significands (schoolbook division with estimated digits,
+// Knuth TAOCP vol. 2, 4.3.1, here with FP32 digit estimates).  For a, b
+// normal, M = ma or 2 ma with M / mb in [1, 2); Q = floor(M 2^53 / mb) has 54
+// bits (53 significand bits and a guard bit) and the final remainder R is
+// exact, so guard bit, sticky bit (R != 0) and the last bit decide
+// round-to-nearest-even exactly.  `slow` is set for zeros, subnormals,
+// infinities, NaNs and quotients outside the normal range; the caller then
+// divides natively.
+__device__ __forceinline__ double div_fast(double a, double b, bool& slow) {
+  const uint64_t A = bits(a), B = bits(b);
+  const uint32_t ea = static_cast<uint32_t>(A >> 52) & 0x7ffu;
+  const uint32_t eb = static_cast<uint32_t>(B >> 52) & 0x7ffu;
+  const uint64_t ma = (A & kFrac) | kHidden, mb = (B & kFrac) | kHidden;
+  const uint32_t sh = ma < mb ? 1u : 0u;
+  const uint64_t M = ma << sh;
+  int e = static_cast<int>(ea) - static_cast<int>(eb) + 1023 - static_cast<int>(sh);
+  const float rf = __frcp_rn(__uint2float_rn(static_cast<uint32_t>(mb >> 21)));
+  uint64_t Q = 1u, R = M - mb;  // the leading quotient bit is 1
+  div_round<20>(Q, R, mb, rf);
+  div_round<20>(Q, R, mb, rf);
+  div_round<13>(Q, R, mb, rf);
+  const uint64_t m0 = Q >> 1;  // [2^52, 2^53)
+  const bool up = (Q & 1u) && (R != 0u || (m0 & 1u));
+  uint64_t mant = m0 + (up ? 1u : 0u);
+  if (mant >> 53) {
+    mant >>= 1;
+    e += 1;
+  }
+  slow |= (ea - 1u >= 2046u) || (eb - 1u >= 2046u) || e <= 0 || e >= 2047;
+  return from_bits(((A ^ B) & kSign) | (static_cast<uint64_t>(e & 0x7ff) << 52) |
+                   (mant & kFrac));
+}
+
 }  // namespace f64emu
 }  // namespace b200

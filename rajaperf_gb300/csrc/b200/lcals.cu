@@ -3,6 +3,7 @@
 // one index (citations at each functor); the arithmetic is written in the
 // macro's operation order.
 #include "b200_internal.cuh"
+#include "b200_f64emu.cuh"
 #include "b200_map.cuh"
 #include "b200_reduce.cuh"
 
@@ -130,12 +131,31 @@ hydro2d_body1(double* __restrict__ za, double* __restrict__ zb,
               int64_t kn, int64_t jn) {
   const int64_t j = 1 + static_cast<int64_t>(blockIdx.x) * BS + threadIdx.x;
   if (j >= jn - 1) return;
+  // The two divisions run on the integer and FP32 pipes (f64emu::div_fast,
+  // correctly rounded, bit-identical to the FP64 divide); the FP64 pipe keeps
+  // the 12 adds and multiplies of a point.  A thread that met a zero,
+  // subnormal or non-finite operand or quotient rewrites its points with the
+  // FP64 divide after the loop.
+  bool slow = false;
   for (int64_t k = 1 + blockIdx.y; k < kn - 1; k += gridDim.y) {
     const int64_t c = j + k * jn;
-    za[c] = (ld(zp + c - 1 + jn) + ld(zq + c - 1 + jn) - ld(zp + c - 1) - ld(zq + c - 1)) *
-            (ld(zr + c) + ld(zr + c - 1)) / (ld(zm + c - 1) + ld(zm + c - 1 + jn));
-    zb[c] = (ld(zp + c - 1) + ld(zq + c - 1) - ld(zp + c) - ld(zq + c)) *
-            (ld(zr + c) + ld(zr + c - jn)) / (ld(zm + c) + ld(zm + c - 1));
+    za[c] = f64emu::div_fast(
+        (ld(zp + c - 1 + jn) + ld(zq + c - 1 + jn) - ld(zp + c - 1) - ld(zq + c - 1)) *
+            (ld(zr + c) + ld(zr + c - 1)),
+        ld(zm + c - 1) + ld(zm + c - 1 + jn), slow);
+    zb[c] = f64emu::div_fast(
+        (ld(zp + c - 1) + ld(zq + c - 1) - ld(zp + c) - ld(zq + c)) *
+            (ld(zr + c) + ld(zr + c - jn)),
+        ld(zm + c) + ld(zm + c - 1), slow);
+  }
+  if (__any_sync(__activemask(), slow) && slow) {
+    for (int64_t k = 1 + blockIdx.y; k < kn - 1; k += gridDim.y) {
+      const int64_t c = j + k * jn;
+      za[c] = (ld(zp + c - 1 + jn) + ld(zq + c - 1 + jn) - ld(zp + c - 1) - ld(zq + c - 1)) *
+              (ld(zr + c) + ld(zr + c - 1)) / (ld(zm + c - 1) + ld(zm + c - 1 + jn));
+      zb[c] = (ld(zp + c - 1) + ld(zq + c - 1) - ld(zp + c) - ld(zq + c)) *
+              (ld(zr + c) + ld(zr + c - jn)) / (ld(zm + c) + ld(zm + c - 1));
+    }
   }
 }
 
