@@ -32,7 +32,9 @@ struct Pressure {
   }
 };
 
-// apps/ENERGY.hpp:111-178 (BODY1..BODY6 in order)
+// apps/ENERGY.hpp:111-178 (BODY1..BODY6 in order).  Bound by the FP64 pipe;
+// the exact power-of-two products and the division by 6.0 move to the
+// integer and FP32 pipes (see body()).
 struct Energy {
   double* __restrict__ e_new;
   const double* __restrict__ e_old;
@@ -51,12 +53,20 @@ struct Energy {
   const double* __restrict__ vnewc;
   double rho0, e_cut, emin, q_cut;
 
-  __device__ void operator()(int64_t i) const {
+  // One element, BODY1..BODY6.  FAST: the power-of-two products (0.5 * dv,
+  // 0.5 * wk, 4.0 * x, 8.0 * x) are exponent moves and the division by 6.0 is
+  // f64emu::div_fast -- all exact or correctly rounded, so every result bit
+  // equals the FP64 pipe's -- and `slow` reports an operand outside their
+  // fast paths, for which the caller recomputes the element natively.
+  template <bool FAST>
+  __device__ __forceinline__ void body(int64_t i, bool& slow) const {
     const double dv = ld(delvc + i);
     const double po = ld(p_old + i), qo = ld(q_old + i), wk = ld(work + i);
     const double ph = ld(pHalfStep + i), pn = ld(p_new + i);
+    const double hdv = FAST ? f64emu::mul_pow2_fast<-1>(dv, slow) : 0.5 * dv;
+    const double hwk = FAST ? f64emu::mul_pow2_fast<-1>(wk, slow) : 0.5 * wk;
     // BODY1
-    double e = ld(e_old + i) - 0.5 * dv * (po + qo) + 0.5 * wk;
+    double e = ld(e_old + i) - hdv * (po + qo) + hwk;
     // BODY2
     double qn;
     if (dv > 0.0) {
@@ -69,9 +79,11 @@ struct Energy {
       qn = (ssc * ld(ql_old + i) + ld(qq_old + i));
     }
     // BODY3
-    e = e + 0.5 * dv * (3.0 * (po + qo) - 4.0 * (ph + qn));
+    const double phqn = ph + qn;
+    e = e + hdv * (3.0 * (po + qo) -
+                   (FAST ? f64emu::mul_pow2_fast<2>(phqn, slow) : 4.0 * phqn));
     // BODY4
-    e += 0.5 * wk;
+    e += hwk;
     if (fabs(e) < e_cut) e = 0.0;
     if (e < emin) e = emin;
     // BODY5
@@ -85,7 +97,10 @@ struct Energy {
       else ssc = sqrt(ssc);
       q_tilde = (ssc * ld(ql_old + i) + ld(qq_old + i));
     }
-    e = e - (7.0 * (po + qo) - 8.0 * (ph + qn) + (pn + q_tilde)) * dv / 6.0;
+    const double num = (7.0 * (po + qo) -
+                        (FAST ? f64emu::mul_pow2_fast<3>(phqn, slow) : 8.0 * phqn) +
+                        (pn + q_tilde)) * dv;
+    e = e - (FAST ? f64emu::div_fast(num, 6.0, slow) : num / 6.0);
     if (fabs(e) < e_cut) e = 0.0;
     if (e < emin) e = emin;
     // BODY6
@@ -99,6 +114,11 @@ struct Energy {
     }
     e_new[i] = e;
     q_new[i] = qn;
+  }
+  __device__ void operator()(int64_t i) const {
+    bool slow = false;
+    body<true>(i, slow);
+    if (__any_sync(__activemask(), slow) && slow) body<false>(i, slow);
   }
 };
 

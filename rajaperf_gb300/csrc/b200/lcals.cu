@@ -112,10 +112,20 @@ struct Planckian {
   const double* __restrict__ u;
   const double* __restrict__ v;
   double* __restrict__ w;
+  // The two divisions run on the integer and FP32 pipes (f64emu::div_fast,
+  // correctly rounded); an element with an operand or quotient outside its
+  // fast path (zero, subnormal, non-finite) is recomputed natively.
   __device__ void operator()(int64_t i) const {
-    double yi = ld(u + i) / ld(v + i);
+    bool slow = false;
+    const double ui = ld(u + i), vi = ld(v + i), xi = ld(x + i);
+    double yi = f64emu::div_fast(ui, vi, slow);
+    double wi = f64emu::div_fast(xi, exp(yi) - 1.0, slow);
+    if (__any_sync(__activemask(), slow) && slow) {
+      yi = ui / vi;
+      wi = xi / (exp(yi) - 1.0);
+    }
     y[i] = yi;
-    w[i] = ld(x + i) / (exp(yi) - 1.0);
+    w[i] = wi;
   }
 };
 
