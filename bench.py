@@ -234,7 +234,9 @@ def _bandwidth_cases():
             self.bytes_per_rep = (8 * (4 * n + 4 * n + 4 * (kn - 2) * (jn - 2)) +
                                   8 * 6 * (kn - 2) * (jn - 2))
             self.flops_per_rep = 44 * (kn - 2) * (jn - 2)
-            self.fp64_instr_per_rep = None  # BODY1 28 per point; BODY2+3 not counted
+            # ncu: BODY1 12 per point (its divisions run on the integer and
+            # FP32 pipes), BODY2+BODY3 20 per point
+            self.fp64_instr_per_rep = 32 * (kn - 2) * (jn - 2)
 
         def inputs(self):
             return self.arr[2:9]
@@ -333,7 +335,8 @@ def _bandwidth_cases():
             self.div = self.zeros(nn)
             self.bytes_per_rep = 8 * self.nz + 4 * 8 * n_real_nodes + 8 * self.nz
             self.flops_per_rep = 54 * self.nz
-            self.fp64_instr_per_rep = 51 * self.nz  # ncu: 51.0 per zone (halves on the integer pipe)
+            # 41 per zone: halves and divisions off the FP64 pipe
+            self.fp64_instr_per_rep = 41 * self.nz
 
         def inputs(self):
             return [self.x, self.y, self.xdot, self.ydot, self.zones]
@@ -470,8 +473,8 @@ BW27 = {
     "Stream_TRIAD": (24, 1), "Stream_DOT": (16, 1), "Basic_DAXPY": (24, 1),
     "Basic_INIT3": (40, 1), "Basic_MULADDSUB": (40, 3), "Lcals_HYDRO_1D": (24, 3),
     "Lcals_EOS": (32, 8), "Lcals_FIRST_DIFF": (16, 1), "Lcals_INT_PREDICT": (88, 10),
-    "Lcals_FIRST_MIN": (8, 0), "Lcals_DIFF_PREDICT": (160, 9), "Lcals_PLANCKIAN": (40, 32),
-    "Apps_PRESSURE": (48, 6), "Apps_ENERGY": (216, 29), "Algorithm_SCAN": (16, 0),
+    "Lcals_FIRST_MIN": (8, 0), "Lcals_DIFF_PREDICT": (160, 9), "Lcals_PLANCKIAN": (40, 16),
+    "Apps_PRESSURE": (48, 6), "Apps_ENERGY": (216, 18), "Algorithm_SCAN": (16, 0),
     "Algorithm_REDUCE_SUM": (8, 1), "Algorithm_MEMSET": (8, 0), "Algorithm_MEMCPY": (16, 0),
     "Basic_INDEXLIST": (10, 0), "Algorithm_HISTOGRAM": (8, 0), "Basic_MULTI_REDUCE": (16, 1),
 }
