@@ -959,6 +959,55 @@ def measure_gemm(torch, rp, stream, sizes=(1024, 4096, 8192), seed=4793):
     return out
 
 
+def measure_3mm(torch, rp, stream, n=2048, seed=4793):
+    """Polybench 3MM, square N: E = A*B, F = C*D, G = E*F with entries uniform
+    in [-1, 1); native FP64 (b200_polybench_3mm) against three split-precision
+    products (b200_gemm_split, alpha 1, beta 0), TFLOP/s at 3 * 2 N^3 and the
+    split G's relative Frobenius error against the native G."""
+    L = rp.b200()
+    s = stream.cuda_stream
+    g = torch.Generator(device="cuda").manual_seed(seed + 3 * n)
+    A, B, C, D = (torch.rand(n, n, dtype=torch.float64, device="cuda", generator=g) * 2 - 1
+                  for _ in range(4))
+    E, F, G = (torch.zeros(n, n, dtype=torch.float64, device="cuda") for _ in range(3))
+    Es, Fs, Gs = (torch.zeros(n, n, dtype=torch.float64, device="cuda") for _ in range(3))
+    wb = L.b200_gemm_split_workspace_bytes(n, n, n, None)
+    ws = torch.empty(wb, dtype=torch.uint8, device="cuda")
+    P = lambda t: t.data_ptr()
+
+    def native():
+        return L.b200_polybench_3mm(P(A), P(B), P(C), P(D), P(E), P(F), P(G), n, n, n, n, n,
+                                    None, s)
+
+    def split():
+        for x, y, z in ((A, B, Es), (C, D, Fs), (Es, Fs, Gs)):
+            rc = L.b200_gemm_split(P(x), P(y), P(z), n, n, n, 1.0, 0.0, P(ws), wb, None, s)
+            if rc != 0:
+                return rc
+        return 0
+
+    res = {"n": n}
+    for name, fn in (("native", native), ("split", split)):
+        rp.check(fn(), name)  # warm-up
+        best = None
+        for _ in range(3):
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            rp.check(fn(), name)
+            e1.record(stream)
+            torch.cuda.synchronize()
+            t = e0.elapsed_time(e1) / 1e3
+            best = t if best is None else min(best, t)
+        res[f"{name}_ms"] = round(best * 1e3, 3)
+        res[f"{name}_tflops"] = round(3 * 2.0 * n ** 3 / best / 1e12, 3)
+    res["rel_err_vs_fp64"] = float((Gs - G).norm() / G.norm())
+    res["speedup"] = round(res["split_tflops"] / res["native_tflops"], 2)
+    del A, B, C, D, E, F, G, Es, Fs, Gs, ws
+    torch.cuda.empty_cache()
+    return res
+
+
 BATCH_KERNELS = ["Stream_COPY", "Stream_MUL", "Stream_ADD", "Stream_TRIAD", "Stream_DOT",
                  "Lcals_HYDRO_1D", "Lcals_HYDRO_2D", "Lcals_EOS", "Lcals_FIRST_DIFF",
                  "Lcals_INT_PREDICT", "Lcals_FIRST_MIN", "Apps_DEL_DOT_VEC_2D", "Apps_VOL3D",
@@ -1171,11 +1220,12 @@ def main():
 
     res = run_gpu(args, rank, world)
     dist = res.pop("dist")
-    gemm = None
+    gemm = mm3 = None
     if args.gemm == "on" or (args.gemm == "auto" and not args.kernels and world == 1):
         import torch
         import rajaperf_gb300 as rp
         gemm = measure_gemm(torch, rp, torch.cuda.current_stream(), sizes=args.gemm_sizes)
+        mm3 = measure_3mm(torch, rp, torch.cuda.current_stream())
     bw27 = batch = None
     extras = args.extras
     if extras == "auto":
@@ -1211,6 +1261,7 @@ def main():
         "cpu_baseline": cpu, "clocks": res["clocks"], "gpu_launches": res["launches"],
         "fp64_peak_gflops": round(res["fp64"]["gflops"], 1),
         "gemm_split_vs_fp64": gemm,
+        "3mm_split_vs_fp64": mm3,
         "bandwidth_all_1d": bw27,
         "graph_batch": batch,
         "per_kernel": [{k: (round(v, 4) if isinstance(v, float) else v) for k, v in p.items()}
