@@ -14,6 +14,7 @@
 #include "b200_internal.cuh"
 #include "b200_async.cuh"
 #include "b200_lookback.cuh"
+#include "b200_pipeline.cuh"
 #include "b200_reduce.cuh"
 
 using namespace b200;
@@ -25,12 +26,6 @@ constexpr int kScanThreads = kScanBlock + 32;           // + the lookback warp
 constexpr int kScanItemsMin = 16;                       // smallest tile: 4096 items
 constexpr int kScanItemsDefault = 32;                   // default tile: 8192 items
 constexpr int kScanTileMin = kScanBlock * kScanItemsMin;
-__device__ __forceinline__ void named_sync(int id, int count) {
-  asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(count) : "memory");
-}
-__device__ __forceinline__ void named_arrive(int id, int count) {
-  asm volatile("bar.arrive %0, %1;" ::"r"(id), "r"(count) : "memory");
-}
 
 // One CTA per tile of kScanBlock * IT items.  Warp 0 is the lookback warp:
 // it walks the predecessors' flags as soon as the tile id is known, while
@@ -170,85 +165,46 @@ scan_kernel(const T* __restrict__ x, T* __restrict__ y, int64_t n, T init,
 }
 
 // ---- pipelined persistent SCAN ---------------------------------------------
-// One CTA per SM walks tiles of 4096 items through a ring of seven
-// shared-memory stages, each role a warp of its own (or four):
-//  * producer (warp 0): once a stage is free, draws the next tile id from the
-//    launch counter and issues one bulk copy (TMA) of the tile.  A tile id is
-//    drawn only when its stage is free: an id held while waiting would delay
-//    that tile's aggregate and stall its successors' lookback;
-//  * aggregator (warp 1): as each tile lands, sums it and publishes the tile
-//    aggregate at once, so a successor's lookback depends only on data
-//    arrival, never on this CTA's earlier tiles;
-//  * lookback (warps 2-3, alternate tiles): starts as soon as the tile id is
-//    drawn, walks back to the nearest inclusive prefix and publishes this
-//    tile's inclusive prefix once the aggregate is in;
+// One CTA per SM on the stage ring of b200_pipeline.cuh (producer warp 0,
+// lookback warps 2-3), plus:
+//  * aggregator (warp 1): sums each tile as it lands and publishes the
+//    aggregate at once;
 //  * compute (warps 4-7): a thread owns a run of 32 consecutive items (16
-//    item pairs), sums it, scans the run sums across the tile, and when the
-//    tile's exclusive prefix arrives writes every item's prefix in place;
+//    item pairs), sums it, scans the run sums across the tile and, when the
+//    tile's exclusive prefix arrives, writes every item's prefix in place;
 //  * store (warp 8): writes a finished tile back with one bulk store and
-//    frees the stage when the store has read it.
-// A compute thread visits its pairs rotated by (run mod 16), so every
-// 16-byte shared-memory access of a warp is conflict-free without padding
-// the bulk-copied tile.  mbarriers link the roles per stage: drawn (tile id
-// set), full (data landed), summed (aggregate ready), prefix (exclusive
-// prefix ready), ready (results in place), empty (store has read the stage).
-// Every wait is bounded; one that gives up sets the workspace error word and
-// ends the CTA's work.  Measured on GB300 (int64, 2^26 items, time marks per
+//    frees the stage once the store has read it (mbarrier ready[s]: compute
+//    -> store).
+// A compute thread visits its pairs rotated by (run mod 16), so every 16-byte
+// shared-memory access of a warp is conflict-free without padding the
+// bulk-copied tile.  Measured on GB300 (int64, 2^26 items, time marks per
 // tile and role): the bare load -> store pipeline runs at the copy peak; what
 // the lookback adds is its L2 round trips under saturated HBM, which the
 // seven stages of loads in flight are there to cover.
 namespace pipe {
 
-constexpr int kTile = 4096;
-constexpr int kStages = 7;
-constexpr int kLookbackWarps = 2;
+using ring::kStages;
+using ring::kTile;
+using ring::kEnd;
 constexpr int kComputeWarps = 4;
-constexpr int kFirstCompute = 2 + kLookbackWarps;
+constexpr int kFirstCompute = 2 + ring::kLookbackWarps;
 constexpr int kStoreWarp = kFirstCompute + kComputeWarps;
 constexpr int kThreads = 32 * (kStoreWarp + 1);
 constexpr int kRuns = 32 * kComputeWarps;    // 128 runs per tile
 constexpr int kPairs = kTile / kRuns / 2;    // 16 pairs per run
-constexpr int kLookbackLanes = 8;            // 256 predecessors per round
-constexpr unsigned int kEnd = 0xffffffffu;
-constexpr uint64_t kWaitNs = 2000000000ull;  // 2 s
 
 template <typename T>
 struct Smem {
-  T tile[kStages][kTile];
-  T agg[kStages];
-  T excl[kStages];
+  ring::Ring<T, T> r;
   T warp_total[kComputeWarps];
-  unsigned int ticket[kStages];
-  unsigned int phases[kStages];  // full-barrier phases started per stage
-  uint64_t drawn[kStages];
-  uint64_t full[kStages];
-  uint64_t summed[kStages];
-  uint64_t prefix[kStages];
-  uint64_t ready[kStages];
-  uint64_t empty[kStages];
-  unsigned long long epoch;
-  int abort;
-  int fail_loaded;   // compute group: a wait before its first barrier gave up
-  int fail_prefix;   // compute group: a wait before its second barrier gave up
+  uint64_t ready[kStages];  // compute -> store warp: the stage holds results
+  int fail_loaded;          // compute group: a wait before its first barrier gave up
+  int fail_prefix;          // compute group: a wait before its second barrier gave up
 };
 
 template <typename T>
 constexpr size_t smem_bytes() { return sizeof(Smem<T>) + 128; }
 static_assert(sizeof(Smem<double>) + 128 <= 232448, "shared memory budget");
-
-// Bounded wait by a whole warp; the result is the same in every lane (a lane
-// that gave up fails the warp).  On expiry records the error and stops every
-// role of the CTA.
-template <typename T>
-__device__ __forceinline__ bool wait(Smem<T>& sm, uint64_t* bar, uint32_t parity,
-                                     ScanHeader* hdr) {
-  const bool ok = __all_sync(0xffffffffu, mbar_wait_for(bar, parity, kWaitNs));
-  if (!ok && (threadIdx.x & 31) == 0) {
-    atomicExch(&hdr->error, 1u);
-    *reinterpret_cast<volatile int*>(&sm.abort) = 1;
-  }
-  return ok;
-}
 
 template <typename T>
 __global__ void __launch_bounds__(kThreads, 1)
@@ -259,88 +215,28 @@ scan_pipelined(const T* __restrict__ x, T* __restrict__ y, int64_t n, T init,
   extern __shared__ unsigned char s_raw[];
   Smem<T>& sm = *reinterpret_cast<Smem<T>*>(
       (reinterpret_cast<uintptr_t>(s_raw) + 127) & ~static_cast<uintptr_t>(127));
+  ring::Ring<T, T>& r = sm.r;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
 
   if (tid == 0) {
-    for (int s = 0; s < kStages; ++s) {
-      mbar_init(&sm.drawn[s], 1);
-      mbar_init(&sm.full[s], 1);
-      mbar_init(&sm.summed[s], 1);
-      mbar_init(&sm.prefix[s], 1);
-      mbar_init(&sm.ready[s], 1);
-      mbar_init(&sm.empty[s], 1);
-      sm.phases[s] = 0u;
-    }
-    sm.abort = 0;
+    ring::init(r);
+    for (int s = 0; s < kStages; ++s) mbar_init(&sm.ready[s], 1);
     sm.fail_loaded = 0;
     sm.fail_prefix = 0;
     mbar_init_fence();
   }
   __syncthreads();
-  volatile int* abort_flag = &sm.abort;
 
   if (warp == 0) {
-    // ---- producer ----
-    const unsigned long long draws = static_cast<unsigned long long>(tiles) + gridDim.x;
-    int ends = 0;
-    for (int k = 0; ends < kLookbackWarps && !__any_sync(0xffffffffu, *abort_flag); ++k) {
-      const int s = k % kStages;
-      if (k >= kStages && !wait(sm, &sm.empty[s], ((k / kStages) - 1) & 1, hdr)) break;
-      unsigned int tile = kEnd;
-      if (ends == 0) {
-        unsigned long long t = 0;
-        if (lane == 0) {
-          t = atomicAdd(&hdr->ticket, 1ull);
-          // the launch's last draw: every CTA has drawn; reset and next epoch
-          if (static_cast<unsigned int>(t) == draws - 1)
-            atomicAdd(&hdr->ticket, (1ull << 32) - draws);
-        }
-        t = __shfl_sync(0xffffffffu, t, 0);
-        if (k == 0 && lane == 0) sm.epoch = t >> 32;
-        if (static_cast<unsigned int>(t) < tiles) tile = static_cast<unsigned int>(t);
-      }
-      if (lane == 0) {
-        sm.ticket[s] = tile;
-        mbar_arrive(&sm.drawn[s]);
-      }
-      if (tile == kEnd) {
-        // one end marker per lookback warp (they take alternate stages)
-        ++ends;
-        __syncwarp();
-        if (lane == 0) {
-          ++sm.phases[s];
-          mbar_arrive(&sm.full[s]);
-        }
-        continue;
-      }
-      const int64_t base = static_cast<int64_t>(tile) * kTile;
-      if (base + kTile <= n) {
-        if (lane == 0) {
-          ++sm.phases[s];
-          mbar_arrive_expect_tx(&sm.full[s], kTile * sizeof(T));
-          bulk_load(sm.tile[s], x + base, kTile * sizeof(T), &sm.full[s]);
-        }
-      } else {
-        // the ragged last tile: plain loads, zero-filled
-        for (int i = lane; i < kTile; i += 32) sm.tile[s][i] = (base + i < n) ? x[base + i] : T(0);
-        __syncwarp();
-        if (lane == 0) {
-          ++sm.phases[s];
-          mbar_arrive(&sm.full[s]);
-        }
-      }
-    }
+    ring::produce(r, x, n, tiles, hdr);
   } else if (warp == 1) {
-    // ---- aggregator ----
+    // ---- aggregator: lane L sums pairs L, L + 32, ... (conflict-free) ----
     for (int k = 0;; ++k) {
       const int s = k % kStages;
-      const uint32_t par = (k / kStages) & 1;
-      if (!wait(sm, &sm.full[s], par, hdr)) break;
-      const unsigned int tile = sm.ticket[s];
+      if (!ring::wait(r, &r.full[s], (k / kStages) & 1, hdr)) break;
+      const unsigned int tile = r.ticket[s];
       if (tile == kEnd) break;
-      // lane L sums pairs L, L + 32, ... (consecutive lanes: consecutive
-      // 16-byte words, conflict-free)
-      const V2* tv = reinterpret_cast<const V2*>(sm.tile[s]);
+      const V2* tv = reinterpret_cast<const V2*>(r.tile[s]);
       T total = T(0);
 #pragma unroll 16
       for (int q = lane; q < kTile / 2; q += 32) {
@@ -350,32 +246,12 @@ scan_pipelined(const T* __restrict__ x, T* __restrict__ y, int64_t n, T init,
       }
 #pragma unroll
       for (int off = 16; off > 0; off >>= 1) total += __shfl_xor_sync(0xffffffffu, total, off);
-      if (lane == 0) {
-        sm.agg[s] = total;
-        if (tile > 0) desc_store(descs + tile, sm.epoch * 4 + 1, to_bits<T>(total));
-      }
+      if (lane == 0) ring::publish_aggregate(r, descs, s, tile, total);
       __syncwarp();
-      if (lane == 0) mbar_arrive(&sm.summed[s]);
+      if (lane == 0) mbar_arrive(&r.summed[s]);
     }
   } else if (warp < kFirstCompute) {
-    // ---- lookback (alternate tiles) ----
-    for (int k = warp - 2;; k += kLookbackWarps) {
-      const int s = k % kStages;
-      const uint32_t par = (k / kStages) & 1;
-      if (!wait(sm, &sm.drawn[s], par, hdr)) break;
-      const unsigned int tile = sm.ticket[s];
-      if (tile == kEnd) break;
-      const unsigned long long AGG = sm.epoch * 4 + 1, INC = sm.epoch * 4 + 2;
-      const T excl =
-          (tile > 0) ? lookback_exclusive<T, kLookbackLanes>(descs, tile, AGG, INC, hdr) : init;
-      if (!wait(sm, &sm.summed[s], par, hdr)) break;
-      if (lane == 0) {
-        desc_store(descs + tile, INC, to_bits<T>(excl + sm.agg[s]));
-        sm.excl[s] = excl;
-      }
-      __syncwarp();
-      if (lane == 0) mbar_arrive(&sm.prefix[s]);
-    }
+    ring::look_back(r, descs, init, hdr, warp - 2);
   } else if (warp < kStoreWarp) {
     // ---- compute ----
     // The four warps decide together whether to go on: a warp whose wait
@@ -391,10 +267,10 @@ scan_pipelined(const T* __restrict__ x, T* __restrict__ y, int64_t n, T init,
     for (int k = 0;; ++k) {
       const int s = k % kStages;
       const uint32_t par = (k / kStages) & 1;
-      const bool loaded = wait(sm, &sm.full[s], par, hdr);
-      const unsigned int tile = sm.ticket[s];
+      const bool loaded = ring::wait(r, &r.full[s], par, hdr);
+      const unsigned int tile = r.ticket[s];
       if (!loaded) *fail_loaded = 1;
-      V2* tv = reinterpret_cast<V2*>(sm.tile[s]) + ct * kPairs;
+      V2* tv = reinterpret_cast<V2*>(r.tile[s]) + ct * kPairs;
       V2 v[kPairs];
       T head = T(0), tail = T(0);  // pairs q < rot come first in index order
       if (loaded && tile != kEnd) {
@@ -421,18 +297,18 @@ scan_pipelined(const T* __restrict__ x, T* __restrict__ y, int64_t n, T init,
       }
       T woff = T(0);
       for (int w = 0; w < cw; ++w) woff += sm.warp_total[w];
-      const bool have_prefix = wait(sm, &sm.prefix[s], par, hdr);
+      const bool have_prefix = ring::wait(r, &r.prefix[s], par, hdr);
       if (have_prefix) {
-        const T base = sm.excl[s] + (woff + (inc - rs));
-        T r = base + head;
+        const T base = r.excl[s] + (woff + (inc - rs));
+        T run = base + head;
 #pragma unroll
         for (int w = 0; w < kPairs; ++w) {
-          if (w == kPairs - rot) r = base;
+          if (w == kPairs - rot) run = base;
           V2 o;
-          o.x = r;
-          r += v[w].x;
-          o.y = r;
-          r += v[w].y;
+          o.x = run;
+          run += v[w].x;
+          o.y = run;
+          run += v[w].y;
           tv[(w + rot) & (kPairs - 1)] = o;
         }
         fence_proxy_async_smem();
@@ -444,38 +320,33 @@ scan_pipelined(const T* __restrict__ x, T* __restrict__ y, int64_t n, T init,
       const int64_t first = static_cast<int64_t>(tile) * kTile;
       if (first + kTile > n) {
         // the ragged last tile: plain stores
-        for (int i = ct; first + i < n; i += 32 * kComputeWarps) y[first + i] = sm.tile[s][i];
+        for (int i = ct; first + i < n; i += 32 * kComputeWarps) y[first + i] = r.tile[s][i];
       }
       if (ct == 0) mbar_arrive(&sm.ready[s]);
     }
   } else {
-    // ---- store: one bulk store per finished tile ----
+    // ---- store: one bulk store per finished tile, then the stage is free ----
     for (int k = 0;; ++k) {
       const int s = k % kStages;
-      if (!wait(sm, &sm.ready[s], (k / kStages) & 1, hdr)) break;
-      const unsigned int tile = sm.ticket[s];
+      if (!ring::wait(r, &sm.ready[s], (k / kStages) & 1, hdr)) break;
+      const unsigned int tile = r.ticket[s];
       if (tile == kEnd) break;
       const int64_t first = static_cast<int64_t>(tile) * kTile;
       if (lane == 0) {
         if (first + kTile <= n) {
-          bulk_store(y + first, sm.tile[s], kTile * sizeof(T));
+          bulk_store(y + first, r.tile[s], kTile * sizeof(T));
           bulk_commit();
           bulk_wait_read<0>();
         }
-        mbar_arrive(&sm.empty[s]);
+        mbar_arrive(&r.empty[s]);
       }
       __syncwarp();
     }
     if (lane == 0) bulk_wait_all();
   }
 
-  // After an abort, bulk copies may still be landing in shared memory: wait
-  // (bounded) for the last phase started in each stage before the CTA exits.
   __syncthreads();
-  if (tid == 0 && sm.abort) {
-    for (int s = 0; s < kStages; ++s)
-      if (sm.phases[s] > 0u) mbar_wait_for(&sm.full[s], (sm.phases[s] - 1u) & 1u, kWaitNs);
-  }
+  if (tid == 0) ring::drain(r);
 }
 
 }  // namespace pipe

@@ -141,6 +141,14 @@ __device__ __forceinline__ double mul_pow2_fast(double x, bool& slow) {
   return __hiloint2double(hi + K * (1 << 20), __double2loint(x));
 }
 
+// x < 0.0 on the integer pipe: the sign bit is set and the magnitude is
+// neither zero (-0.0 is not below 0) nor a NaN (no NaN compares below 0);
+// -inf counts.  Equal to the FP64 compare for every input.
+__device__ __forceinline__ bool lt_zero(double x) {
+  const uint64_t u = bits(x);
+  return (u >> 63) && ((u & ~kSign) - 1u) < 0x7FF0000000000000ULL;
+}
+
 // One round of the significand long division in div_fast: appends K quotient
 // bits to Q and leaves the exact remainder in R (0 <= R < mb on entry and on
 // exit).  The digit q = floor(R * 2^K / mb) is estimated in FP32 from the top

@@ -43,11 +43,16 @@ def test_memset_memcpy(n, offset):
     assert np.all(d[offset + n:] == -1.0)
 
 
-@pytest.mark.parametrize("case", ["empty", "none", "all", "random", "sparse", "ragged"])
-def test_indexlist(case):
+@pytest.mark.parametrize("algo", [0, 1])
+@pytest.mark.parametrize("case", ["empty", "none", "all", "random", "sparse", "ragged",
+                                  "many_tiles", "one_pair", "special"])
+def test_indexlist(case, algo):
+    """algo 0: the persistent ring kernel (x aligned); algo 1: one CTA per
+    tile.  many_tiles runs several tiles per SM through the ring."""
     torch = gu.torch_cuda()
     rng = np.random.default_rng(5)
-    n = {"empty": 0, "ragged": 4096 * 7 + 123}.get(case, 1 << 20)
+    n = {"empty": 0, "ragged": 4096 * 7 + 123, "many_tiles": 4096 * 152 * 5 + 77,
+         "one_pair": 2}.get(case, 1 << 20)
     x = rng.uniform(-1, 1, n)
     if case == "none":
         x = np.abs(x) + 0.1
@@ -56,6 +61,11 @@ def test_indexlist(case):
     elif case == "sparse":
         x = np.abs(x) + 0.1
         x[rng.integers(0, n, 37)] = -1.0
+    elif case == "special":  # x < 0 is tested on the integer pipe: IEEE semantics
+        neg_nan = np.frombuffer(np.uint64(0xFFF8000000000001).tobytes(), dtype=np.float64)[0]
+        vals = np.array([-0.0, 0.0, np.nan, neg_nan, -np.inf, np.inf, -5e-324, 5e-324,
+                         -1.7976931348623157e308, 2.2250738585072014e-308])
+        x[rng.integers(0, n, 4000)] = vals[rng.integers(0, vals.size, 4000)]
     dx = gu.dev(x) if n else zeros(1, torch.float64)
     lst = torch.full((max(n, 1),), -5, dtype=torch.int32, device="cuda")
     ln = zeros(1, torch.int64)
@@ -63,7 +73,8 @@ def test_indexlist(case):
     ws = zeros(wsb, torch.uint8)
     for _ in range(2):  # the workspace is reused
         rp.check(lib().b200_basic_indexlist(dx.data_ptr(), lst.data_ptr(), n, ln.data_ptr(),
-                                            ws.data_ptr(), wsb, None, gu.stream()))
+                                            ws.data_ptr(), wsb, ctypes.byref(rp.Tune(algo=algo)),
+                                            gu.stream()))
         want = np.nonzero(x < 0.0)[0]
         got_len = int(gu.host(ln)[0])
         assert got_len == want.size
@@ -71,6 +82,7 @@ def test_indexlist(case):
         assert np.array_equal(got[:want.size], want.astype(np.int32))
         assert np.all(got[want.size:n] == -5)  # entries past the count untouched
     assert int(gu.host(ws[16:20]).view(np.uint32)[0]) == 0
+    assert int(gu.host(ws[0:4]).view(np.uint32)[0]) == 0  # ticket count reset
 
 
 @pytest.mark.parametrize("num_bins", [1, 10, 1000, 20000])
