@@ -101,7 +101,9 @@ int b200_probe_dfma(double* out, int32_t iters, int64_t* fma_count,
  * exponents, range edges, [0.5, 1.5)), op 0 = add, 1 = sub, 2 = mul,
  * 3 = a * 0.5, 4 = a * 0.125, 5 = a * 2, 6 = a / b (the FP64-free division
  * of HYDRO_2D and DEL_DOT_VEC_2D, with quotients near rounding midpoints, near
- * 1 and extreme divisor significands added); adds to *mismatches (device) the number of
+ * 1 and extreme divisor significands added), 7 = a < 0 (INDEXLIST's
+ * integer test; signed zeros, infinities and NaNs added); adds to
+ * *mismatches (device) the number of
  * results whose bits differ from the FP64 pipe's.  Not in the reference. */
 int b200_f64emu_selftest(int64_t n, uint64_t seed, int32_t op,
                          unsigned long long* mismatches, b200_stream_t stream);

@@ -356,6 +356,13 @@ __global__ void f64emu_check_kernel(int64_t n, uint64_t seed, int op,
         break;
       }
     }
+    if (op == 7 && (i % 7) == 6) {  // x < 0: signed zeros, infinities, NaNs
+      const uint64_t sp[6] = {0x0ULL, 0x8000000000000000ULL, 0x7FF0000000000000ULL,
+                              0xFFF0000000000000ULL, 0x7FF8000000000001ULL,
+                              0xFFF8000000000000ULL};
+      A = sp[(ra >> 60) % 6u];
+      if ((rb >> 61) & 1u) B = sp[(rb >> 56) % 6u];
+    }
     if (op == 6) {  // division: three more families that stress rounding
       const uint64_t bb = (rb & 0x800FFFFFFFFFFFFFULL) | ((((rb >> 52) & 0x7ffu) % 1500u + 270u) << 52);
       switch ((i >> 3) % 4) {
@@ -399,11 +406,14 @@ __global__ void f64emu_check_kernel(int64_t n, uint64_t seed, int op,
       bool slow = false;
       got = b200::f64emu::mul_pow2_fast<1>(a, slow);
       if (slow) got = __dmul_rn(a, 2.0);
-    } else {
+    } else if (op == 6) {
       want = __ddiv_rn(a, b);
       bool slow = false;
       got = b200::f64emu::div_fast(a, b, slow);
       if (slow) got = __ddiv_rn(a, b);
+    } else {  // x < 0 as INDEXLIST tests it
+      want = a < 0.0 ? 1.0 : 0.0;
+      got = b200::f64emu::lt_zero(a) ? 1.0 : 0.0;
     }
     const bool same = (__double_as_longlong(want) == __double_as_longlong(got)) ||
                       (isnan(want) && isnan(got));
@@ -416,7 +426,7 @@ __global__ void f64emu_check_kernel(int64_t n, uint64_t seed, int op,
 
 extern "C" int b200_f64emu_selftest(int64_t n, uint64_t seed, int32_t op,
                                     unsigned long long* mismatches, b200_stream_t stream) {
-  if (n < 0 || !mismatches || op < 0 || op > 6) return invalid("b200_f64emu_selftest: bad args");
+  if (n < 0 || !mismatches || op < 0 || op > 7) return invalid("b200_f64emu_selftest: bad args");
   const int blocks = device_info().sm_count * 8;
   f64emu_check_kernel<<<blocks, 256, 0, as_stream(stream)>>>(n, seed, op, mismatches);
   return after_launch("b200_f64emu_selftest");

@@ -308,12 +308,13 @@ def test_null_pointer_rejected(fn, args):
     assert f(*argv) == rp.B200_ERR_INVALID_ARG
 
 
-@pytest.mark.parametrize("op", [0, 1, 2, 3, 4, 5, 6])
+@pytest.mark.parametrize("op", [0, 1, 2, 3, 4, 5, 6, 7])
 def test_integer_pipe_fp64_is_bit_exact(op):
     """The integer-pipe add/sub/mul used by the mixed-pipe stencils, the
     exponent-shift products by 0.5, 0.125 and 2 of DEL_DOT_VEC_2D and HEAT_3D,
-    and the FP64-free division of HYDRO_2D and DEL_DOT_VEC_2D, against the
-    FP64 pipe on 16M operands (every class of double; 64M for the division)."""
+    the FP64-free division of HYDRO_2D and DEL_DOT_VEC_2D, and INDEXLIST's
+    integer x < 0 test, against the FP64 pipe on 16M operands (every class of
+    double; 64M for the division)."""
     torch = gu.torch_cuda()
     bad = torch.zeros(1, dtype=torch.int64, device="cuda")
     n = (1 << 26) if op == 6 else (1 << 24)
