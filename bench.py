@@ -361,7 +361,7 @@ def _bandwidth_cases():
             self.A, self.B = self.uniform(N * N), self.uniform(N * N)
             self.bytes_per_rep = (8 * (N * N - 4) * 2 + 8 * (N - 2) * (N - 2) * 2) * tsteps
             self.flops_per_rep = tsteps * 10 * (N - 2) * (N - 2)
-            self.fp64_instr_per_rep = tsteps * 10 * (N - 2) * (N - 2)
+            self.fp64_instr_per_rep = tsteps * 8 * (N - 2) * (N - 2)  # 4 adds per point per half-step
 
         def inputs(self):
             return [self.A, self.B]

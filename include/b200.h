@@ -102,7 +102,8 @@ int b200_probe_dfma(double* out, int32_t iters, int64_t* fma_count,
  * 3 = a * 0.5, 4 = a * 0.125, 5 = a * 2, 6 = a / b (the FP64-free division
  * of HYDRO_2D and DEL_DOT_VEC_2D, with quotients near rounding midpoints, near
  * 1 and extreme divisor significands added), 7 = a < 0 (INDEXLIST's
- * integer test; signed zeros, infinities and NaNs added); adds to
+ * integer test; signed zeros, infinities and NaNs added), 8 = a * b on the
+ * integer pipe (JACOBI_2D's a * 0.2 for every other pair); adds to
  * *mismatches (device) the number of
  * results whose bits differ from the FP64 pipe's.  Not in the reference. */
 int b200_f64emu_selftest(int64_t n, uint64_t seed, int32_t op,
@@ -294,9 +295,11 @@ int b200_apps_del_dot_vec_2d(const double* x, const double* y,
 
 /* tsteps x (B <- 5-point average of A, then A <- of B) on an N x N grid
  *   -- polybench/POLYBENCH_JACOBI_2D.hpp:38-44, -Cuda.cpp:86-114
- * tune->algo > 0 selects the mixed-pipe kernel: algo-1 of every 8 warps run
- * bit-identical integer-pipe FP64 (rows per warp: tile_y emulated, tile_z
- * native).                                                                  */
+ * Default: column segments of tune->items rows per thread (2, 4 or 8;
+ * default 2), the product by 0.2 on the integer pipe (bit-identical);
+ * tune->items 1: one point per thread.  tune->algo > 0 selects the
+ * mixed-pipe kernel: algo-1 of every 8 warps run bit-identical integer-pipe
+ * FP64 (rows per warp: tile_y emulated, tile_z native).                     */
 int b200_polybench_jacobi_2d(double* A, double* B, int64_t N, int64_t tsteps,
                              const b200_tune* tune, b200_stream_t stream);
 

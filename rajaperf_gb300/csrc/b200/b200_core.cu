@@ -411,9 +411,15 @@ __global__ void f64emu_check_kernel(int64_t n, uint64_t seed, int op,
       bool slow = false;
       got = b200::f64emu::div_fast(a, b, slow);
       if (slow) got = __ddiv_rn(a, b);
-    } else {  // x < 0 as INDEXLIST tests it
+    } else if (op == 7) {  // x < 0 as INDEXLIST tests it
       want = a < 0.0 ? 1.0 : 0.0;
       got = b200::f64emu::lt_zero(a) ? 1.0 : 0.0;
+    } else {  // a * b on the integer pipe; every other pair as JACOBI_2D's a * 0.2
+      const double c = (i & 1) ? 0.2 : b;
+      want = __dmul_rn(a, c);
+      bool slow = false;
+      got = b200::f64emu::mul_fast(a, c, slow);
+      if (slow) got = __dmul_rn(a, c);
     }
     const bool same = (__double_as_longlong(want) == __double_as_longlong(got)) ||
                       (isnan(want) && isnan(got));
@@ -426,7 +432,7 @@ __global__ void f64emu_check_kernel(int64_t n, uint64_t seed, int op,
 
 extern "C" int b200_f64emu_selftest(int64_t n, uint64_t seed, int32_t op,
                                     unsigned long long* mismatches, b200_stream_t stream) {
-  if (n < 0 || !mismatches || op < 0 || op > 7) return invalid("b200_f64emu_selftest: bad args");
+  if (n < 0 || !mismatches || op < 0 || op > 8) return invalid("b200_f64emu_selftest: bad args");
   const int blocks = device_info().sm_count * 8;
   f64emu_check_kernel<<<blocks, 256, 0, as_stream(stream)>>>(n, seed, op, mismatches);
   return after_launch("b200_f64emu_selftest");

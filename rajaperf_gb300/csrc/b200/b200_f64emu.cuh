@@ -125,6 +125,34 @@ __device__ __forceinline__ double scale2(double x, int k) {
   return from_bits(X + (static_cast<uint64_t>(static_cast<int64_t>(k)) << 52));
 }
 
+// a * b, correctly rounded (RN-even), on the integer pipe: the 106-bit
+// product of the significands (64-bit multiply and high half), one
+// normalising shift, then round-to-nearest-even on the bits shifted out.
+// `slow` is set for zeros, subnormals, infinities, NaNs and products outside
+// the normal range; the caller then multiplies natively.  With a constant b
+// the compiler folds b's fields.
+__device__ __forceinline__ double mul_fast(double a, double b, bool& slow) {
+  const uint64_t A = bits(a), B = bits(b);
+  const uint32_t eA = static_cast<uint32_t>(A >> 52) & 0x7ffu;
+  const uint32_t eB = static_cast<uint32_t>(B >> 52) & 0x7ffu;
+  const uint64_t mA = (A & kFrac) | kHidden, mB = (B & kFrac) | kHidden;
+  const uint64_t lo = mA * mB;
+  const uint64_t hi = __umul64hi(mA, mB);  // product < 2^106: hi < 2^42
+  int e = static_cast<int>(eA) + static_cast<int>(eB) - 1023;
+  const bool top = (hi >> 41) != 0u;  // product in [2^105, 2^106)
+  uint64_t mant = top ? ((hi << 11) | (lo >> 53)) : ((hi << 12) | (lo >> 52));
+  const uint64_t rem = top ? (lo & ((1ULL << 53) - 1u)) : (lo & ((1ULL << 52) - 1u));
+  const uint64_t half = top ? (1ULL << 52) : (1ULL << 51);
+  e += top ? 1 : 0;
+  if (rem > half || (rem == half && (mant & 1u))) mant += 1u;
+  if (mant >> 53) {
+    mant >>= 1;
+    e += 1;
+  }
+  slow |= (eA - 1u >= 2046u) || (eB - 1u >= 2046u) || e <= 0 || e >= 2047;
+  return from_bits(((A ^ B) & kSign) | ((static_cast<uint64_t>(e & 0x7ff) - 1u) << 52) + mant);
+}
+
 // x * 2^K for a constant K as an exponent move on the integer pipe.  Exact
 // and equal to the FP64 pipe's x * 2^K while x and the result are normal
 // numbers; `slow` is set for every other input (zeros, subnormals,

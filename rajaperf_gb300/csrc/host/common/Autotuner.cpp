@@ -16,7 +16,7 @@ namespace rajaperf {
 
 namespace {
 
-enum class Family { Map, Stream, Reduce, Scan, Hydro2D, Fixed };
+enum class Family { Map, Stream, Reduce, Scan, Hydro2D, Rows, Fixed };
 
 Family familyOf(KernelID kid) {
   switch (kid) {
@@ -28,13 +28,15 @@ Family familyOf(KernelID kid) {
       return Family::Scan;
     case Lcals_HYDRO_2D:
       return Family::Hydro2D;
+    case Polybench_JACOBI_2D:
+      return Family::Rows;
     case Basic_DAXPY: case Basic_INIT3: case Basic_MULADDSUB: case Lcals_DIFF_PREDICT:
     case Lcals_EOS: case Lcals_FIRST_DIFF: case Lcals_HYDRO_1D: case Lcals_INT_PREDICT:
     case Lcals_PLANCKIAN: case Apps_DEL_DOT_VEC_2D: case Apps_ENERGY: case Apps_PRESSURE:
     case Apps_VOL3D:
       return Family::Map;
     default:
-      return Family::Fixed;  // Polybench: one shape per kernel
+      return Family::Fixed;  // the other Polybench kernels: one shape each
   }
 }
 
@@ -77,6 +79,14 @@ std::vector<b200_tune> autotuneCandidates(KernelID kid) {
     for (int items : {16, 32}) {
       b200_tune t{};
       t.algo = 1;
+      t.items = items;
+      out.push_back(t);
+    }
+    return out;
+  }
+  if (f == Family::Rows) {  // rows per thread of the column-segment stencil
+    for (int items : {1, 2, 4, 8}) {
+      b200_tune t{};
       t.items = items;
       out.push_back(t);
     }

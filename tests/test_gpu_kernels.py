@@ -308,13 +308,13 @@ def test_null_pointer_rejected(fn, args):
     assert f(*argv) == rp.B200_ERR_INVALID_ARG
 
 
-@pytest.mark.parametrize("op", [0, 1, 2, 3, 4, 5, 6, 7])
+@pytest.mark.parametrize("op", [0, 1, 2, 3, 4, 5, 6, 7, 8])
 def test_integer_pipe_fp64_is_bit_exact(op):
     """The integer-pipe add/sub/mul used by the mixed-pipe stencils, the
     exponent-shift products by 0.5, 0.125 and 2 of DEL_DOT_VEC_2D and HEAT_3D,
-    the FP64-free division of HYDRO_2D and DEL_DOT_VEC_2D, and INDEXLIST's
-    integer x < 0 test, against the FP64 pipe on 16M operands (every class of
-    double; 64M for the division)."""
+    the FP64-free division of HYDRO_2D and DEL_DOT_VEC_2D, INDEXLIST's integer
+    x < 0 test and JACOBI_2D's integer-pipe multiply, against the FP64 pipe on
+    16M operands (every class of double; 64M for the division)."""
     torch = gu.torch_cuda()
     bad = torch.zeros(1, dtype=torch.int64, device="cuda")
     n = (1 << 26) if op == 6 else (1 << 24)
@@ -377,5 +377,33 @@ def test_heat_exponent_shift_special_values(case):
     t = rp.Tune(algo=1)
     rp.check(lib().b200_polybench_heat_3d(dA2.data_ptr(), dB2.data_ptr(), N, ts,
                                           ctypes.byref(t), gu.stream()))
+    assert np.array_equal(gu.host(dA1).view(np.int64), gu.host(dA2).view(np.int64))
+    assert np.array_equal(gu.host(dB1).view(np.int64), gu.host(dB2).view(np.int64))
+
+
+@pytest.mark.parametrize("case", ["zeros", "subnormal", "mixed"])
+def test_jacobi_integer_multiply_special_values(case):
+    """The default JACOBI_2D kernel multiplies by 0.2 on the integer pipe and
+    rewrites a thread's points natively when a sum is zero, subnormal or
+    non-finite; its results must equal the all-FP64-pipe kernel's (algo 1:
+    no emulated warps) bit for bit on such data."""
+    N, ts = 70, 3
+    rng = np.random.default_rng(11)
+    if case == "zeros":
+        A = np.zeros(N * N)
+        A[rng.integers(0, N * N, 30)] = 1.0
+    elif case == "subnormal":
+        A = rng.uniform(0.5, 1.5, N * N) * 1e-310
+    else:
+        A = rng.uniform(0.5, 1.5, N * N)
+        A[: N * N // 3] = 0.0
+        A[rng.integers(0, N * N, 50)] = 3e-309
+    B = rng.uniform(0.5, 1.5, N * N)
+    dA1, dB1, dA2, dB2 = dev(A), dev(B), dev(A), dev(B)
+    rp.check(lib().b200_polybench_jacobi_2d(dA1.data_ptr(), dB1.data_ptr(), N, ts, None,
+                                            gu.stream()))
+    t = rp.Tune(algo=1)
+    rp.check(lib().b200_polybench_jacobi_2d(dA2.data_ptr(), dB2.data_ptr(), N, ts,
+                                            ctypes.byref(t), gu.stream()))
     assert np.array_equal(gu.host(dA1).view(np.int64), gu.host(dA2).view(np.int64))
     assert np.array_equal(gu.host(dB1).view(np.int64), gu.host(dB2).view(np.int64))
