@@ -472,7 +472,7 @@ BW27 = {
     "Stream_COPY": (16, 0), "Stream_MUL": (16, 1), "Stream_ADD": (24, 1),
     "Stream_TRIAD": (24, 1), "Stream_DOT": (16, 1), "Basic_DAXPY": (24, 1),
     "Basic_INIT3": (40, 1), "Basic_MULADDSUB": (40, 3), "Lcals_HYDRO_1D": (24, 3),
-    "Lcals_EOS": (32, 8), "Lcals_FIRST_DIFF": (16, 1), "Lcals_INT_PREDICT": (88, 10),
+    "Lcals_EOS": (32, 8), "Lcals_FIRST_DIFF": (16, 1), "Lcals_INT_PREDICT": (88, 9),
     "Lcals_FIRST_MIN": (8, 0), "Lcals_DIFF_PREDICT": (160, 9), "Lcals_PLANCKIAN": (40, 16),
     "Apps_PRESSURE": (48, 6), "Apps_ENERGY": (216, 18), "Algorithm_SCAN": (16, 0),
     "Algorithm_REDUCE_SUM": (8, 1), "Algorithm_MEMSET": (8, 0), "Algorithm_MEMCPY": (16, 0),

@@ -48,13 +48,25 @@ struct IntPredict {
   double* px;
   int64_t o;
   double dm22, dm23, dm24, dm25, dm26, dm27, dm28, c0;
+  // The first product runs on the integer pipe (f64emu::mul_fast, correctly
+  // rounded); the rest of the sum contracts into FMAs on the FP64 pipe.
   __device__ void operator()(int64_t i) const {
     const double* p = px;
-    px[i] = dm28 * ld(p + i + o * 12) + dm27 * ld(p + i + o * 11) +
-            dm26 * ld(p + i + o * 10) + dm25 * ld(p + i + o * 9) +
-            dm24 * ld(p + i + o * 8) + dm23 * ld(p + i + o * 7) +
-            dm22 * ld(p + i + o * 6) +
-            c0 * (ld(p + i + o * 4) + ld(p + i + o * 5)) + ld(p + i + o * 2);
+    const double p12 = ld(p + i + o * 12);
+    bool slow = false;
+    const double first = f64emu::mul_fast(dm28, p12, slow);
+    double v = first + dm27 * ld(p + i + o * 11) +
+               dm26 * ld(p + i + o * 10) + dm25 * ld(p + i + o * 9) +
+               dm24 * ld(p + i + o * 8) + dm23 * ld(p + i + o * 7) +
+               dm22 * ld(p + i + o * 6) +
+               c0 * (ld(p + i + o * 4) + ld(p + i + o * 5)) + ld(p + i + o * 2);
+    if (__any_sync(__activemask(), slow) && slow)
+      v = dm28 * p12 + dm27 * ld(p + i + o * 11) +
+          dm26 * ld(p + i + o * 10) + dm25 * ld(p + i + o * 9) +
+          dm24 * ld(p + i + o * 8) + dm23 * ld(p + i + o * 7) +
+          dm22 * ld(p + i + o * 6) +
+          c0 * (ld(p + i + o * 4) + ld(p + i + o * 5)) + ld(p + i + o * 2);
+    px[i] = v;
   }
 };
 
