@@ -335,8 +335,8 @@ def _bandwidth_cases():
             self.div = self.zeros(nn)
             self.bytes_per_rep = 8 * self.nz + 4 * 8 * n_real_nodes + 8 * self.nz
             self.flops_per_rep = 54 * self.nz
-            # 41 per zone: halves and divisions off the FP64 pipe
-            self.fp64_instr_per_rep = 41 * self.nz
+            # 36 per zone: halves, divisions and standalone products off the FP64 pipe
+            self.fp64_instr_per_rep = 36 * self.nz
 
         def inputs(self):
             return [self.x, self.y, self.xdot, self.ydot, self.zones]

@@ -220,12 +220,20 @@ struct DelDotVec2D {
       fyi = half * (fy1 + fy2 - fy3 - fy4);
       fyj = half * (fy2 + fy3 - fy4 - fy1);
     }
-    const double rarea = fast ? f64emu::div_fast(1.0, xi * yj - xj * yi + ptiny, slow)
-                              : 1.0 / (xi * yj - xj * yi + ptiny);
+    if (fast) {
+      // the standalone products on the integer pipe too (f64emu::mul_fast);
+      // the other products contract into FMAs on the FP64 pipe
+      const double rarea = f64emu::div_fast(1.0, xi * yj - f64emu::mul_fast(xj, yi, slow) + ptiny,
+                                            slow);
+      const double dfxdx = f64emu::mul_fast(rarea, fxi * yj - f64emu::mul_fast(fxj, yi, slow), slow);
+      const double dfydy = f64emu::mul_fast(rarea, fyj * xi - f64emu::mul_fast(fyi, xj, slow), slow);
+      const double affine = f64emu::div_fast(fy1 + fy2 + fy3 + fy4, y1 + y2 + y3 + y4, slow);
+      return dfxdx + dfydy + affine;
+    }
+    const double rarea = 1.0 / (xi * yj - xj * yi + ptiny);
     const double dfxdx = rarea * (fxi * yj - fxj * yi);
     const double dfydy = rarea * (fyj * xi - fyi * xj);
-    const double affine = fast ? f64emu::div_fast(fy1 + fy2 + fy3 + fy4, y1 + y2 + y3 + y4, slow)
-                               : (fy1 + fy2 + fy3 + fy4) / (y1 + y2 + y3 + y4);
+    const double affine = (fy1 + fy2 + fy3 + fy4) / (y1 + y2 + y3 + y4);
     return dfxdx + dfydy + affine;
   }
   __device__ void operator()(int64_t ii) const {
