@@ -358,13 +358,9 @@ template <typename T, int IT, bool VEC>
 int launch_scan_it(const T* x, T* y, int64_t n, T init, char* w, cudaStream_t st) {
   constexpr int kTile = kScanBlock * IT;
   constexpr size_t kSmem = static_cast<size_t>(kTile + kTile / IT) * sizeof(T);
-  const cudaError_t attr = cudaFuncSetAttribute(
-      scan_kernel<T, IT, VEC>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-      static_cast<int>(kSmem));
-  if (attr != cudaSuccess) {
-    set_error("scan: shared memory attribute: %s", cudaGetErrorString(attr));
-    return B200_ERR_LAUNCH;
-  }
+  const int rc = allow_dynamic_smem(reinterpret_cast<const void*>(scan_kernel<T, IT, VEC>),
+                                    kSmem, "scan");
+  if (rc != B200_OK) return rc;
   const int64_t tiles = ceil_div(n, kTile);
   ScanHeader* hdr = reinterpret_cast<ScanHeader*>(w);
   TileDesc* descs = reinterpret_cast<TileDesc*>(w + 256);
@@ -376,13 +372,9 @@ int launch_scan_it(const T* x, T* y, int64_t n, T init, char* w, cudaStream_t st
 template <typename T>
 int launch_scan_pipelined(const T* x, T* y, int64_t n, T init, char* w, cudaStream_t st) {
   constexpr size_t kSmem = pipe::smem_bytes<T>();
-  const cudaError_t attr = cudaFuncSetAttribute(
-      pipe::scan_pipelined<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-      static_cast<int>(kSmem));
-  if (attr != cudaSuccess) {
-    set_error("scan: shared memory attribute: %s", cudaGetErrorString(attr));
-    return B200_ERR_LAUNCH;
-  }
+  const int rc = allow_dynamic_smem(reinterpret_cast<const void*>(pipe::scan_pipelined<T>),
+                                    kSmem, "scan");
+  if (rc != B200_OK) return rc;
   const int64_t tiles = ceil_div(n, pipe::kTile);
   const int grid = static_cast<int>(std::min<int64_t>(tiles, device_info().sm_count));
   pipe::scan_pipelined<T><<<grid, pipe::kThreads, kSmem, st>>>(

@@ -3,7 +3,9 @@
 #include "b200_f64emu.cuh"
 #include "b200_internal.cuh"
 
+#include <map>
 #include <mutex>
+#include <utility>
 #include <vector>
 
 namespace b200 {
@@ -76,6 +78,24 @@ const DeviceInfo& device_info() {
     d.device = dev;
   }
   return d;
+}
+
+int allow_dynamic_smem(const void* kernel, size_t bytes, const char* what) {
+  int dev = 0;
+  cudaGetDevice(&dev);
+  static std::mutex mu;
+  static std::map<std::pair<const void*, int>, size_t> granted;  // (kernel, device) -> bytes
+  std::lock_guard<std::mutex> lk(mu);
+  size_t& have = granted[{kernel, dev}];
+  if (bytes <= have) return B200_OK;
+  const cudaError_t e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             static_cast<int>(bytes));
+  if (e != cudaSuccess) {
+    set_error("%s: shared memory attribute (%zu bytes): %s", what, bytes, cudaGetErrorString(e));
+    return B200_ERR_LAUNCH;
+  }
+  have = bytes;
+  return B200_OK;
 }
 
 Shape resolve_1d(const b200_tune* t, int64_t units, int def_block,

@@ -29,6 +29,11 @@ int unsupported(const char* fmt, ...);
 // B200_ERR_LAUNCH with the CUDA error recorded.
 int after_launch(const char* what, int nlaunches = 1);
 
+// Raises `kernel`'s dynamic shared-memory limit to at least `bytes` on the
+// current device; the attribute is set once per kernel and device (later
+// calls are a map lookup).  Returns B200_OK or B200_ERR_LAUNCH (recorded).
+int allow_dynamic_smem(const void* kernel, size_t bytes, const char* what);
+
 // ---- device properties -----------------------------------------------------
 
 struct DeviceInfo {

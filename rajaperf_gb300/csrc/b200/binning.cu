@@ -250,13 +250,9 @@ int b200_algorithm_histogram(const int64_t* bins, int64_t n, int64_t num_bins,
     } else if (num_bins <= kSharedBins) {
       const size_t smem = static_cast<size_t>(num_bins) * sizeof(unsigned int);
       if (smem > 48 * 1024) {
-        const cudaError_t e = cudaFuncSetAttribute(histogram_shared_kernel,
-                                                   cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                                   static_cast<int>(smem));
-        if (e != cudaSuccess) {
-          set_error("b200_algorithm_histogram: %s", cudaGetErrorString(e));
-          return B200_ERR_LAUNCH;
-        }
+        const int rc = allow_dynamic_smem(reinterpret_cast<const void*>(histogram_shared_kernel),
+                                          smem, "b200_algorithm_histogram");
+        if (rc != B200_OK) return rc;
       }
       histogram_shared_kernel<<<bin_grid(n), kBlock, smem, st>>>(bins, n, num_bins, counts);
     } else {
@@ -294,13 +290,9 @@ int b200_basic_multi_reduce(const int64_t* bins, const double* data, int64_t n,
   }
   const size_t smem = static_cast<size_t>(num_bins) * kBlock * sizeof(double);
   if (smem > 48 * 1024) {
-    const cudaError_t e = cudaFuncSetAttribute(multi_reduce_private_kernel,
-                                               cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                               static_cast<int>(smem));
-    if (e != cudaSuccess) {
-      set_error("b200_basic_multi_reduce: %s", cudaGetErrorString(e));
-      return B200_ERR_LAUNCH;
-    }
+    const int rc = allow_dynamic_smem(reinterpret_cast<const void*>(multi_reduce_private_kernel),
+                                      smem, "b200_basic_multi_reduce");
+    if (rc != B200_OK) return rc;
   }
   char* w = static_cast<char*>(workspace);
   multi_reduce_private_kernel<<<bin_grid(n), kBlock, smem, st>>>(

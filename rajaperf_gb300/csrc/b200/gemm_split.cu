@@ -725,13 +725,9 @@ int b200_gemm_split(const double* A, const double* B, double* C, int64_t m, int6
   CUtensorMap tmA, tmB;
   if (!tc::encode_slices(&tmA, As, S * L.Mp, L.Kp) || !tc::encode_slices(&tmB, Bt, S * L.Np, L.Kp))
     return unsupported("b200_gemm_split: cuTensorMapEncodeTiled unavailable or rejected the slices");
-  const cudaError_t attr = cudaFuncSetAttribute(tc::ozaki_tc_kernel,
-                                                cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                                static_cast<int>(tc::kSmemBytes));
-  if (attr != cudaSuccess) {
-    set_error("b200_gemm_split: shared memory attribute: %s", cudaGetErrorString(attr));
-    return B200_ERR_LAUNCH;
-  }
+  const int attr = allow_dynamic_smem(reinterpret_cast<const void*>(tc::ozaki_tc_kernel),
+                                      tc::kSmemBytes, "b200_gemm_split");
+  if (attr != B200_OK) return attr;
   const cudaError_t ms = cudaMemsetAsync(err, 0, sizeof(unsigned int), st);
   if (ms != cudaSuccess) {
     set_error("b200_gemm_split: clearing the error word: %s", cudaGetErrorString(ms));

@@ -300,13 +300,9 @@ int b200_basic_indexlist(const double* x, int32_t* list, int64_t n, int64_t* len
   const bool vec = aligned16(x) && !(tune && tune->vec == 1);
   if (algo == 0 && vec) {
     constexpr size_t kSmem = sizeof(ilpipe::Smem) + 128;
-    const cudaError_t attr = cudaFuncSetAttribute(
-        ilpipe::indexlist_pipelined, cudaFuncAttributeMaxDynamicSharedMemorySize,
-        static_cast<int>(kSmem));
-    if (attr != cudaSuccess) {
-      set_error("b200_basic_indexlist: shared memory attribute: %s", cudaGetErrorString(attr));
-      return B200_ERR_LAUNCH;
-    }
+    const int rc = allow_dynamic_smem(reinterpret_cast<const void*>(ilpipe::indexlist_pipelined),
+                                      kSmem, "b200_basic_indexlist");
+    if (rc != B200_OK) return rc;
     const int64_t tiles = ceil_div(n, ilpipe::kTile);
     const int grid = static_cast<int>(std::min<int64_t>(tiles, device_info().sm_count));
     ilpipe::indexlist_pipelined<<<grid, ilpipe::kThreads, kSmem, st>>>(
