@@ -407,3 +407,93 @@ def test_jacobi_integer_multiply_special_values(case):
                                             ctypes.byref(t), gu.stream()))
     assert np.array_equal(gu.host(dA1).view(np.int64), gu.host(dA2).view(np.int64))
     assert np.array_equal(gu.host(dB1).view(np.int64), gu.host(dB2).view(np.int64))
+
+
+def close_special(got, want, rtol=1e-12):
+    """NaNs and infinities in the same places (infinities with the same
+    sign), the finite values within rtol."""
+    got, want = np.asarray(got), np.asarray(want)
+    assert np.array_equal(np.isnan(got), np.isnan(want)), "NaN positions differ"
+    inf = np.isinf(want)
+    assert np.array_equal(np.isinf(got), inf), "infinity positions differ"
+    assert np.array_equal(got[inf], want[inf]), "infinity signs differ"
+    fin = np.isfinite(want)
+    if fin.any():
+        close(got[fin], want[fin], rtol)
+
+
+def test_hydro_2d_division_special_values():
+    """BODY1 divides without the FP64 pipe and falls back to the FP64 divide
+    for zero, subnormal and non-finite operands or quotients: zero
+    denominators (+-inf and 0/0) and subnormal numerators must come out as
+    the suite's loop gives them."""
+    kn, jn = 70, 67
+    rng = np.random.default_rng(21)
+    arrs = [rng.uniform(0.5, 1.5, kn * jn) for _ in range(11)]
+    za, zb, zm, zp, zq, zr = arrs[0], arrs[1], arrs[2], arrs[3], arrs[4], arrs[5]
+    zm[rng.integers(0, kn * jn, 300)] = 0.0          # zero denominators
+    zp[rng.integers(0, kn * jn, 200)] = zq[0] * 0.0  # zero numerator terms
+    zr[rng.integers(0, kn * jn, 100)] = 1e-310       # subnormal factors
+    d = [dev(a) for a in arrs]
+    rp.check(lib().b200_lcals_hydro_2d(*[t.data_ptr() for t in d], 0.0041, 0.0037, kn, jn,
+                                       None, gu.stream()))
+    ref = [a.copy() for a in arrs]
+    oracle.call("oracle_hydro_2d_rep", *ref, 0.0041, 0.0037, kn, jn)
+    for g, w in zip(d[:2], ref[:2]):  # za, zb: BODY1's quotients
+        close_special(gu.host(g), w)
+
+
+def test_del_dot_vec_2d_division_special_values():
+    """Degenerate zones (equal corners: zero area with ptiny 0, zero y sums)
+    take the FP64 divide: +-inf and NaN where the suite's loop gives them."""
+    rng = np.random.default_rng(22)
+    jp, nn = 37, 37 * 40
+    x, y, xd, yd = (rng.uniform(0.5, 1.5, nn) for _ in range(4))
+    x[rng.integers(0, nn, 150)] = 0.0
+    y[rng.integers(0, nn, 150)] = 0.0
+    x[:jp * 4] = 1.0   # the first rows: equal corners, zero area
+    y[:jp * 4] = 0.0   # and zero y sums
+    div = np.zeros(nn)
+    zones = np.arange(0, nn - jp - 1).astype(np.int64)
+    dd, dx, dy, dxd, dyd, dz = dev(div), dev(x), dev(y), dev(xd), dev(yd), dev(zones)
+    rp.check(lib().b200_apps_del_dot_vec_2d(dx.data_ptr(), dy.data_ptr(), dxd.data_ptr(),
+                                            dyd.data_ptr(), dd.data_ptr(), dz.data_ptr(),
+                                            zones.size, jp, 0.0, 0.5, None, gu.stream()))
+    oracle.call("oracle_del_dot_vec_2d_rep", x, y, xd, yd, div, zones, zones.size, jp, 0.0, 0.5)
+    # Zones whose area cancels between two equal nonzero products are left
+    # out: there the FMA-contracted GPU area keeps the products' rounding
+    # residual while the suite's loop (each product rounded) gets exactly 0.
+    c1, c2, c3, c4 = zones + 1, zones + 1 + jp, zones + jp, zones
+    xi = 0.5 * (x[c1] + x[c2] - x[c3] - x[c4])
+    xj = 0.5 * (x[c2] + x[c3] - x[c4] - x[c1])
+    yi = 0.5 * (y[c1] + y[c2] - y[c3] - y[c4])
+    yj = 0.5 * (y[c2] + y[c3] - y[c4] - y[c1])
+    cancel = (xi * yj == xj * yi) & (xi * yj != 0.0)
+    keep = np.ones(nn, dtype=bool)
+    keep[zones[cancel]] = False
+    assert keep.sum() > nn // 2
+    close_special(gu.host(dd)[keep], div[keep])
+
+
+def test_planckian_division_special_values():
+    """u / v and x / (exp(y) - 1) without the FP64 pipe, with the FP64 divide
+    for zero, subnormal and non-finite cases (v = 0, u = v = 0, huge y)."""
+    rng = np.random.default_rng(23)
+    n = 50000
+    x, u, v = rng.uniform(0.5, 1.5, n), rng.uniform(0.5, 1.5, n), rng.uniform(0.5, 1.5, n)
+    v[rng.integers(0, n, 300)] = 0.0
+    u[rng.integers(0, n, 300)] = 0.0
+    u[rng.integers(0, n, 300)] = 1e-310
+    v[rng.integers(0, n, 300)] = 1e-3     # exp(y) overflows for large u / v
+    u[rng.integers(0, n, 300)] = 900.0
+    dx, du, dv = dev(x), dev(u), dev(v)
+    torch = gu.torch_cuda()
+    dy = torch.zeros(n, dtype=torch.float64, device="cuda")
+    dw = torch.zeros(n, dtype=torch.float64, device="cuda")
+    rp.check(lib().b200_lcals_planckian(dx.data_ptr(), dy.data_ptr(), du.data_ptr(),
+                                        dv.data_ptr(), dw.data_ptr(), n, None, gu.stream()))
+    with np.errstate(divide="ignore", invalid="ignore", over="ignore"):
+        want_y = u / v
+        want_w = x / (np.exp(want_y) - 1.0)
+    close_special(gu.host(dy), want_y)            # a quotient: correctly rounded both ways
+    close_special(gu.host(dw), want_w, rtol=1e-14)  # exp may differ in the last bit
