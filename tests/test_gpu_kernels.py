@@ -93,6 +93,12 @@ def test_energy_all_branches(n):
     arrs[5] = np.zeros(n)                     # q_new
     arrs[0] = np.zeros(n)                     # e_new
     arrs[11][::7] = -5.0                      # pbvc: drive ssc <= tiny
+    # zeros and subnormals in delvc and work: the exponent-move products and
+    # the integer-pipe division by 6 fall back to the FP64 pipe for them
+    arrs[2][::11] = 0.0
+    arrs[2][5::13] = 3e-310
+    arrs[7][::17] = 0.0
+    arrs[7][3::19] = -2e-309
     scal = (0.3, 0.01, -0.5, 0.02)
     d = [dev(a) for a in arrs]
     rp.check(lib().b200_apps_energy(*[t.data_ptr() for t in d], *scal, n, None, gu.stream()))
