@@ -10,8 +10,8 @@ of the suite).  One "step" runs every kernel of the workload once.
                   [--workload bandwidth_stencil|stream]
 
 * value: kernels timed with CUDA events on the launching stream, inputs
-  resident in HBM, L2 flushed before every kernel (a 256 MiB write, then a
-  256 MiB read of another buffer so no dirty flush lines remain).
+  resident in HBM, L2 flushed before every kernel (a 256 MiB write, then two
+  256 MiB reads of another buffer so no dirty flush lines remain).
 * e2e: the same metric through the C ABI with host buffers: each step copies
   the kernel's inputs from pinned host memory, runs it and reads the
   result back, all inside the timed region.
@@ -335,8 +335,9 @@ def _bandwidth_cases():
             self.div = self.zeros(nn)
             self.bytes_per_rep = 8 * self.nz + 4 * 8 * n_real_nodes + 8 * self.nz
             self.flops_per_rep = 54 * self.nz
-            # 36 per zone: halves, divisions and standalone products off the FP64 pipe
-            self.fp64_instr_per_rep = 36 * self.nz
+            # 34 per zone (31 DADD, 3 DFMA): halves, divisions and standalone
+            # products off the FP64 pipe
+            self.fp64_instr_per_rep = 34 * self.nz
 
         def inputs(self):
             return [self.x, self.y, self.xdot, self.ydot, self.zones]
@@ -799,16 +800,19 @@ def run_gpu(args, rank, world):
     stream = torch.cuda.current_stream()
     s = stream.cuda_stream
     # L2 flush before every kernel: a write of a 256 MiB buffer evicts the
-    # kernel's inputs and outputs, then a read of a second 256 MiB buffer
-    # evicts the flush's own dirty lines, so that their write-back to HBM is
+    # kernel's inputs and outputs, then two reads of a second 256 MiB buffer
+    # evict the flush's own dirty lines, so that their write-back to HBM is
     # not charged to the timed kernel (at 2^24 elements it would add up to
-    # ~128 MB of writes to a kernel that moves 134-268 MB).
+    # ~128 MB of writes to a kernel that moves 134-268 MB).  One read was not
+    # enough: FIRST_MIN at 2^24 took 31.4 us after write + one read, 28.7 us
+    # after write + two reads, 27.2 us back to back with no flush at all.
     flush_w = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device="cuda")
     flush_r = torch.zeros(L2_FLUSH_BYTES // 4, dtype=torch.float32, device="cuda")
     fp64 = measure_fp64_peak(torch, rp, stream)
 
     def l2_flush():
         flush_w.zero_()
+        flush_r.sum()
         flush_r.sum()
 
     def one_step(timed_events=None):
@@ -1187,8 +1191,8 @@ def main():
     desc = WORKLOADS[args.workload]["description"]
     config = {"workload": args.workload, "description": desc,
               "kernels": [k for k, _ in workload_kernels(args.workload, args.kernels)],
-              "l2": "flushed before every kernel: 256 MiB write, then 256 MiB read of a "
-                    "second buffer (no dirty flush lines left to write back)",
+              "l2": "flushed before every kernel: 256 MiB write, then two 256 MiB reads "
+                    "of a second buffer (no dirty flush lines left to write back)",
               "init": f"uniform [0.5,1.5) seed {args.seed}"}
     metric = "geomean % of measured HBM copy peak over kernels (suite Bytes/rep)"
 

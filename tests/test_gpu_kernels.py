@@ -269,6 +269,53 @@ def test_first_min_exact(case):
         assert got_val == float(x[want]) or (np.isnan(got_val) and np.isnan(x[want]))
 
 
+@pytest.mark.parametrize("n", [(1 << 20) + 4095, (1 << 20) + 1, 3 * (1 << 20) + 17])
+@pytest.mark.parametrize("case", ["tail", "last_tile", "tie_tile_tail", "tie_ctas", "uniform"])
+@pytest.mark.parametrize("tune", ["default", "grid7", "algo1", "unaligned"])
+def test_first_min_tails(n, case, tune):
+    """Sizes past 2^20 that are not multiples of 4096 (and odd): the minimum in
+    the ragged end, ties between distant tiles and between a tile and the end,
+    the default grid, a 7-CTA grid (long grid-stride loops), an algo tuning and
+    an unaligned start (8-byte loads instead of pairs)."""
+    rng = np.random.default_rng(n + len(case))
+    x = rng.uniform(0.5, 1.5, n)
+    whole = (n // 4096) * 4096
+    if case == "tail":
+        x[n - 1] = -1.0
+    elif case == "last_tile":
+        x[whole - 1] = -1.0
+        x[n - 1] = -1.0
+    elif case == "tie_tile_tail":
+        x[n - 1] = -1.0
+        x[4096 * 3 + 5] = -1.0
+    elif case == "tie_ctas":
+        for i in (4096 * 200 + 7, 4096 * 1 + 4095, 4096 * 5 + 2, whole - 4096):
+            x[i] = -4.0
+    torch = gu.torch_cuda()
+    loc = torch.full((1,), -2, dtype=torch.int64, device="cuda")
+    val = torch.zeros(1, dtype=torch.float64, device="cuda")
+    wsb = lib().b200_reduce_workspace_bytes(n, None)
+    w = ws(wsb)
+    dx = dev(x)
+    ptr, m, xs = dx.data_ptr(), n, x
+    t = None
+    if tune == "grid7":
+        t = rp.Tune(grid_blocks=7)
+    elif tune == "algo1":
+        t = rp.Tune(algo=1)
+    elif tune == "unaligned":
+        ptr, m, xs = ptr + 8, n - 1, x[1:]
+    want = int(np.argmin(xs))
+    want = want if xs[want] < xs[0] else 0
+    for _ in range(3):
+        rp.check(lib().b200_lcals_first_min(ptr, m, float(xs[0]), 0, loc.data_ptr(),
+                                            val.data_ptr(), w.data_ptr(), wsb,
+                                            ctypes.byref(t) if t is not None else None,
+                                            gu.stream()))
+        assert int(gu.host(loc)[0]) == want
+        assert float(gu.host(val)[0]) == float(xs[want])
+
+
 @pytest.mark.parametrize("n", [0, 1, 1000, 1 << 22])
 def test_reduce_sum(n):
     rng = np.random.default_rng(n)
