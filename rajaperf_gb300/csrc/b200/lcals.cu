@@ -153,21 +153,23 @@ hydro2d_body1(double* __restrict__ za, double* __restrict__ zb,
               int64_t kn, int64_t jn) {
   const int64_t j = 1 + static_cast<int64_t>(blockIdx.x) * BS + threadIdx.x;
   if (j >= jn - 1) return;
-  // The two divisions run on the integer and FP32 pipes (f64emu::div_fast,
-  // correctly rounded, bit-identical to the FP64 divide); the FP64 pipe keeps
-  // the 12 adds and multiplies of a point.  A thread that met a zero,
-  // subnormal or non-finite operand or quotient rewrites its points with the
-  // FP64 divide after the loop.
+  // The two divisions and the two products run on the integer and FP32
+  // pipes (f64emu::div_fast and f64emu::mul_fast, correctly rounded,
+  // bit-identical to the FP64 divide and multiply); the FP64 pipe keeps the
+  // 10 adds of a point.  A thread that met a zero, subnormal or non-finite
+  // operand, product or quotient rewrites its points with the FP64 pipe after
+  // the loop.
   bool slow = false;
   for (int64_t k = 1 + blockIdx.y; k < kn - 1; k += gridDim.y) {
     const int64_t c = j + k * jn;
     za[c] = f64emu::div_fast(
-        (ld(zp + c - 1 + jn) + ld(zq + c - 1 + jn) - ld(zp + c - 1) - ld(zq + c - 1)) *
-            (ld(zr + c) + ld(zr + c - 1)),
+        f64emu::mul_fast(
+            ld(zp + c - 1 + jn) + ld(zq + c - 1 + jn) - ld(zp + c - 1) - ld(zq + c - 1),
+            ld(zr + c) + ld(zr + c - 1), slow),
         ld(zm + c - 1) + ld(zm + c - 1 + jn), slow);
     zb[c] = f64emu::div_fast(
-        (ld(zp + c - 1) + ld(zq + c - 1) - ld(zp + c) - ld(zq + c)) *
-            (ld(zr + c) + ld(zr + c - jn)),
+        f64emu::mul_fast(ld(zp + c - 1) + ld(zq + c - 1) - ld(zp + c) - ld(zq + c),
+                         ld(zr + c) + ld(zr + c - jn), slow),
         ld(zm + c) + ld(zm + c - 1), slow);
   }
   if (__any_sync(__activemask(), slow) && slow) {
@@ -195,10 +197,22 @@ hydro2d_body23(const double* __restrict__ za, const double* __restrict__ zb,
     const double za0 = ld(za + c), za1 = ld(za + c - 1);
     const double zb0 = ld(zb + c), zb1 = ld(zb + c + jn);
     const double zz0 = ld(zz + c), zr0 = ld(zr + c);
-    const double u = zu[c] + s * (za0 * (zz0 - ld(zz + c + 1)) - za1 * (zz0 - ld(zz + c - 1)) -
-                                  zb0 * (zz0 - ld(zz + c - jn)) + zb1 * (zz0 - ld(zz + c + jn)));
-    const double v = zv[c] + s * (za0 * (zr0 - ld(zr + c + 1)) - za1 * (zr0 - ld(zr + c - 1)) -
-                                  zb0 * (zr0 - ld(zr + c - jn)) + zb1 * (zr0 - ld(zr + c + jn)));
+    const double du1 = zz0 - ld(zz + c + 1), du2 = zz0 - ld(zz + c - 1);
+    const double du3 = zz0 - ld(zz + c - jn), du4 = zz0 - ld(zz + c + jn);
+    const double dv1 = zr0 - ld(zr + c + 1), dv2 = zr0 - ld(zr + c - 1);
+    const double dv3 = zr0 - ld(zr + c - jn), dv4 = zr0 - ld(zr + c + jn);
+    // zu + s * (((za0 du1 - za1 du2) - zb0 du3) + zb1 du4), left to right as
+    // the suite writes it: the leading product on the integer pipe
+    // (f64emu::mul_fast; recomputed by the FP64 pipe for operands outside its
+    // fast path), the others and s * (...) as FMAs.
+    bool slow = false;
+    double pu = f64emu::mul_fast(za0, du1, slow), pv = f64emu::mul_fast(za0, dv1, slow);
+    if (__any_sync(__activemask(), slow) && slow) {
+      pu = za0 * du1;
+      pv = za0 * dv1;
+    }
+    const double u = fma(s, fma(zb1, du4, fma(-zb0, du3, fma(-za1, du2, pu))), zu[c]);
+    const double v = fma(s, fma(zb1, dv4, fma(-zb0, dv3, fma(-za1, dv2, pv))), zv[c]);
     zu[c] = u;
     zv[c] = v;
     zrout[c] = zr0 + t * u;
