@@ -103,7 +103,9 @@ int b200_probe_dfma(double* out, int32_t iters, int64_t* fma_count,
  * of HYDRO_2D and DEL_DOT_VEC_2D, with quotients near rounding midpoints, near
  * 1 and extreme divisor significands added), 7 = a < 0 (INDEXLIST's
  * integer test; signed zeros, infinities and NaNs added), 8 = a * b on the
- * integer pipe (JACOBI_2D's a * 0.2 for every other pair); adds to
+ * integer pipe (JACOBI_2D's a * 0.2 for every other pair), 9 = a + b for a b
+ * below a's last bit (DEL_DOT_VEC_2D's + ptiny; exponent gaps 50-60 around
+ * the fast path's bound of 55, powers of two, special values added); adds to
  * *mismatches (device) the number of
  * results whose bits differ from the FP64 pipe's.  Not in the reference. */
 int b200_f64emu_selftest(int64_t n, uint64_t seed, int32_t op,

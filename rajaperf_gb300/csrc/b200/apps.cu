@@ -223,9 +223,12 @@ struct DelDotVec2D {
     if (fast) {
       // the standalone products on the integer pipe too (f64emu::mul_fast);
       // each a * b - c is one FMA on the FP64 pipe, written out (the
-      // compiler left two of the three as a multiply and a subtract)
-      const double rarea =
-          f64emu::div_fast(1.0, fma(xi, yj, -f64emu::mul_fast(xj, yi, slow)) + ptiny, slow);
+      // compiler left two of the three as a multiply and a subtract); + ptiny
+      // gives the area back unchanged unless the area is within 2^55 of
+      // ptiny (f64emu::add_negligible)
+      const double rarea = f64emu::div_fast(
+          1.0, f64emu::add_negligible(fma(xi, yj, -f64emu::mul_fast(xj, yi, slow)), ptiny, slow),
+          slow);
       const double dfxdx =
           f64emu::mul_fast(rarea, fma(fxi, yj, -f64emu::mul_fast(fxj, yi, slow)), slow);
       const double dfydy =

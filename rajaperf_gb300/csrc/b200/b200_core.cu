@@ -376,7 +376,7 @@ __global__ void f64emu_check_kernel(int64_t n, uint64_t seed, int op,
         break;
       }
     }
-    if (op == 7 && (i % 7) == 6) {  // x < 0: signed zeros, infinities, NaNs
+    if ((op == 7 || op == 9) && (i % 7) == 6) {  // signed zeros, infinities, NaNs
       const uint64_t sp[6] = {0x0ULL, 0x8000000000000000ULL, 0x7FF0000000000000ULL,
                               0xFFF0000000000000ULL, 0x7FF8000000000001ULL,
                               0xFFF8000000000000ULL};
@@ -404,6 +404,14 @@ __global__ void f64emu_check_kernel(int64_t n, uint64_t seed, int op,
         }
         default: break;
       }
+    }
+    if (op == 9 && (i % 5) != 0 && (i % 5) != 3) {  // a + tiny b: gaps 50-60 around 55
+      const uint64_t e = ((ra >> 12) % 1900u) + 70u;
+      const uint64_t gap = 50u + (rb >> 58) % 11u;
+      A = (ra & 0x800FFFFFFFFFFFFFULL) | (e << 52);
+      if ((ra >> 11) & 1u) A &= 0xFFF0000000000000ULL;  // a power of two: the tighter side
+      B = (rb & 0x800FFFFFFFFFFFFFULL) | ((e - gap) << 52);
+      if ((rb >> 11) & 1u) B |= 0x000FFFFFFFFFFFFFULL;  // b at the top of its binade
     }
     const double a = __longlong_as_double(static_cast<long long>(A));
     const double b = __longlong_as_double(static_cast<long long>(B));
@@ -434,6 +442,11 @@ __global__ void f64emu_check_kernel(int64_t n, uint64_t seed, int op,
     } else if (op == 7) {  // x < 0 as INDEXLIST tests it
       want = a < 0.0 ? 1.0 : 0.0;
       got = b200::f64emu::lt_zero(a) ? 1.0 : 0.0;
+    } else if (op == 9) {  // a + b for b below a's last bit, as DEL_DOT_VEC_2D's + ptiny
+      want = __dadd_rn(a, b);
+      bool slow = false;
+      got = b200::f64emu::add_negligible(a, b, slow);
+      if (slow) got = __dadd_rn(a, b);
     } else {  // a * b on the integer pipe; every other pair as JACOBI_2D's a * 0.2
       const double c = (i & 1) ? 0.2 : b;
       want = __dmul_rn(a, c);
@@ -452,7 +465,7 @@ __global__ void f64emu_check_kernel(int64_t n, uint64_t seed, int op,
 
 extern "C" int b200_f64emu_selftest(int64_t n, uint64_t seed, int32_t op,
                                     unsigned long long* mismatches, b200_stream_t stream) {
-  if (n < 0 || !mismatches || op < 0 || op > 8) return invalid("b200_f64emu_selftest: bad args");
+  if (n < 0 || !mismatches || op < 0 || op > 9) return invalid("b200_f64emu_selftest: bad args");
   const int blocks = device_info().sm_count * 8;
   f64emu_check_kernel<<<blocks, 256, 0, as_stream(stream)>>>(n, seed, op, mismatches);
   return after_launch("b200_f64emu_selftest");

@@ -161,12 +161,26 @@ __device__ __forceinline__ double mul_fast(double a, double b, bool& slow) {
 template <int K>
 __device__ __forceinline__ double mul_pow2_fast(double x, bool& slow) {
   static_assert(K > -1000 && K < 1000 && K != 0, "small nonzero K");
-  constexpr unsigned kLo = (K < 0) ? 1u - K : 1u;        // smallest exponent kept normal
-  constexpr unsigned kHi = (K > 0) ? 2046u - K : 2046u;  // largest
+  constexpr unsigned kLo = (K < 0) ? static_cast<unsigned>(1 - K) : 1u;  // smallest kept normal
+  constexpr unsigned kHi = (K > 0) ? static_cast<unsigned>(2046 - K) : 2046u;  // largest
   const int hi = __double2hiint(x);
   const unsigned e = (static_cast<unsigned>(hi) >> 20) & 0x7ffu;
   slow |= (e - kLo) > (kHi - kLo);
   return __hiloint2double(hi + K * (1 << 20), __double2loint(x));
+}
+
+// a + b for a b far below a's last bit, without the FP64 pipe: returns a,
+// which is RN(a + b) when a is normal and a's biased exponent exceeds b's by
+// at least 55.  Then |b| < 2^(eb - 1022) <= 2^(ea - 1077), a quarter of a's
+// ulp, below half the gap to a's neighbours on either side (the gap below a
+// power of two is half an ulp), so rounding to nearest gives back a.  `slow`
+// is set for every other pair (a zero, subnormal, infinite or NaN a; an
+// infinite or NaN b; a gap under 55), for which the caller adds natively.
+__device__ __forceinline__ double add_negligible(double a, double b, bool& slow) {
+  const unsigned ea = (static_cast<unsigned>(__double2hiint(a)) >> 20) & 0x7ffu;
+  const unsigned eb = (static_cast<unsigned>(__double2hiint(b)) >> 20) & 0x7ffu;
+  slow |= (ea - 1u >= 2046u) || (ea < eb + 55u);
+  return a;
 }
 
 // x < 0.0 on the integer pipe: the sign bit is set and the magnitude is

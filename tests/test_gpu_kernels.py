@@ -361,13 +361,14 @@ def test_null_pointer_rejected(fn, args):
     assert f(*argv) == rp.B200_ERR_INVALID_ARG
 
 
-@pytest.mark.parametrize("op", [0, 1, 2, 3, 4, 5, 6, 7, 8])
+@pytest.mark.parametrize("op", [0, 1, 2, 3, 4, 5, 6, 7, 8, 9])
 def test_integer_pipe_fp64_is_bit_exact(op):
     """The integer-pipe add/sub/mul used by the mixed-pipe stencils, the
     exponent-shift products by 0.5, 0.125 and 2 of DEL_DOT_VEC_2D and HEAT_3D,
     the FP64-free division of HYDRO_2D and DEL_DOT_VEC_2D, INDEXLIST's integer
-    x < 0 test and JACOBI_2D's integer-pipe multiply, against the FP64 pipe on
-    16M operands (every class of double; 64M for the division)."""
+    x < 0 test, the integer-pipe multiply of JACOBI_2D, HYDRO_2D and
+    DEL_DOT_VEC_2D and DEL_DOT_VEC_2D's + ptiny, against the FP64 pipe on 16M
+    operands (every class of double; 64M for the division)."""
     torch = gu.torch_cuda()
     bad = torch.zeros(1, dtype=torch.int64, device="cuda")
     n = (1 << 26) if op == 6 else (1 << 24)
