@@ -234,10 +234,9 @@ def _bandwidth_cases():
             self.bytes_per_rep = (8 * (4 * n + 4 * n + 4 * (kn - 2) * (jn - 2)) +
                                   8 * 6 * (kn - 2) * (jn - 2))
             self.flops_per_rep = 44 * (kn - 2) * (jn - 2)
-            # BODY1 10 per point (its divisions and products run on the
-            # integer and FP32 pipes), BODY2+BODY3 18 per point (the leading
-            # product of u and of v on the integer pipe)
-            self.fp64_instr_per_rep = 28 * (kn - 2) * (jn - 2)
+            # ncu: BODY1 10 per point (its divisions and products run on the
+            # integer and FP32 pipes), BODY2+BODY3 20 per point
+            self.fp64_instr_per_rep = 30 * (kn - 2) * (jn - 2)
 
         def inputs(self):
             return self.arr[2:9]

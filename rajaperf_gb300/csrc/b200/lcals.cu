@@ -202,17 +202,12 @@ hydro2d_body23(const double* __restrict__ za, const double* __restrict__ zb,
     const double dv1 = zr0 - ld(zr + c + 1), dv2 = zr0 - ld(zr + c - 1);
     const double dv3 = zr0 - ld(zr + c - jn), dv4 = zr0 - ld(zr + c + jn);
     // zu + s * (((za0 du1 - za1 du2) - zb0 du3) + zb1 du4), left to right as
-    // the suite writes it: the leading product on the integer pipe
-    // (f64emu::mul_fast; recomputed by the FP64 pipe for operands outside its
-    // fast path), the others and s * (...) as FMAs.
-    bool slow = false;
-    double pu = f64emu::mul_fast(za0, du1, slow), pv = f64emu::mul_fast(za0, dv1, slow);
-    if (__any_sync(__activemask(), slow) && slow) {
-      pu = za0 * du1;
-      pv = za0 * dv1;
-    }
-    const double u = fma(s, fma(zb1, du4, fma(-zb0, du3, fma(-za1, du2, pu))), zu[c]);
-    const double v = fma(s, fma(zb1, dv4, fma(-zb0, dv3, fma(-za1, dv2, pv))), zv[c]);
+    // the suite writes it, the products after the first and s * (...) as
+    // FMAs.  (The leading product on the integer pipe gained nothing: its
+    // two-instruction fallback is compiled as predicated FP64 multiplies,
+    // which occupy the FP64 pipe like executed ones.)
+    const double u = fma(s, fma(zb1, du4, fma(-zb0, du3, fma(-za1, du2, za0 * du1))), zu[c]);
+    const double v = fma(s, fma(zb1, dv4, fma(-zb0, dv3, fma(-za1, dv2, za0 * dv1))), zv[c]);
     zu[c] = u;
     zv[c] = v;
     zrout[c] = zr0 + t * u;
