@@ -12,6 +12,7 @@
 // counter and advances the epoch.  Every wait is bounded; a wait that gives up sets the error word of
 // the workspace header (byte offset 16) and the call's results are invalid.
 #include "b200_internal.cuh"
+#include "b200_fma_form.cuh"
 #include "b200_async.cuh"
 #include "b200_lookback.cuh"
 #include "b200_pipeline.cuh"
@@ -421,10 +422,13 @@ template <int BS, int IT>
 __global__ void __launch_bounds__(BS)
 reduce_sum_kernel(const double* __restrict__ x, int64_t n, double init,
                   double* __restrict__ out, double* __restrict__ partials,
-                  unsigned int* __restrict__ counter) {
+                  unsigned int* __restrict__ counter, int zero) {
   __shared__ double smem[BS / 32];
   __shared__ bool last_flag;
   double s = 0.0;
+  // s + v as a register-operand FMA (fform: bit-identical, full FP64 rate
+  // where DADD gets 5/6 of it); `zero` is 0 at run time
+  const double one = fform::regs(zero).one;
   for (int64_t t0 = static_cast<int64_t>(blockIdx.x) * (BS * IT); t0 < n;
        t0 += static_cast<int64_t>(gridDim.x) * (BS * IT)) {
     double v[IT];
@@ -434,7 +438,7 @@ reduce_sum_kernel(const double* __restrict__ x, int64_t n, double init,
       v[u] = (i < n) ? __ldg(x + i) : 0.0;
     }
 #pragma unroll
-    for (int u = 0; u < IT; ++u) s += v[u];
+    for (int u = 0; u < IT; ++u) s = fma(v[u], one, s);  // s + v[u]
   }
   s = block_sum<BS>(s, smem);
   if (threadIdx.x == 0) partials[blockIdx.x] = s;
@@ -494,7 +498,7 @@ int b200_algorithm_reduce_sum(const double* x, int64_t n, double sum_init, doubl
   double* partials = reinterpret_cast<double*>(static_cast<char*>(workspace) + 256);
   cudaStream_t st = as_stream(stream);
   B200_DISPATCH_BLOCK(block, BS, B200_DISPATCH_ITEMS(items, IT,
-    reduce_sum_kernel<BS, IT><<<grid, BS, 0, st>>>(x, n, sum_init, sum, partials, counter)));
+    reduce_sum_kernel<BS, IT><<<grid, BS, 0, st>>>(x, n, sum_init, sum, partials, counter, 0)));
   return after_launch("b200_algorithm_reduce_sum");
 }
 

@@ -7,6 +7,7 @@
 // bodies stay in registers.
 #include "b200_internal.cuh"
 #include "b200_f64emu.cuh"
+#include "b200_fma_form.cuh"
 #include "b200_map.cuh"
 
 using namespace b200;
@@ -195,30 +196,38 @@ struct DelDotVec2D {
   const int64_t* __restrict__ real_zones;
   int64_t jp;
   double ptiny, half;
+  int zero;  // 0 at run time (fform)
   __device__ __forceinline__ double body(double x1, double x2, double x3, double x4,
                                         double y1, double y2, double y3, double y4,
                                         double fx1, double fx2, double fx3, double fx4,
                                         double fy1, double fy2, double fy3, double fy4,
                                         bool fast, bool& slow) const {
     double xi, xj, yi, yj, fxi, fxj, fyi, fyj;
+    // the fast path's adds are register-operand FMAs (fform, bit-identical),
+    // which the FP64 pipe issues at its full rate where DADD gets 5/6 of it
+    const fform::Regs fr = fform::regs(zero);
+    // ((a + b) - c) - d, left to right as the suite writes it
+    auto s4 = [&](double a, double b, double c, double d) {
+      return fform::sub(fform::sub(fform::add(a, b, fr), c, fr), d, fr);
+    };
     if (fast) {
-      xi = f64emu::mul_pow2_fast<-1>(x1 + x2 - x3 - x4, slow);
-      xj = f64emu::mul_pow2_fast<-1>(x2 + x3 - x4 - x1, slow);
-      yi = f64emu::mul_pow2_fast<-1>(y1 + y2 - y3 - y4, slow);
-      yj = f64emu::mul_pow2_fast<-1>(y2 + y3 - y4 - y1, slow);
-      fxi = f64emu::mul_pow2_fast<-1>(fx1 + fx2 - fx3 - fx4, slow);
-      fxj = f64emu::mul_pow2_fast<-1>(fx2 + fx3 - fx4 - fx1, slow);
-      fyi = f64emu::mul_pow2_fast<-1>(fy1 + fy2 - fy3 - fy4, slow);
-      fyj = f64emu::mul_pow2_fast<-1>(fy2 + fy3 - fy4 - fy1, slow);
-    } else {
-      xi = half * (x1 + x2 - x3 - x4);
-      xj = half * (x2 + x3 - x4 - x1);
-      yi = half * (y1 + y2 - y3 - y4);
-      yj = half * (y2 + y3 - y4 - y1);
-      fxi = half * (fx1 + fx2 - fx3 - fx4);
-      fxj = half * (fx2 + fx3 - fx4 - fx1);
-      fyi = half * (fy1 + fy2 - fy3 - fy4);
-      fyj = half * (fy2 + fy3 - fy4 - fy1);
+      xi = f64emu::mul_pow2_fast<-1>(s4(x1, x2, x3, x4), slow);
+      xj = f64emu::mul_pow2_fast<-1>(s4(x2, x3, x4, x1), slow);
+      yi = f64emu::mul_pow2_fast<-1>(s4(y1, y2, y3, y4), slow);
+      yj = f64emu::mul_pow2_fast<-1>(s4(y2, y3, y4, y1), slow);
+      fxi = f64emu::mul_pow2_fast<-1>(s4(fx1, fx2, fx3, fx4), slow);
+      fxj = f64emu::mul_pow2_fast<-1>(s4(fx2, fx3, fx4, fx1), slow);
+      fyi = f64emu::mul_pow2_fast<-1>(s4(fy1, fy2, fy3, fy4), slow);
+      fyj = f64emu::mul_pow2_fast<-1>(s4(fy2, fy3, fy4, fy1), slow);
+    } else {  // the same sums as the fast path (shared, not recomputed)
+      xi = half * s4(x1, x2, x3, x4);
+      xj = half * s4(x2, x3, x4, x1);
+      yi = half * s4(y1, y2, y3, y4);
+      yj = half * s4(y2, y3, y4, y1);
+      fxi = half * s4(fx1, fx2, fx3, fx4);
+      fxj = half * s4(fx2, fx3, fx4, fx1);
+      fyi = half * s4(fy1, fy2, fy3, fy4);
+      fyj = half * s4(fy2, fy3, fy4, fy1);
     }
     if (fast) {
       // the standalone products on the integer pipe too (f64emu::mul_fast);
@@ -233,15 +242,18 @@ struct DelDotVec2D {
           f64emu::mul_fast(rarea, fma(fxi, yj, -f64emu::mul_fast(fxj, yi, slow)), slow);
       const double dfydy =
           f64emu::mul_fast(rarea, fma(fyj, xi, -f64emu::mul_fast(fyi, xj, slow)), slow);
-      const double affine = f64emu::div_fast(fy1 + fy2 + fy3 + fy4, y1 + y2 + y3 + y4, slow);
-      return dfxdx + dfydy + affine;
+      const double affine = f64emu::div_fast(
+          fform::add(fform::add(fform::add(fy1, fy2, fr), fy3, fr), fy4, fr),
+          fform::add(fform::add(fform::add(y1, y2, fr), y3, fr), y4, fr), slow);
+      return fform::add(fform::add(dfxdx, dfydy, fr), affine, fr);
     }
     // the same FMAs as the fast path, so both give the same bits on its inputs
     const double rarea = 1.0 / (fma(xi, yj, -(xj * yi)) + ptiny);
     const double dfxdx = rarea * fma(fxi, yj, -(fxj * yi));
     const double dfydy = rarea * fma(fyj, xi, -(fyi * xj));
-    const double affine = (fy1 + fy2 + fy3 + fy4) / (y1 + y2 + y3 + y4);
-    return dfxdx + dfydy + affine;
+    const double affine = fform::add(fform::add(fform::add(fy1, fy2, fr), fy3, fr), fy4, fr) /
+                          fform::add(fform::add(fform::add(y1, y2, fr), y3, fr), y4, fr);
+    return fform::add(fform::add(dfxdx, dfydy, fr), affine, fr);
   }
   __device__ void operator()(int64_t ii) const {
     const int64_t i = ld(real_zones + ii);
@@ -318,10 +330,10 @@ int b200_apps_del_dot_vec_2d(const double* x, const double* y, const double* xdo
   // two zones per thread by default: 1.3% faster than four at 4096^2 zones
   if (half == 0.5)
     return launch_map1d("b200_apps_del_dot_vec_2d",
-                        DelDotVec2D<true>{x, y, xdot, ydot, div, real_zones, jp, ptiny, half},
+                        DelDotVec2D<true>{x, y, xdot, ydot, div, real_zones, jp, ptiny, half, 0},
                         n_real_zones, tune, as_stream(stream), 256, 2);
   return launch_map1d("b200_apps_del_dot_vec_2d",
-                      DelDotVec2D<false>{x, y, xdot, ydot, div, real_zones, jp, ptiny, half},
+                      DelDotVec2D<false>{x, y, xdot, ydot, div, real_zones, jp, ptiny, half, 0},
                       n_real_zones, tune, as_stream(stream));
 }
 

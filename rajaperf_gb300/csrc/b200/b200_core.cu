@@ -295,14 +295,24 @@ namespace {
 // Sixteen independent FMA chains per thread (enough to cover the pipe's
 // latency at full occupancy); out[] receives one value per thread so the
 // chains are live.  `out` must hold probe_threads() doubles.
+// a and b are copied into per-thread registers (through threadIdx.x and an
+// argument that is zero at run time): a DFMA with a kernel-argument operand
+// (constant bank or uniform register) issues at 5/6 of the rate of one whose
+// operands are all per-thread registers (501 vs 595 G/s measured), and the
+// probe is meant to find the pipe's full rate.
 __global__ void __launch_bounds__(256) dfma_probe_kernel(double* out, double a, double b,
-                                                         int iters) {
+                                                         int iters, int zero) {
+  const unsigned long long z = threadIdx.x & static_cast<unsigned>(zero);
+  const double ar = __longlong_as_double(static_cast<long long>(
+      static_cast<unsigned long long>(__double_as_longlong(a)) + z));
+  const double br = __longlong_as_double(static_cast<long long>(
+      static_cast<unsigned long long>(__double_as_longlong(b)) + z));
   double x[16];
 #pragma unroll
   for (int c = 0; c < 16; ++c) x[c] = threadIdx.x * 1e-3 + c;
   for (int i = 0; i < iters; ++i) {
 #pragma unroll
-    for (int c = 0; c < 16; ++c) x[c] = fma(x[c], a, b);
+    for (int c = 0; c < 16; ++c) x[c] = fma(x[c], ar, br);
   }
   double s = 0.0;
 #pragma unroll
@@ -321,7 +331,7 @@ int64_t b200_probe_dfma_threads(void) {
 int b200_probe_dfma(double* out, int32_t iters, int64_t* fma_count, b200_stream_t stream) {
   if (!out || iters <= 0 || !fma_count) return invalid("b200_probe_dfma: bad args");
   int blocks = device_info().sm_count * 8;
-  dfma_probe_kernel<<<blocks, 256, 0, as_stream(stream)>>>(out, 0.999999, 1e-7, iters);
+  dfma_probe_kernel<<<blocks, 256, 0, as_stream(stream)>>>(out, 0.999999, 1e-7, iters, 0);
   *fma_count = static_cast<int64_t>(blocks) * 256 * 16 * iters;
   return after_launch("b200_probe_dfma");
 }

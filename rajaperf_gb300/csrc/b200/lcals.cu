@@ -4,6 +4,7 @@
 // macro's operation order.
 #include "b200_internal.cuh"
 #include "b200_f64emu.cuh"
+#include "b200_fma_form.cuh"
 #include "b200_map.cuh"
 #include "b200_reduce.cuh"
 
@@ -11,28 +12,40 @@ using namespace b200;
 
 namespace {
 
-// lcals/HYDRO_1D.hpp:30
+// lcals/HYDRO_1D.hpp:30.  Register-operand FMAs throughout (fform: the
+// product r * z as an FMA with -0, the coefficients in per-thread registers),
+// which the FP64 pipe issues at its full rate; `zero` is 0 at run time.
 struct Hydro1D {
   double* __restrict__ x;
   const double* __restrict__ y;
   const double* __restrict__ z;
   double q, r, t;
+  int zero;
   __device__ void operator()(int64_t i) const {
-    x[i] = q + ld(y + i) * (r * ld(z + i + 10) + t * ld(z + i + 11));
+    const fform::Regs fr = fform::regs(zero);
+    x[i] = fma(ld(y + i), fma(fform::reg(t, zero), ld(z + i + 11),
+                              fform::mul(fform::reg(r, zero), ld(z + i + 10), fr)),
+               fform::reg(q, zero));
   }
 };
 
-// lcals/EOS.hpp:33
+// lcals/EOS.hpp:33: x = u + r (z + r y) + t (u3 + r (u2 + r u1) + t (u6 +
+// q (u5 + q u4))), each a + b * c an FMA as the compiler contracts it, with
+// q, r, t in per-thread registers (fform::reg) so that every FMA has
+// register operands; `zero` is 0 at run time.
 struct Eos {
   double* __restrict__ x;
   const double* __restrict__ y;
   const double* __restrict__ z;
   const double* __restrict__ u;
   double q, r, t;
+  int zero;
   __device__ void operator()(int64_t i) const {
-    x[i] = ld(u + i) + r * (ld(z + i) + r * ld(y + i)) +
-           t * (ld(u + i + 3) + r * (ld(u + i + 2) + r * ld(u + i + 1)) +
-                t * (ld(u + i + 6) + q * (ld(u + i + 5) + q * ld(u + i + 4))));
+    const double rr = fform::reg(r, zero), tr = fform::reg(t, zero), qr = fform::reg(q, zero);
+    const double a = fma(rr, fma(rr, ld(y + i), ld(z + i)), ld(u + i));
+    const double b = fma(rr, fma(rr, ld(u + i + 1), ld(u + i + 2)), ld(u + i + 3));
+    const double c = fma(qr, fma(qr, ld(u + i + 4), ld(u + i + 5)), ld(u + i + 6));
+    x[i] = fma(tr, fma(tr, c, b), a);
   }
 };
 
@@ -150,27 +163,33 @@ __global__ void __launch_bounds__(BS)
 hydro2d_body1(double* __restrict__ za, double* __restrict__ zb,
               const double* __restrict__ zm, const double* __restrict__ zp,
               const double* __restrict__ zq, const double* __restrict__ zr,
-              int64_t kn, int64_t jn) {
+              int64_t kn, int64_t jn, int zero) {
   const int64_t j = 1 + static_cast<int64_t>(blockIdx.x) * BS + threadIdx.x;
   if (j >= jn - 1) return;
   // The two divisions and the two products run on the integer and FP32
   // pipes (f64emu::div_fast and f64emu::mul_fast, correctly rounded,
   // bit-identical to the FP64 divide and multiply); the FP64 pipe keeps the
-  // 10 adds of a point.  A thread that met a zero, subnormal or non-finite
-  // operand, product or quotient rewrites its points with the FP64 pipe after
-  // the loop.
+  // 10 adds of a point, as register-operand FMAs (fform, bit-identical, full
+  // FP64 rate where DADD gets 5/6 of it; `zero` is 0 at run time).  A thread
+  // that met a zero, subnormal or non-finite operand, product or quotient
+  // rewrites its points with the FP64 pipe after the loop.
+  const fform::Regs fr = fform::regs(zero);
   bool slow = false;
   for (int64_t k = 1 + blockIdx.y; k < kn - 1; k += gridDim.y) {
     const int64_t c = j + k * jn;
     za[c] = f64emu::div_fast(
         f64emu::mul_fast(
-            ld(zp + c - 1 + jn) + ld(zq + c - 1 + jn) - ld(zp + c - 1) - ld(zq + c - 1),
-            ld(zr + c) + ld(zr + c - 1), slow),
-        ld(zm + c - 1) + ld(zm + c - 1 + jn), slow);
+            fform::sub(fform::sub(fform::add(ld(zp + c - 1 + jn), ld(zq + c - 1 + jn), fr),
+                                  ld(zp + c - 1), fr),
+                       ld(zq + c - 1), fr),
+            fform::add(ld(zr + c), ld(zr + c - 1), fr), slow),
+        fform::add(ld(zm + c - 1), ld(zm + c - 1 + jn), fr), slow);
     zb[c] = f64emu::div_fast(
-        f64emu::mul_fast(ld(zp + c - 1) + ld(zq + c - 1) - ld(zp + c) - ld(zq + c),
-                         ld(zr + c) + ld(zr + c - jn), slow),
-        ld(zm + c) + ld(zm + c - 1), slow);
+        f64emu::mul_fast(
+            fform::sub(fform::sub(fform::add(ld(zp + c - 1), ld(zq + c - 1), fr), ld(zp + c), fr),
+                       ld(zq + c), fr),
+            fform::add(ld(zr + c), ld(zr + c - jn), fr), slow),
+        fform::add(ld(zm + c), ld(zm + c - 1), fr), slow);
   }
   if (__any_sync(__activemask(), slow) && slow) {
     for (int64_t k = 1 + blockIdx.y; k < kn - 1; k += gridDim.y) {
@@ -189,29 +208,36 @@ hydro2d_body23(const double* __restrict__ za, const double* __restrict__ zb,
                const double* __restrict__ zr, double* __restrict__ zu,
                double* __restrict__ zv, const double* __restrict__ zz,
                double* __restrict__ zrout, double* __restrict__ zzout, double s,
-               double t, int64_t kn, int64_t jn) {
+               double t, int64_t kn, int64_t jn, int zero) {
   const int64_t j = 1 + static_cast<int64_t>(blockIdx.x) * BS + threadIdx.x;
   if (j >= jn - 1) return;
+  // Every FP64 instruction a register-operand FMA (fform: the differences and
+  // the leading products, s and t in per-thread registers), which the FP64
+  // pipe issues at its full rate; `zero` is 0 at run time.  (The leading
+  // product on the integer pipe gained nothing: its two-instruction fallback
+  // is compiled as predicated FP64 multiplies, which occupy the FP64 pipe
+  // like executed ones.)
+  const fform::Regs fr = fform::regs(zero);
+  const double sr = fform::reg(s, zero), tr = fform::reg(t, zero);
   for (int64_t k = 1 + blockIdx.y; k < kn - 1; k += gridDim.y) {
     const int64_t c = j + k * jn;
     const double za0 = ld(za + c), za1 = ld(za + c - 1);
     const double zb0 = ld(zb + c), zb1 = ld(zb + c + jn);
     const double zz0 = ld(zz + c), zr0 = ld(zr + c);
-    const double du1 = zz0 - ld(zz + c + 1), du2 = zz0 - ld(zz + c - 1);
-    const double du3 = zz0 - ld(zz + c - jn), du4 = zz0 - ld(zz + c + jn);
-    const double dv1 = zr0 - ld(zr + c + 1), dv2 = zr0 - ld(zr + c - 1);
-    const double dv3 = zr0 - ld(zr + c - jn), dv4 = zr0 - ld(zr + c + jn);
+    const double du1 = fform::sub(zz0, ld(zz + c + 1), fr), du2 = fform::sub(zz0, ld(zz + c - 1), fr);
+    const double du3 = fform::sub(zz0, ld(zz + c - jn), fr), du4 = fform::sub(zz0, ld(zz + c + jn), fr);
+    const double dv1 = fform::sub(zr0, ld(zr + c + 1), fr), dv2 = fform::sub(zr0, ld(zr + c - 1), fr);
+    const double dv3 = fform::sub(zr0, ld(zr + c - jn), fr), dv4 = fform::sub(zr0, ld(zr + c + jn), fr);
     // zu + s * (((za0 du1 - za1 du2) - zb0 du3) + zb1 du4), left to right as
-    // the suite writes it, the products after the first and s * (...) as
-    // FMAs.  (The leading product on the integer pipe gained nothing: its
-    // two-instruction fallback is compiled as predicated FP64 multiplies,
-    // which occupy the FP64 pipe like executed ones.)
-    const double u = fma(s, fma(zb1, du4, fma(-zb0, du3, fma(-za1, du2, za0 * du1))), zu[c]);
-    const double v = fma(s, fma(zb1, dv4, fma(-zb0, dv3, fma(-za1, dv2, za0 * dv1))), zv[c]);
+    // the suite writes it, the products after the first and s * (...) as FMAs
+    const double u = fma(sr, fma(zb1, du4, fma(-zb0, du3, fma(-za1, du2, fform::mul(za0, du1, fr)))),
+                         zu[c]);
+    const double v = fma(sr, fma(zb1, dv4, fma(-zb0, dv3, fma(-za1, dv2, fform::mul(za0, dv1, fr)))),
+                         zv[c]);
     zu[c] = u;
     zv[c] = v;
-    zrout[c] = zr0 + t * u;
-    zzout[c] = zz0 + t * v;
+    zrout[c] = fma(tr, u, zr0);
+    zzout[c] = fma(tr, v, zz0);
   }
 }
 
@@ -328,7 +354,7 @@ int b200_lcals_hydro_1d(double* x, const double* y, const double* z, double q,
                         double r, double t, int64_t n, const b200_tune* tune,
                         b200_stream_t stream) {
   if (n < 0 || (n > 0 && (!x || !y || !z))) return invalid("b200_lcals_hydro_1d: bad args");
-  return launch_map1d("b200_lcals_hydro_1d", Hydro1D{x, y, z, q, r, t}, n, tune,
+  return launch_map1d("b200_lcals_hydro_1d", Hydro1D{x, y, z, q, r, t, 0}, n, tune,
                       as_stream(stream));
 }
 
@@ -336,7 +362,7 @@ int b200_lcals_eos(double* x, const double* y, const double* z, const double* u,
                    double q, double r, double t, int64_t n, const b200_tune* tune,
                    b200_stream_t stream) {
   if (n < 0 || (n > 0 && (!x || !y || !z || !u))) return invalid("b200_lcals_eos: bad args");
-  return launch_map1d("b200_lcals_eos", Eos{x, y, z, u, q, r, t}, n, tune,
+  return launch_map1d("b200_lcals_eos", Eos{x, y, z, u, q, r, t, 0}, n, tune,
                       as_stream(stream));
 }
 
@@ -389,9 +415,9 @@ int b200_lcals_hydro_2d(double* za, double* zb, const double* zm, const double* 
   cudaStream_t st = as_stream(stream);
   dim3 grid = rows_grid(jn, kn, bs);
   B200_DISPATCH_BLOCK(bs, BS,
-    hydro2d_body1<BS><<<grid, BS, 0, st>>>(za, zb, zm, zp, zq, zr, kn, jn);
+    hydro2d_body1<BS><<<grid, BS, 0, st>>>(za, zb, zm, zp, zq, zr, kn, jn, 0);
     hydro2d_body23<BS><<<grid, BS, 0, st>>>(za, zb, zr, zu, zv, zz, zrout, zzout, s, t,
-                                            kn, jn));
+                                            kn, jn, 0));
   return after_launch("b200_lcals_hydro_2d", 2);
 }
 

@@ -11,6 +11,7 @@
 // into registers while the current one is consumed.  Each C element's dot
 // product runs over k in increasing order, as the suite's loop does.
 #include "b200_f64emu.cuh"
+#include "b200_fma_form.cuh"
 #include "b200_internal.cuh"
 
 using namespace b200;
@@ -56,9 +57,12 @@ jacobi2d_step(const double* __restrict__ src, double* __restrict__ dst, int64_t 
 // jacobi2d_step.  With the multiply off the FP64 pipe, the independent rows
 // hide its integer latency: 165 -> 133 us per half-step at 4096^2 (one point
 // per thread with the FP64 multiply: 165 us; with the integer multiply: 158).
+// The four adds are register-operand FMAs (fform::add, bit-identical), which
+// the FP64 pipe issues at its full rate where DADD gets 5/6 of it: 133 ->
+// 115 us.  `zero` is 0 at run time.
 template <int BX, int R>
 __global__ void __launch_bounds__(BX)
-jacobi2d_rows(const double* __restrict__ src, double* __restrict__ dst, int64_t N) {
+jacobi2d_rows(const double* __restrict__ src, double* __restrict__ dst, int64_t N, int zero) {
   const int64_t j = 1 + static_cast<int64_t>(blockIdx.x) * BX + threadIdx.x;
   if (j >= N - 1) return;
   const int64_t i0 = 1 + static_cast<int64_t>(blockIdx.y) * R;
@@ -75,9 +79,12 @@ jacobi2d_rows(const double* __restrict__ src, double* __restrict__ dst, int64_t 
       lft[r] = ld(p + (r + 1) * N - 1);
       rgt[r] = ld(p + (r + 1) * N + 1);
     }
+    const fform::Regs fr = fform::regs(zero);
 #pragma unroll
     for (int r = 0; r < R; ++r)
-      q[r * N] = f64emu::mul_fast(col[r + 1] + lft[r] + rgt[r] + col[r + 2] + col[r], 0.2, slow);
+      q[r * N] = f64emu::mul_fast(
+          fform::add(fform::add(fform::add(fform::add(col[r + 1], lft[r], fr), rgt[r], fr),
+                                col[r + 2], fr), col[r], fr), 0.2, slow);
   } else {
     for (int64_t r = 0; r < rows; ++r) {
       const double* c = p + (r + 1) * N;
@@ -96,24 +103,30 @@ jacobi2d_rows(const double* __restrict__ src, double* __restrict__ dst, int64_t 
 // Index k + N*(j + N*i); threads run along k (contiguous).
 template <int BX, int BY>
 __global__ void __launch_bounds__(BX * BY)
-heat3d_step(const double* __restrict__ S, double* __restrict__ D, int64_t N) {
+heat3d_step(const double* __restrict__ S, double* __restrict__ D, int64_t N, int zero) {
   const int64_t k = 1 + static_cast<int64_t>(blockIdx.x) * BX + threadIdx.x;
   const int64_t j = 1 + static_cast<int64_t>(blockIdx.y) * BY + threadIdx.y;
   if (k >= N - 1 || j >= N - 1) return;
   const int64_t NN = N * N;
   // 2.0 * a and 0.125 * v are exact: exponent moves on the integer pipe, so
-  // the FP64 pipe keeps only the 9 adds of a point.  A thread that met a
-  // zero, subnormal or non-finite value rewrites its points with the FP64
-  // products after the loop (the same results, bit for bit).
+  // the FP64 pipe keeps only the 9 adds of a point, issued as register-operand
+  // FMAs (fform, bit-identical; full rate where DADD gets 5/6 of it).  A
+  // thread that met a zero, subnormal or non-finite value rewrites its points
+  // with the FP64 products after the loop (the same results, bit for bit).
+  // `zero` is 0 at run time.
+  const fform::Regs fr = fform::regs(zero);
   bool slow = false;
   for (int64_t i = 1 + blockIdx.z; i < N - 1; i += gridDim.z) {
     const int64_t c = k + N * (j + N * i);
     const double a = ld(S + c);
     const double a2 = f64emu::mul_pow2_fast<1>(a, slow);
-    const double ti = f64emu::mul_pow2_fast<-3>(ld(S + c + NN) - a2 + ld(S + c - NN), slow);
-    const double tj = f64emu::mul_pow2_fast<-3>(ld(S + c + N) - a2 + ld(S + c - N), slow);
-    const double tk = f64emu::mul_pow2_fast<-3>(ld(S + c + 1) - a2 + ld(S + c - 1), slow);
-    D[c] = ti + tj + tk + a;
+    const double ti = f64emu::mul_pow2_fast<-3>(
+        fform::add(fform::sub(ld(S + c + NN), a2, fr), ld(S + c - NN), fr), slow);
+    const double tj = f64emu::mul_pow2_fast<-3>(
+        fform::add(fform::sub(ld(S + c + N), a2, fr), ld(S + c - N), fr), slow);
+    const double tk = f64emu::mul_pow2_fast<-3>(
+        fform::add(fform::sub(ld(S + c + 1), a2, fr), ld(S + c - 1), fr), slow);
+    D[c] = fform::add(fform::add(fform::add(ti, tj, fr), tk, fr), a, fr);
   }
   if (__any_sync(__activemask(), slow) && slow) {
     for (int64_t i = 1 + blockIdx.z; i < N - 1; i += gridDim.z) {
@@ -400,8 +413,8 @@ int b200_polybench_jacobi_2d(double* A, double* B, int64_t N, int64_t tsteps,
     const dim3 g(static_cast<unsigned>(ceil_div(N - 2, BX)), static_cast<unsigned>(gy));
     auto run = [&](auto kernel) {
       for (int64_t t = 0; t < tsteps; ++t) {
-        kernel<<<g, BX, 0, st>>>(A, B, N);
-        kernel<<<g, BX, 0, st>>>(B, A, N);
+        kernel<<<g, BX, 0, st>>>(A, B, N, 0);
+        kernel<<<g, BX, 0, st>>>(B, A, N, 0);
       }
     };
     if (rows == 2) run(jacobi2d_rows<BX, 2>);
@@ -443,8 +456,8 @@ int b200_polybench_heat_3d(double* A, double* B, int64_t N, int64_t tsteps,
          static_cast<unsigned>(gz));
   if (ceil_div(N - 2, BY) > 65535) return invalid("b200_polybench_heat_3d: N too large");
   for (int64_t t = 0; t < tsteps; ++t) {
-    heat3d_step<BX, BY><<<g, dim3(BX, BY), 0, st>>>(A, B, N);
-    heat3d_step<BX, BY><<<g, dim3(BX, BY), 0, st>>>(B, A, N);
+    heat3d_step<BX, BY><<<g, dim3(BX, BY), 0, st>>>(A, B, N, 0);
+    heat3d_step<BX, BY><<<g, dim3(BX, BY), 0, st>>>(B, A, N, 0);
   }
   return after_launch("b200_polybench_heat_3d", static_cast<int>(2 * tsteps));
 }
