@@ -146,30 +146,41 @@ heat3d_step(const double* __restrict__ S, double* __restrict__ D, int64_t N, int
 template <int BX, int BY>
 __global__ void __launch_bounds__(BX * BY)
 fdtd2d_e(double* __restrict__ ex, double* __restrict__ ey, const double* __restrict__ hz,
-         const double* __restrict__ fict, int64_t t, int64_t nx, int64_t ny) {
+         const double* __restrict__ fict, int64_t t, int64_t nx, int64_t ny, int zero) {
   const int64_t j = static_cast<int64_t>(blockIdx.x) * BX + threadIdx.x;
   if (j >= ny) return;
   const double f = ld(fict + t);
+  // register-operand FMAs (fform: the differences, and e - 0.5 d as the FMA
+  // the compiler contracts it to, with -0.5 in a per-thread register), the
+  // FP64 pipe's full-rate form; `zero` is 0 at run time
+  const fform::Regs fr = fform::regs(zero);
+  const double mhalf = fform::reg(-0.5, zero);
   for (int64_t i = static_cast<int64_t>(blockIdx.y) * BY + threadIdx.y; i < nx;
        i += static_cast<int64_t>(gridDim.y) * BY) {
     const int64_t c = j + i * ny;
     const double h = ld(hz + c);
     if (i == 0) ey[c] = f;
-    else ey[c] = ey[c] - 0.5 * (h - ld(hz + c - ny));
-    if (j >= 1) ex[c] = ex[c] - 0.5 * (h - ld(hz + c - 1));
+    else ey[c] = fma(mhalf, fform::sub(h, ld(hz + c - ny), fr), ey[c]);
+    if (j >= 1) ex[c] = fma(mhalf, fform::sub(h, ld(hz + c - 1), fr), ex[c]);
   }
 }
 
 template <int BX, int BY>
 __global__ void __launch_bounds__(BX * BY)
 fdtd2d_h(const double* __restrict__ ex, const double* __restrict__ ey,
-         double* __restrict__ hz, int64_t nx, int64_t ny) {
+         double* __restrict__ hz, int64_t nx, int64_t ny, int zero) {
   const int64_t j = static_cast<int64_t>(blockIdx.x) * BX + threadIdx.x;
   if (j >= ny - 1) return;
+  const fform::Regs fr = fform::regs(zero);
+  const double m07 = fform::reg(-0.7, zero);
   for (int64_t i = static_cast<int64_t>(blockIdx.y) * BY + threadIdx.y; i < nx - 1;
        i += static_cast<int64_t>(gridDim.y) * BY) {
     const int64_t c = j + i * ny;
-    hz[c] = hz[c] - 0.7 * (ld(ex + c + 1) - ld(ex + c) + ld(ey + c + ny) - ld(ey + c));
+    // hz - 0.7 (((ex1 - ex0) + ey1) - ey0), left to right as the suite writes it
+    hz[c] = fma(m07,
+                fform::sub(fform::add(fform::sub(ld(ex + c + 1), ld(ex + c), fr), ld(ey + c + ny), fr),
+                           ld(ey + c), fr),
+                hz[c]);
   }
 }
 
@@ -474,8 +485,8 @@ int b200_polybench_fdtd_2d(double* ex, double* ey, double* hz, const double* fic
   dim3 ge = grid2(ny, nx, BX, BY);
   dim3 gh = grid2(ny - 1, nx - 1, BX, BY);
   for (int64_t t = 0; t < tsteps; ++t) {
-    fdtd2d_e<BX, BY><<<ge, dim3(BX, BY), 0, st>>>(ex, ey, hz, fict, t, nx, ny);
-    if (nx > 1 && ny > 1) fdtd2d_h<BX, BY><<<gh, dim3(BX, BY), 0, st>>>(ex, ey, hz, nx, ny);
+    fdtd2d_e<BX, BY><<<ge, dim3(BX, BY), 0, st>>>(ex, ey, hz, fict, t, nx, ny, 0);
+    if (nx > 1 && ny > 1) fdtd2d_h<BX, BY><<<gh, dim3(BX, BY), 0, st>>>(ex, ey, hz, nx, ny, 0);
   }
   int per = (nx > 1 && ny > 1) ? 2 : 1;
   return after_launch("b200_polybench_fdtd_2d", static_cast<int>(per * tsteps));
