@@ -910,7 +910,7 @@ def measure_gemm(torch, rp, stream, sizes=(1024, 4096, 8192), seed=4793):
         B = torch.rand(n, n, dtype=torch.float64, device="cuda", generator=g) * 2 - 1
         C0 = torch.rand(n, n, dtype=torch.float64, device="cuda", generator=g) * 2 - 1
         ws_bytes = L.b200_gemm_split_workspace_bytes(n, n, n, None)
-        ws = torch.empty(ws_bytes, dtype=torch.uint8, device="cuda")
+        ws = torch.zeros(ws_bytes, dtype=torch.uint8, device="cuda")
         res = {"n": n}
         for name, fn in (("native", lambda C: L.b200_gemm_f64(A.data_ptr(), B.data_ptr(),
                                                              C.data_ptr(), n, n, n, 1.5, 1.2,
@@ -976,7 +976,7 @@ def measure_3mm(torch, rp, stream, n=2048, seed=4793):
     E, F, G = (torch.zeros(n, n, dtype=torch.float64, device="cuda") for _ in range(3))
     Es, Fs, Gs = (torch.zeros(n, n, dtype=torch.float64, device="cuda") for _ in range(3))
     wb = L.b200_gemm_split_workspace_bytes(n, n, n, None)
-    ws = torch.empty(wb, dtype=torch.uint8, device="cuda")
+    ws = torch.zeros(wb, dtype=torch.uint8, device="cuda")
     P = lambda t: t.data_ptr()
 
     def native():

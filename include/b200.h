@@ -50,7 +50,11 @@ typedef enum b200_status {
  * vec: elements per vector memory access (1, 2).  grid_blocks: CTA count
  * cap (0 = one tile per CTA).  tile_*: stencil tile shape.  time_block:
  * stencil time steps fused per launch.  algo: kernel-specific algorithm
- * selector (documented per entry point). */
+ * selector (documented per entry point).  wait_limit_us: limit of every
+ * bounded device-side wait of the call (scan and index-list lookback and
+ * stage waits, split-GEMM pipeline waits); 0 = the library default (2 s for
+ * the scan and index list, 1 s for the split GEMM).  A wait that runs out
+ * sets the workspace's error word, which b200_workspace_status() reports. */
 typedef struct b200_tune {
   int32_t block_size;
   int32_t items;
@@ -61,7 +65,8 @@ typedef struct b200_tune {
   int32_t tile_z;
   int32_t time_block;
   int32_t algo;
-  int32_t reserved[3];
+  int32_t wait_limit_us;
+  int32_t reserved[2];
 } b200_tune;
 
 typedef struct b200_caps {
@@ -85,6 +90,17 @@ int b200_device_caps(b200_caps* out);
 
 /* Number of kernels this library has launched since it was loaded. */
 int64_t b200_launch_count(void);
+
+/* Status of the calls that used a workspace with bounded device-side waits
+ * (b200_algorithm_scan*, b200_basic_indexlist*, b200_gemm_split): waits for
+ * `stream`, then reads the workspace's error word.  Returns B200_OK, or
+ * B200_ERR_TIMEOUT when a wait of an earlier call on that workspace gave up
+ * (its results are invalid); in that case the whole workspace is zero-filled
+ * again (stream-ordered, then waited for), so it is ready for the next call.
+ * The reference has no device-side waits to report: its Base_CUDA variants
+ * check every CUDA call and abort on an error (common/CudaDataUtils.hpp:67).
+ * This call synchronises the stream, unlike the kernel entry points. */
+int b200_workspace_status(void* workspace, size_t workspace_bytes, b200_stream_t stream);
 
 /* FP64 pipe probe: launches 16 independent fma chains of `iters` steps in
  * each of b200_probe_dfma_threads() threads (out must hold that many
@@ -180,8 +196,11 @@ int b200_stream_dot(const double* a, const double* b, int64_t n,
  * shape needing more returns B200_ERR_WORKSPACE.  The call allocates nothing
  * and clears the scratch counter itself.  All calls share the array, so
  * calls that overlap on the GPU race and must be ordered by the caller.  The
- * first call on a device looks the array's address up (cudaGetSymbolAddress)
- * and should come before any stream capture that contains this call. */
+ * first call in a CUDA context looks the array's address up
+ * (cudaGetSymbolAddress) and caches it under that context's unique id, so a
+ * context created later (after a device reset, or a second context on the
+ * device) gets its own lookup; that first call should come before any stream
+ * capture that contains this call. */
 size_t b200_stream_dot_static_max_scratch_bytes(void);
 int b200_stream_dot_static(const double* a, const double* b, int64_t n,
                            double dot_init, double* dot_accum,
@@ -350,10 +369,11 @@ size_t b200_gemm_split_workspace_bytes(int64_t m, int64_t n, int64_t k,
  * tensor cores; the weighted sum is formed in FP64.  k <= 8192 (the bound
  * under which the FP32 accumulation stays exact).  tune->algo picks the
  * engine: 0 (default) tcgen05 MMA with TMA-fed operands and tensor-memory
- * accumulators, 1 the legacy mma.sync path.  The 32-bit word at the start of
- * the workspace is cleared by every call and set to 1 if a bounded wait of
- * the tcgen05 engine gave up (C is then invalid).  Not in the reference: the
- * split-precision form of polybench/POLYBENCH_GEMM.hpp:40-56.              */
+ * accumulators, 1 the legacy mma.sync path.  Zero the workspace once before
+ * its first use.  The 32-bit word at byte offset 16 of the workspace is set
+ * to 1 if a bounded wait of the tcgen05 engine gave up (C is then invalid);
+ * it stays set until b200_workspace_status() reports and clears it.  Not in
+ * the reference: the split-precision form of polybench/POLYBENCH_GEMM.hpp:40-56. */
 int b200_gemm_split(const double* A, const double* B, double* C, int64_t m,
                     int64_t n, int64_t k, double alpha, double beta,
                     void* workspace, size_t workspace_bytes,
@@ -365,7 +385,7 @@ int b200_gemm_split(const double* A, const double* B, double* C, int64_t m,
  * once before first use; calls leave it ready for the next call.  The
  * 32-bit word at byte offset 16 becomes nonzero if a bounded wait gave up;
  * the results of that call are invalid and the workspace must be zeroed
- * again before the next call. */
+ * again before the next call, which b200_workspace_status() does. */
 size_t b200_scan_workspace_bytes(int64_t n);
 
 /* y[i] = init + sum_{j<i} x[j] (exclusive), single-pass decoupled lookback.

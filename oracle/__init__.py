@@ -23,7 +23,6 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 # never loaded by mistake
 LIB_PATH = os.path.join(HERE, f"liboracle.{platform.machine()}.so")
 REF_EXE = os.path.join(HERE, "_ref", "rajaperf_ref")
-REF_SRC_DEFAULT = "/root/reference"
 
 
 class OracleOpts(ctypes.Structure):
@@ -58,8 +57,13 @@ def build(force: bool = False) -> str:
 def build_ref(ref_root: str | None = None) -> str | None:
     """Builds the suite's own Base_Seq code into oracle/_ref when the suite
     checkout is available; returns the executable path or None."""
-    ref_root = ref_root or os.environ.get("RAJAPERF_REF", REF_SRC_DEFAULT)
-    if not os.path.isdir(os.path.join(ref_root, "src", "common")):
+    if not ref_root:
+        # the recipe resolves the checkout (RAJAPERF_REF, else its default)
+        r = subprocess.run(["make", "-s", "--no-print-directory", "-C",
+                            os.path.join(HERE, "ref_build"), "print-ref"],
+                           capture_output=True, text=True)
+        ref_root = r.stdout.strip() if r.returncode == 0 else ""
+    if not ref_root or not os.path.isdir(os.path.join(ref_root, "src", "common")):
         return None
     subprocess.run(["make", "-s", "-j8", "-C", os.path.join(HERE, "ref_build"),
                     f"REF={ref_root}"], check=True)

@@ -37,7 +37,8 @@ class Tune(ctypes.Structure):
                 ("vec", ctypes.c_int32), ("grid_blocks", ctypes.c_int32),
                 ("tile_x", ctypes.c_int32), ("tile_y", ctypes.c_int32),
                 ("tile_z", ctypes.c_int32), ("time_block", ctypes.c_int32),
-                ("algo", ctypes.c_int32), ("reserved", ctypes.c_int32 * 3)]
+                ("algo", ctypes.c_int32), ("wait_limit_us", ctypes.c_int32),
+                ("reserved", ctypes.c_int32 * 2)]
 
 
 class Caps(ctypes.Structure):

@@ -44,7 +44,7 @@ template <> struct Vec2<long long> { using type = longlong2; };
 template <typename T, int IT, bool VEC>
 __global__ void __launch_bounds__(kScanThreads, 3)
 scan_kernel(const T* __restrict__ x, T* __restrict__ y, int64_t n, T init,
-            ScanHeader* __restrict__ hdr, TileDesc* __restrict__ descs) {
+            ScanHeader* __restrict__ hdr, TileDesc* __restrict__ descs, uint64_t limit_ns) {
   using V2 = typename Vec2<T>::type;
   constexpr int kTile = kScanBlock * IT;
   constexpr int kPadShift = (IT == 32) ? 5 : 4;
@@ -69,7 +69,7 @@ scan_kernel(const T* __restrict__ x, T* __restrict__ y, int64_t n, T init,
     // One round examines 32 * kLookbackPerLane predecessors, nearest first
     // (window slot w = j * 32 + lane is predecessor p_hi - w).
     const T exclusive =
-        (tile > 0) ? lookback_exclusive<T>(descs, tile, AGG, INC, hdr) : init;
+        (tile > 0) ? lookback_exclusive<T>(descs, tile, AGG, INC, hdr, limit_ns) : init;
     named_sync(2, kScanThreads);  // the loaders have the tile aggregate
     if (lane == 0) {
       desc_store(descs + tile, INC, to_bits<T>(exclusive + s_agg));
@@ -211,7 +211,7 @@ template <typename T>
 __global__ void __launch_bounds__(kThreads, 1)
 scan_pipelined(const T* __restrict__ x, T* __restrict__ y, int64_t n, T init,
                unsigned int tiles, ScanHeader* __restrict__ hdr,
-               TileDesc* __restrict__ descs) {
+               TileDesc* __restrict__ descs, uint64_t limit_ns) {
   using V2 = typename Vec2<T>::type;
   extern __shared__ unsigned char s_raw[];
   Smem<T>& sm = *reinterpret_cast<Smem<T>*>(
@@ -220,7 +220,7 @@ scan_pipelined(const T* __restrict__ x, T* __restrict__ y, int64_t n, T init,
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
 
   if (tid == 0) {
-    ring::init(r);
+    ring::init(r, limit_ns);
     for (int s = 0; s < kStages; ++s) mbar_init(&sm.ready[s], 1);
     sm.fail_loaded = 0;
     sm.fail_prefix = 0;
@@ -356,7 +356,8 @@ scan_pipelined(const T* __restrict__ x, T* __restrict__ y, int64_t n, T init,
 int64_t scan_tiles_max(int64_t n) { return ceil_div(n > 0 ? n : 1, kScanTileMin); }
 
 template <typename T, int IT, bool VEC>
-int launch_scan_it(const T* x, T* y, int64_t n, T init, char* w, cudaStream_t st) {
+int launch_scan_it(const T* x, T* y, int64_t n, T init, char* w, uint64_t limit_ns,
+                   cudaStream_t st) {
   constexpr int kTile = kScanBlock * IT;
   constexpr size_t kSmem = static_cast<size_t>(kTile + kTile / IT) * sizeof(T);
   const int rc = allow_dynamic_smem(reinterpret_cast<const void*>(scan_kernel<T, IT, VEC>),
@@ -366,12 +367,13 @@ int launch_scan_it(const T* x, T* y, int64_t n, T init, char* w, cudaStream_t st
   ScanHeader* hdr = reinterpret_cast<ScanHeader*>(w);
   TileDesc* descs = reinterpret_cast<TileDesc*>(w + 256);
   scan_kernel<T, IT, VEC><<<static_cast<int>(tiles), kScanThreads, kSmem, st>>>(
-      x, y, n, init, hdr, descs);
+      x, y, n, init, hdr, descs, limit_ns);
   return B200_OK;
 }
 
 template <typename T>
-int launch_scan_pipelined(const T* x, T* y, int64_t n, T init, char* w, cudaStream_t st) {
+int launch_scan_pipelined(const T* x, T* y, int64_t n, T init, char* w, uint64_t limit_ns,
+                          cudaStream_t st) {
   constexpr size_t kSmem = pipe::smem_bytes<T>();
   const int rc = allow_dynamic_smem(reinterpret_cast<const void*>(pipe::scan_pipelined<T>),
                                     kSmem, "scan");
@@ -380,7 +382,7 @@ int launch_scan_pipelined(const T* x, T* y, int64_t n, T init, char* w, cudaStre
   const int grid = static_cast<int>(std::min<int64_t>(tiles, device_info().sm_count));
   pipe::scan_pipelined<T><<<grid, pipe::kThreads, kSmem, st>>>(
       x, y, n, init, static_cast<unsigned int>(tiles), reinterpret_cast<ScanHeader*>(w),
-      reinterpret_cast<TileDesc*>(w + 256));
+      reinterpret_cast<TileDesc*>(w + 256), limit_ns);
   return B200_OK;
 }
 
@@ -405,14 +407,15 @@ int launch_scan(const char* name, const T* x, T* y, int64_t n, T init, void* ws,
   }
   char* w = static_cast<char*>(ws);
   const bool vec = aligned16(x) && aligned16(y) && !(tune && tune->vec == 1);
+  const uint64_t lim = wait_limit_ns(tune, kDefaultWaitNs);
   int rc;
   if (algo == 0 && vec)
-    rc = launch_scan_pipelined<T>(x, y, n, init, w, st);
+    rc = launch_scan_pipelined<T>(x, y, n, init, w, lim, st);
   else
-    rc = (items == 16) ? (vec ? launch_scan_it<T, 16, true>(x, y, n, init, w, st)
-                              : launch_scan_it<T, 16, false>(x, y, n, init, w, st))
-                       : (vec ? launch_scan_it<T, 32, true>(x, y, n, init, w, st)
-                              : launch_scan_it<T, 32, false>(x, y, n, init, w, st));
+    rc = (items == 16) ? (vec ? launch_scan_it<T, 16, true>(x, y, n, init, w, lim, st)
+                              : launch_scan_it<T, 16, false>(x, y, n, init, w, lim, st))
+                       : (vec ? launch_scan_it<T, 32, true>(x, y, n, init, w, lim, st)
+                              : launch_scan_it<T, 32, false>(x, y, n, init, w, lim, st));
   if (rc != B200_OK) return rc;
   return after_launch(name);
 }

@@ -118,6 +118,7 @@ Shape resolve_1d(const b200_tune* t, int64_t units, int def_block,
 using b200::g_last_error;
 using b200::g_launches;
 using b200::invalid;
+using b200::set_error;
 using b200::after_launch;
 using b200::as_stream;
 using b200::device_info;
@@ -227,6 +228,38 @@ int b200_device_caps(b200_caps* out) {
 }
 
 int64_t b200_launch_count(void) { return g_launches.load(); }
+
+int b200_workspace_status(void* workspace, size_t workspace_bytes, b200_stream_t stream) {
+  // the error word sits at byte 16 of the 256-byte header of every
+  // workspace whose kernels wait (scan, index list, split GEMM)
+  if (!workspace || workspace_bytes < 256)
+    return invalid("b200_workspace_status: workspace of %zu bytes (needs its 256-byte header)",
+                   workspace_bytes);
+  cudaStream_t st = as_stream(stream);
+  unsigned int word = 0;
+  cudaError_t e = cudaMemcpyAsync(&word, static_cast<char*>(workspace) + 16, sizeof(word),
+                                  cudaMemcpyDeviceToHost, st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    set_error("b200_workspace_status: reading the error word: %s", cudaGetErrorString(e));
+    return B200_ERR_LAUNCH;
+  }
+  if (word == 0u) return B200_OK;
+  // a wait gave up: the tile tickets and statuses may be mid-launch, so the
+  // whole workspace starts over from zero
+  e = cudaMemsetAsync(workspace, 0, workspace_bytes, st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    set_error("b200_workspace_status: clearing the workspace: %s", cudaGetErrorString(e));
+    return B200_ERR_LAUNCH;
+  }
+  set_error("a bounded device-side wait gave up (error word %u): the results of the calls "
+            "on this workspace since its last check are invalid; the workspace was cleared",
+            word);
+  return B200_ERR_TIMEOUT;
+}
 
 int b200_init_reference(double* p, int64_t n, double factor,
                         b200_stream_t stream) {

@@ -69,6 +69,13 @@ struct Shape {
 Shape resolve_1d(const b200_tune* t, int64_t units, int def_block,
                  int def_items, int def_vec, int64_t max_grid = 0);
 
+// Limit of the bounded device-side waits of a call (b200_tune.wait_limit_us;
+// 0 or negative = `def_ns`).
+inline uint64_t wait_limit_ns(const b200_tune* t, uint64_t def_ns) {
+  return (t && t->wait_limit_us > 0) ? static_cast<uint64_t>(t->wait_limit_us) * 1000ull
+                                     : def_ns;
+}
+
 inline bool valid_block(int b) {
   return b == 64 || b == 128 || b == 256 || b == 512 || b == 1024;
 }

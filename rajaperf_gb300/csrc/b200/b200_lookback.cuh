@@ -15,10 +15,13 @@
 #include <cstdint>
 #include <cstring>
 
+#include "b200_async.cuh"
+
 namespace b200 {
 
 constexpr int kLookbackPerLane = 4;   // a lookback round covers 128 predecessors
-constexpr long long kSpinLimit = 1LL << 22;
+// Default limit of a bounded wait (b200_tune.wait_limit_us = 0).
+constexpr uint64_t kDefaultWaitNs = 2000000000ull;  // 2 s
 
 struct ScanHeader {
   // Low 32 bits: tickets taken in this launch; high 32 bits: the launch
@@ -118,15 +121,17 @@ __device__ __forceinline__ void take_tile(ScanHeader* hdr, unsigned int* s_tile,
 // nearest inclusive prefix matter; those still unpublished are re-read
 // together (one memory round trip per retry, however many are late) until
 // every one has at least its aggregate.  Values are summed in a fixed order
-// (slots per lane, then a lane tree).  A slot that stays unpublished past the
-// spin limit records the error and counts as an inclusive prefix of 0.
+// (slots per lane, then a lane tree).  A slot that stays unpublished for
+// longer than limit_ns (%globaltimer, from the first retry of the call)
+// records the error and counts as an inclusive prefix of 0.
 template <typename T, int PER_LANE = kLookbackPerLane>
 __device__ T lookback_exclusive(const TileDesc* descs, unsigned int tile,
                                 unsigned long long AGG, unsigned long long INC,
-                                ScanHeader* hdr) {
+                                ScanHeader* hdr, uint64_t limit_ns) {
   const int lane = threadIdx.x & 31;
   T acc = T(0);
   int64_t p_hi = static_cast<int64_t>(tile) - 1;  // nearest unexamined predecessor
+  uint64_t t0 = 0;                                 // time of the first retry
   for (;;) {
     unsigned long long f[PER_LANE], bits[PER_LANE];
 #pragma unroll
@@ -149,7 +154,12 @@ __device__ T lookback_exclusive(const TileDesc* descs, unsigned int tile,
       for (int j = 0; j < PER_LANE; ++j)
         pending |= (j * 32 + lane < stop) && !published(f[j], AGG, INC);
       if (!__any_sync(0xffffffffu, pending)) break;
-      const bool give_up = spins > kSpinLimit;
+      // lane 0's clock decides for the warp
+      uint64_t now = 0;
+      if (lane == 0) now = globaltimer();
+      now = __shfl_sync(0xffffffffu, now, 0);
+      if (t0 == 0) t0 = now;
+      const bool give_up = now - t0 > limit_ns;
       if (give_up && lane == 0) atomicExch(&hdr->error, 1u);
       if (spins > 16) __nanosleep(64);
 #pragma unroll

@@ -22,7 +22,7 @@
 // tile is done), so such a warp waits on drawn[s] before any other barrier
 // of stage s.  full[s] alone does not: bulk copies can complete out of order.  After
 // the last tile the producer places one end marker (tile id kEnd) per warp of
-// the role with the most warps taking alternate tiles.  Every wait is bounded (kWaitNs); one that gives up sets the
+// the role with the most warps taking alternate tiles.  Every wait is bounded (Ring::limit_ns); one that gives up sets the
 // workspace error word and stops every role of the CTA.
 #pragma once
 
@@ -39,7 +39,6 @@ constexpr int kStages = 7;
 constexpr int kLookbackWarps = 2;
 constexpr int kLookbackLanes = 8;            // 256 predecessors per lookback round
 constexpr unsigned int kEnd = 0xffffffffu;   // end marker in ticket[]
-constexpr uint64_t kWaitNs = 2000000000ull;  // 2 s
 
 template <typename In, typename Acc>
 struct Ring {
@@ -54,12 +53,13 @@ struct Ring {
   uint64_t prefix[kStages];
   uint64_t empty[kStages];
   unsigned long long epoch;
+  uint64_t limit_ns;  // limit of every bounded wait of the launch
   int abort;
 };
 
 // Thread 0, before the CTA's first barrier.
 template <typename In, typename Acc>
-__device__ __forceinline__ void init(Ring<In, Acc>& r) {
+__device__ __forceinline__ void init(Ring<In, Acc>& r, uint64_t limit_ns) {
   for (int s = 0; s < kStages; ++s) {
     mbar_init(&r.drawn[s], 1);
     mbar_init(&r.full[s], 1);
@@ -68,6 +68,7 @@ __device__ __forceinline__ void init(Ring<In, Acc>& r) {
     mbar_init(&r.empty[s], 1);
     r.phases[s] = 0u;
   }
+  r.limit_ns = limit_ns;
   r.abort = 0;
 }
 
@@ -77,7 +78,7 @@ __device__ __forceinline__ void init(Ring<In, Acc>& r) {
 template <typename In, typename Acc>
 __device__ __forceinline__ bool wait(Ring<In, Acc>& r, uint64_t* bar, uint32_t parity,
                                      ScanHeader* hdr) {
-  const bool ok = __all_sync(0xffffffffu, mbar_wait_for(bar, parity, kWaitNs));
+  const bool ok = __all_sync(0xffffffffu, mbar_wait_for(bar, parity, r.limit_ns));
   if (!ok && (threadIdx.x & 31) == 0) {
     atomicExch(&hdr->error, 1u);
     *reinterpret_cast<volatile int*>(&r.abort) = 1;
@@ -161,7 +162,9 @@ __device__ void look_back(Ring<In, Acc>& r, TileDesc* descs, Acc init, ScanHeade
     if (tile == kEnd) break;
     const unsigned long long AGG = r.epoch * 4 + 1, INC = r.epoch * 4 + 2;
     const Acc excl =
-        (tile > 0) ? lookback_exclusive<Acc, kLookbackLanes>(descs, tile, AGG, INC, hdr) : init;
+        (tile > 0) ? lookback_exclusive<Acc, kLookbackLanes>(descs, tile, AGG, INC, hdr,
+                                                             r.limit_ns)
+                   : init;
     if (!wait(r, &r.summed[s], par, hdr)) break;
     if (lane == 0) {
       desc_store(descs + tile, INC, to_bits<Acc>(excl + r.agg[s]));
@@ -187,7 +190,7 @@ template <typename In, typename Acc>
 __device__ __forceinline__ void drain(Ring<In, Acc>& r) {
   if (!r.abort) return;
   for (int s = 0; s < kStages; ++s)
-    if (r.phases[s] > 0u) mbar_wait_for(&r.full[s], (r.phases[s] - 1u) & 1u, kWaitNs);
+    if (r.phases[s] > 0u) mbar_wait_for(&r.full[s], (r.phases[s] - 1u) & 1u, r.limit_ns);
 }
 
 }  // namespace ring

@@ -32,8 +32,9 @@
 //  1 mma.sync.m16n8k16 bf16 -> fp32, 128x128 C tile per CTA (8 warps of
 //    64x32), 32-wide K stages double-buffered through shared memory with
 //    cp.async (the legacy tensor-core path, kept for comparison).
-// Every wait of the tcgen05 engine is bounded (1 s); one that gives up sets
-// the error word at the start of the workspace and the CTA winds down.
+// Every wait of the tcgen05 engine is bounded (1 s by default,
+// b200_tune.wait_limit_us); one that gives up sets the error word at byte
+// offset 16 of the workspace and the CTA winds down.
 #include "b200_internal.cuh"
 #include "b200_async.cuh"
 
@@ -175,6 +176,7 @@ struct SplitArgs {
   int64_t M, N, Mp, Np, Kp;
   double alpha, beta;
   int S;
+  uint64_t limit_ns;  // limit of every bounded wait
 };
 
 __global__ void __launch_bounds__(256, 1) ozaki_mma_kernel(SplitArgs g) {
@@ -299,7 +301,7 @@ constexpr uint32_t kStageBytes = 2 * kTileBytes;    // A + B
 constexpr int kThreads = 192;                       // TMA, MMA, 4 epilogue warps
 constexpr uint32_t kTmemCols = 512;
 constexpr uint32_t kAcc64Col = 2 * BN;              // FP64 accumulator columns 256..511
-constexpr uint64_t kWaitLimitNs = 1000000000ull;    // 1 s
+constexpr uint64_t kWaitLimitNs = 1000000000ull;    // default wait limit: 1 s
 constexpr size_t kSmemBytes = 1024 + kStages * kStageBytes + 256;
 
 // Instruction descriptor, kind::f16: D = F32 (bits 4-5 = 1), A = B = BF16
@@ -309,25 +311,26 @@ constexpr uint32_t kIdesc = (1u << 4) | (1u << 7) | (1u << 10) |
                             (static_cast<uint32_t>(BM >> 4) << 24);
 static_assert(kSmemBytes <= 232448, "shared memory budget");
 
-// Waits for the phase of parity `parity` to complete.  Gives up after 1 s
-// (setting the CTA's abort flag) or when another role has aborted.
-__device__ bool mbar_wait(uint64_t* b, uint32_t parity, volatile int* abort_flag) {
+// Waits for the phase of parity `parity` to complete.  Gives up after
+// limit_ns (setting the CTA's abort flag) or when another role has aborted.
+__device__ bool mbar_wait(uint64_t* b, uint32_t parity, volatile int* abort_flag,
+                          uint64_t limit_ns) {
   if (mbar_try_wait(b, parity)) return true;
   const uint64_t t0 = globaltimer();
   for (;;) {
     if (mbar_try_wait(b, parity)) return true;
     if (*abort_flag) return false;
-    if (globaltimer() - t0 > kWaitLimitNs) {
+    if (globaltimer() - t0 > limit_ns) {
       *abort_flag = 1;
       return false;
     }
   }
 }
 // The same wait for the wind-down after an abort: bounded, ignores the flag.
-__device__ bool mbar_wait_drain(uint64_t* b, uint32_t parity) {
+__device__ bool mbar_wait_drain(uint64_t* b, uint32_t parity, uint64_t limit_ns) {
   const uint64_t t0 = globaltimer();
   while (!mbar_try_wait(b, parity))
-    if (globaltimer() - t0 > kWaitLimitNs) return false;
+    if (globaltimer() - t0 > limit_ns) return false;
   return true;
 }
 __device__ __forceinline__ void tma_load_2d(void* dst, const CUtensorMap* map, uint64_t* bar,
@@ -418,6 +421,7 @@ struct TcArgs {
   int64_t M, N, Mp, Np, Kp;
   double alpha, beta;
   int S;
+  uint64_t limit_ns;  // limit of every bounded wait
 };
 
 __global__ void __launch_bounds__(kThreads, 1)
@@ -476,7 +480,7 @@ ozaki_tc_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__
           for (int kb = 0; kb < nkb; ++kb, ++it) {
             const int st = static_cast<int>(it % kStages);
             const uint32_t ph = (it / kStages) & 1u;
-            if (!mbar_wait(empty + st, ph ^ 1u, abort_flag)) {
+            if (!mbar_wait(empty + st, ph ^ 1u, abort_flag, g.limit_ns)) {
               ok = false;
               break;
             }
@@ -492,7 +496,7 @@ ozaki_tc_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__
         // wind-down: let the copies already issued land before the CTA exits
         const uint32_t first = it > static_cast<uint32_t>(kStages) ? it - kStages : 0u;
         for (uint32_t j = first; j < it; ++j)
-          mbar_wait_drain(full + (j % kStages), (j / kStages) & 1u);
+          mbar_wait_drain(full + (j % kStages), (j / kStages) & 1u, g.limit_ns);
       }
     }
   } else if (warp == 1) {
@@ -503,7 +507,7 @@ ozaki_tc_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__
       for (int w = 2; ok && w <= S + 1; ++w, ++wi) {
         const int buf = wi & 1;
         const uint32_t use = static_cast<uint32_t>(wi >> 1);
-        if (!mbar_wait(acc_empty + buf, (use & 1u) ^ 1u, abort_flag)) {
+        if (!mbar_wait(acc_empty + buf, (use & 1u) ^ 1u, abort_flag, g.limit_ns)) {
           ok = false;
           break;
         }
@@ -513,7 +517,7 @@ ozaki_tc_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__
         for (int s = 1; ok && s <= w - 1; ++s) {
           for (int kb = 0; kb < nkb; ++kb, ++it) {
             const int st = static_cast<int>(it % kStages);
-            if (!mbar_wait(full + st, (it / kStages) & 1u, abort_flag)) {
+            if (!mbar_wait(full + st, (it / kStages) & 1u, abort_flag, g.limit_ns)) {
               ok = false;
               break;
             }
@@ -533,7 +537,7 @@ ozaki_tc_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__
       }
       // every MMA issued by this thread completes before teardown
       umma_commit(mma_done);
-      mbar_wait_drain(mma_done, 0u);
+      mbar_wait_drain(mma_done, 0u, g.limit_ns);
     }
   } else {
     // epilogue warps 2..5 own TMEM lane quadrants (warp % 4): tile row = lane
@@ -544,7 +548,7 @@ ozaki_tc_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__
     for (int w = 2; w <= S + 1; ++w, ++wi) {
       const int buf = wi & 1;
       const uint32_t use = static_cast<uint32_t>(wi >> 1);
-      if (!mbar_wait(acc_full + buf, use & 1u, abort_flag)) {
+      if (!mbar_wait(acc_full + buf, use & 1u, abort_flag, g.limit_ns)) {
         ok = false;
         break;
       }
@@ -660,7 +664,7 @@ SplitLayout split_layout(int64_t m, int64_t n, int64_t k, int S) {
   L.Mp = round_up(m > 0 ? m : 1, TM);
   L.Np = round_up(n > 0 ? n : 1, TN);
   L.Kp = round_up(k > 0 ? k : 1, kPadK);
-  L.off_err = 0;
+  L.off_err = 16;  // the error word, at the same offset as in the scan workspaces
   L.off_ea = 256;
   L.off_eb = L.off_ea + round_up(L.Mp * 4, 256);
   L.off_as = L.off_eb + round_up(L.Np * 4, 256);
@@ -728,12 +732,8 @@ int b200_gemm_split(const double* A, const double* B, double* C, int64_t m, int6
   const int attr = allow_dynamic_smem(reinterpret_cast<const void*>(tc::ozaki_tc_kernel),
                                       tc::kSmemBytes, "b200_gemm_split");
   if (attr != B200_OK) return attr;
-  const cudaError_t ms = cudaMemsetAsync(err, 0, sizeof(unsigned int), st);
-  if (ms != cudaSuccess) {
-    set_error("b200_gemm_split: clearing the error word: %s", cudaGetErrorString(ms));
-    return B200_ERR_LAUNCH;
-  }
-  tc::TcArgs g{Ea, Eb, C, err, m, n, L.Mp, L.Np, L.Kp, alpha, beta, S};
+  tc::TcArgs g{Ea, Eb, C, err, m, n, L.Mp, L.Np, L.Kp, alpha, beta, S,
+               wait_limit_ns(tune, tc::kWaitLimitNs)};
   tc::ozaki_tc_kernel<<<dim3(static_cast<unsigned>(L.Np / tc::BN), static_cast<unsigned>(L.Mp / tc::BM)),
                         tc::kThreads, tc::kSmemBytes, st>>>(tmA, tmB, g);
   return after_launch("b200_gemm_split", 5);

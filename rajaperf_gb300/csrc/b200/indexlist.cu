@@ -42,7 +42,7 @@ template <bool VEC>
 __global__ void __launch_bounds__(kBlock, 3)
 indexlist_kernel(const double* __restrict__ x, int32_t* __restrict__ list, int64_t n,
                  int64_t* __restrict__ len, ScanHeader* __restrict__ hdr,
-                 TileDesc* __restrict__ descs) {
+                 TileDesc* __restrict__ descs, uint64_t limit_ns) {
   constexpr int kRows = VEC ? kItems / 2 : kItems;
   __shared__ long long s_woff[kBlock / 32];
   __shared__ long long s_agg;
@@ -93,7 +93,7 @@ indexlist_kernel(const double* __restrict__ x, int32_t* __restrict__ list, int64
     const long long agg = __shfl_sync(0xffffffffu, wi, kBlock / 32 - 1);
     if (tile > 0) {
       if (lane == 0) desc_store(descs + tile, AGG, to_bits<long long>(agg));
-      const long long excl = lookback_exclusive<long long>(descs, tile, AGG, INC, hdr);
+      const long long excl = lookback_exclusive<long long>(descs, tile, AGG, INC, hdr, limit_ns);
       if (lane == 0) {
         desc_store(descs + tile, INC, to_bits<long long>(excl + agg));
         s_excl = excl;
@@ -155,7 +155,8 @@ static_assert(sizeof(Smem) + 128 <= 232448, "shared memory budget");
 __global__ void __launch_bounds__(kThreads, 1)
 indexlist_pipelined(const double* __restrict__ x, int32_t* __restrict__ list, int64_t n,
                     int64_t* __restrict__ len, unsigned int tiles,
-                    ScanHeader* __restrict__ hdr, TileDesc* __restrict__ descs) {
+                    ScanHeader* __restrict__ hdr, TileDesc* __restrict__ descs,
+                    uint64_t limit_ns) {
   extern __shared__ unsigned char s_raw[];
   Smem& sm = *reinterpret_cast<Smem*>(
       (reinterpret_cast<uintptr_t>(s_raw) + 127) & ~static_cast<uintptr_t>(127));
@@ -163,7 +164,7 @@ indexlist_pipelined(const double* __restrict__ x, int32_t* __restrict__ list, in
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
 
   if (tid == 0) {
-    ring::init(r);
+    ring::init(r, limit_ns);
     sm.fail_loaded = 0;
     sm.fail_prefix = 0;
     mbar_init_fence();
@@ -298,6 +299,7 @@ int b200_basic_indexlist(const double* x, int32_t* list, int64_t n, int64_t* len
   const int algo = tune ? tune->algo : 0;
   if (algo != 0 && algo != 1) return invalid("b200_basic_indexlist: algo %d (0 or 1)", algo);
   const bool vec = aligned16(x) && !(tune && tune->vec == 1);
+  const uint64_t lim = wait_limit_ns(tune, kDefaultWaitNs);
   if (algo == 0 && vec) {
     constexpr size_t kSmem = sizeof(ilpipe::Smem) + 128;
     const int rc = allow_dynamic_smem(reinterpret_cast<const void*>(ilpipe::indexlist_pipelined),
@@ -306,14 +308,14 @@ int b200_basic_indexlist(const double* x, int32_t* list, int64_t n, int64_t* len
     const int64_t tiles = ceil_div(n, ilpipe::kTile);
     const int grid = static_cast<int>(std::min<int64_t>(tiles, device_info().sm_count));
     ilpipe::indexlist_pipelined<<<grid, ilpipe::kThreads, kSmem, st>>>(
-        x, list, n, len, static_cast<unsigned int>(tiles), hdr, descs);
+        x, list, n, len, static_cast<unsigned int>(tiles), hdr, descs, lim);
     return after_launch("b200_basic_indexlist");
   }
   const unsigned tiles = static_cast<unsigned>(tiles_of(n));
   if (vec)
-    indexlist_kernel<true><<<tiles, kBlock, 0, st>>>(x, list, n, len, hdr, descs);
+    indexlist_kernel<true><<<tiles, kBlock, 0, st>>>(x, list, n, len, hdr, descs, lim);
   else
-    indexlist_kernel<false><<<tiles, kBlock, 0, st>>>(x, list, n, len, hdr, descs);
+    indexlist_kernel<false><<<tiles, kBlock, 0, st>>>(x, list, n, len, hdr, descs, lim);
   return after_launch("b200_basic_indexlist");
 }
 

@@ -16,10 +16,14 @@
 // kernel (cudaMemsetAsync, stream-ordered), so a call never depends on what
 // an earlier call left behind.
 //
-// The device address of the array is looked up once per device with
-// cudaGetSymbolAddress, on the first call made while that device is current.
-// That first call on a device should therefore come before any stream
-// capture that contains the entry point.
+// The device address of the array is looked up with cudaGetSymbolAddress on
+// the first call made in a CUDA context (the device's primary context, or
+// any other context the caller makes current) and cached under that
+// context's process-unique id (cuCtxGetId), so a call in a context created
+// later -- after a cudaDeviceReset, or a second context on the same device --
+// looks the address up again instead of reusing a stale one.  The first call
+// in a context should therefore come before any stream capture that
+// contains the entry point.
 #include "b200_internal.cuh"
 #include "b200_reduce.cuh"
 
@@ -38,29 +42,78 @@ static __device__ __align__(256) unsigned char g_dot_scratch[kStaticScratchBytes
 
 namespace {
 
-std::mutex g_scratch_mu;
-std::vector<void*> g_scratch_ptr;  // per device; nullptr = not looked up yet
+typedef int (*ctx_get_current_fn)(void** ctx);
+typedef int (*ctx_get_id_fn)(void* ctx, unsigned long long* id);
 
-// Device address of g_dot_scratch on the current device (looked up once).
-int scratch_address(void** out) {
-  int dev = 0;
-  cudaError_t e = cudaGetDevice(&dev);
-  if (e != cudaSuccess) {
-    set_error("b200_stream_dot_static: cudaGetDevice: %s", cudaGetErrorString(e));
-    return B200_ERR_LAUNCH;
-  }
-  std::lock_guard<std::mutex> lk(g_scratch_mu);
-  if (static_cast<int>(g_scratch_ptr.size()) <= dev) g_scratch_ptr.resize(dev + 1, nullptr);
-  if (!g_scratch_ptr[dev]) {
+struct ScratchEntry {
+  unsigned long long ctx_id;
+  void* ptr;
+};
+
+std::mutex g_scratch_mu;
+std::vector<ScratchEntry> g_scratch;  // one entry per context seen
+
+// Process-unique id of the current context (cuCtxGetId), found through the
+// runtime's driver entry points so the library does not link libcuda.
+int current_context_id(unsigned long long* id) {
+  static ctx_get_current_fn get_current = nullptr;
+  static ctx_get_id_fn get_id = nullptr;
+  static std::once_flag once;
+  std::call_once(once, [] {
     void* p = nullptr;
-    e = cudaGetSymbolAddress(&p, g_dot_scratch);
-    if (e != cudaSuccess || !p) {
-      set_error("b200_stream_dot_static: cudaGetSymbolAddress: %s", cudaGetErrorString(e));
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &p, 12000, cudaEnableDefault,
+                                         &q) == cudaSuccess && q == cudaDriverEntryPointSuccess)
+      get_current = reinterpret_cast<ctx_get_current_fn>(p);
+    p = nullptr;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetId", &p, 12000, cudaEnableDefault,
+                                         &q) == cudaSuccess && q == cudaDriverEntryPointSuccess)
+      get_id = reinterpret_cast<ctx_get_id_fn>(p);
+    cudaGetLastError();
+  });
+  if (!get_current || !get_id) return B200_ERR_UNSUPPORTED;
+  // With no context current, cudaSetDevice on the current device makes that
+  // device's primary context current (it initialises it; it allocates no
+  // device memory).
+  void* ctx = nullptr;
+  if (get_current(&ctx) != 0 || !ctx) {
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e == cudaSuccess) e = cudaSetDevice(dev);
+    if (e != cudaSuccess || get_current(&ctx) != 0 || !ctx) {
+      cudaGetLastError();
       return B200_ERR_LAUNCH;
     }
-    g_scratch_ptr[dev] = p;
   }
-  *out = g_scratch_ptr[dev];
+  return get_id(ctx, id) == 0 ? B200_OK : B200_ERR_LAUNCH;
+}
+
+// Device address of g_dot_scratch in the current context (looked up once
+// per context).
+int scratch_address(void** out) {
+  unsigned long long id = 0;
+  int st = current_context_id(&id);
+  if (st != B200_OK) {
+    set_error("b200_stream_dot_static: no current CUDA context (cuCtxGetCurrent/cuCtxGetId)");
+    return st;
+  }
+  std::lock_guard<std::mutex> lk(g_scratch_mu);
+  for (const ScratchEntry& en : g_scratch) {
+    if (en.ctx_id == id) {
+      *out = en.ptr;
+      return B200_OK;
+    }
+  }
+  void* p = nullptr;
+  cudaError_t e = cudaGetSymbolAddress(&p, g_dot_scratch);
+  if (e != cudaSuccess || !p) {
+    // clear the error here so that the next entry point does not report it
+    cudaGetLastError();
+    set_error("b200_stream_dot_static: cudaGetSymbolAddress: %s", cudaGetErrorString(e));
+    return B200_ERR_LAUNCH;
+  }
+  g_scratch.push_back({id, p});
+  *out = p;
   return B200_OK;
 }
 
@@ -126,6 +179,7 @@ int b200_stream_dot_static(const double* a, const double* b, int64_t n, double d
   cudaStream_t s = as_stream(stream);
   cudaError_t e = cudaMemsetAsync(counter, 0, sizeof(unsigned int), s);
   if (e != cudaSuccess) {
+    cudaGetLastError();
     set_error("b200_stream_dot_static: clearing the counter: %s", cudaGetErrorString(e));
     return B200_ERR_LAUNCH;
   }

@@ -15,6 +15,8 @@ namespace algorithm {
 RAJAPERF_GB300_KERNEL(SCAN,
  public:
   void setGB300TuningDefinitions(VariantID vid) override;
+  void prepareRun(size_t tune_idx) override;
+  void finishRun(size_t tune_idx) override;
  private:
   bool isInt64(size_t tune_idx) const;
   Real_ptr m_x = nullptr, m_y = nullptr;

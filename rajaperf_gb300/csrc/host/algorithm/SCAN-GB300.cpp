@@ -71,6 +71,17 @@ KernelBase::RepBody SCAN::makeRepBody(size_t tune_idx) {
   };
 }
 
+void SCAN::prepareRun(size_t tune_idx) {
+  const bool aligned = isInt64(tune_idx)
+                           ? (reinterpret_cast<uintptr_t>(m_xi) % 16 == 0 &&
+                              reinterpret_cast<uintptr_t>(m_yi) % 16 == 0)
+                           : (reinterpret_cast<uintptr_t>(m_x) % 16 == 0 &&
+                              reinterpret_cast<uintptr_t>(m_y) % 16 == 0);
+  injectLookbackStall(m_ws, m_ws_bytes, getTune(tune_idx), aligned);
+}
+
+void SCAN::finishRun(size_t) { checkWorkspace(m_ws, m_ws_bytes, "Algorithm_SCAN"); }
+
 void SCAN::updateChecksum(VariantID vid, size_t tune_idx) {
   const Index_type n = getActualProblemSize();
   if (isInt64(tune_idx)) {

@@ -34,6 +34,7 @@ RAJAPERF_GB300_KERNEL(MULADDSUB,
 // length; both run b200_basic_indexlist (one pass).
 RAJAPERF_GB300_KERNEL(INDEXLIST,
  public:
+  void prepareRun(size_t tune_idx) override;
   void finishRun(size_t tune_idx) override;
  private:
   Real_ptr m_x = nullptr;
@@ -45,6 +46,7 @@ RAJAPERF_GB300_KERNEL(INDEXLIST,
 
 RAJAPERF_GB300_KERNEL(INDEXLIST_3LOOP,
  public:
+  void prepareRun(size_t tune_idx) override;
   void finishRun(size_t tune_idx) override;
  private:
   Real_ptr m_x = nullptr;

@@ -57,7 +57,13 @@ KernelBase::RepBody INDEXLIST::makeRepBody(size_t tune_idx) {
   };
 }
 
+void INDEXLIST::prepareRun(size_t tune_idx) {
+  injectLookbackStall(m_ws, m_ws_bytes, getTune(tune_idx),
+                      reinterpret_cast<uintptr_t>(m_x) % 16 == 0);
+}
+
 void INDEXLIST::finishRun(size_t) {
+  checkWorkspace(m_ws, m_ws_bytes, "Basic_INDEXLIST");
   int64_t len = -1;
   copyToHost(&len, m_dlen, sizeof(len));
   m_len = static_cast<Index_type>(len);
@@ -110,7 +116,13 @@ KernelBase::RepBody INDEXLIST_3LOOP::makeRepBody(size_t tune_idx) {
   };
 }
 
+void INDEXLIST_3LOOP::prepareRun(size_t tune_idx) {
+  injectLookbackStall(m_ws, m_ws_bytes, getTune(tune_idx),
+                      reinterpret_cast<uintptr_t>(m_x) % 16 == 0);
+}
+
 void INDEXLIST_3LOOP::finishRun(size_t) {
+  checkWorkspace(m_ws, m_ws_bytes, "Basic_INDEXLIST_3LOOP");
   int64_t len = -1;
   copyToHost(&len, m_dlen, sizeof(len));
   m_len = static_cast<Index_type>(len);

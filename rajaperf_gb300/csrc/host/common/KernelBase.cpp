@@ -67,10 +67,41 @@ size_t KernelBase::getVariantTuningIndex(VariantID vid,
 b200_tune KernelBase::getTune(size_t tune_idx) const {
   b200_tune t{};
   const std::string& tname = getVariantTuningName(Base_GB300, tune_idx);
-  for (const NamedTune& nt : named_tunes)
-    if (nt.name == tname) return nt.tune;
-  TuningTable::instance().lookup(name, actual_prob_size, &t);
+  bool named = false;
+  for (const NamedTune& nt : named_tunes) {
+    if (nt.name == tname) {
+      t = nt.tune;
+      named = true;
+      break;
+    }
+  }
+  if (!named) TuningTable::instance().lookup(name, actual_prob_size, &t);
+  if (run_params.getWaitLimitUs() > 0) t.wait_limit_us = run_params.getWaitLimitUs();
   return t;
+}
+
+void KernelBase::checkWorkspace(void* ws, size_t bytes, const char* what) const {
+  if (!ws) return;
+  const int st = b200_workspace_status(ws, bytes, getStream());
+  if (st != B200_OK)
+    throw std::runtime_error(std::string(what) + ": " +
+                             (st == B200_ERR_TIMEOUT ? "device-side wait timed out: " : "") +
+                             b200_last_error_string());
+}
+
+void KernelBase::injectLookbackStall(void* ws, size_t bytes, const b200_tune& tn,
+                                     bool pointers_aligned) const {
+  const long k = run_params.getInjectLookbackStall();
+  if (k <= 0 || !ws) return;
+  // Only the persistent ring kernel bounds its tile ids by the tile count,
+  // so only it may start with tickets already taken.
+  if (tn.algo != 0 || tn.vec == 1 || !pointers_aligned || bytes < 256)
+    throw std::runtime_error("--inject-lookback-stall needs the pipelined (algo 0) kernel");
+  // ticket word: low 32 bits = tickets taken, high 32 bits = launch epoch
+  unsigned long long word = 0;
+  checkCuda(cudaMemcpy(&word, ws, sizeof(word), cudaMemcpyDeviceToHost), "stall: read");
+  word += static_cast<unsigned long long>(k);
+  checkCuda(cudaMemcpy(ws, &word, sizeof(word), cudaMemcpyHostToDevice), "stall: write");
 }
 
 bool KernelBase::isGraphTuning(size_t tune_idx) const {

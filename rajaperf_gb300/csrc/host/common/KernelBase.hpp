@@ -148,6 +148,13 @@ class KernelBase {
   // Launch shape for a tuning (table entry for this kernel and size, the
   // tuning's own shape, or zeros = library default).
   b200_tune getTune(size_t tune_idx) const;
+  // Throws when a bounded device-side wait of a call on this workspace gave
+  // up since its last check (b200_workspace_status; clears the workspace).
+  void checkWorkspace(void* ws, size_t bytes, const char* what) const;
+  // --inject-lookback-stall: marks tickets of a lookback workspace as taken
+  // before a run (untimed), so that a lookback wait runs out.
+  void injectLookbackStall(void* ws, size_t bytes, const b200_tune& tn,
+                           bool pointers_aligned) const;
   bool isGraphTuning(size_t tune_idx) const;
   // Runs `reps` repetitions of `rep_body` between startTimer and stopTimer,
   // either as direct calls or, for a graph tuning, as one captured graph.

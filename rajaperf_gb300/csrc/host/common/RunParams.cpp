@@ -158,6 +158,16 @@ RunParams::RunParams(int argc, const char* const* argv) {
           size_map[kid] = v;
         }
       }
+    } else if (opt == "--wait-limit-us") {
+      long long v;
+      if (!parseLong(takeValue(i, opt), v) || v < 0 || v > 2000000000LL)
+        fail("bad --wait-limit-us");
+      wait_limit_us = static_cast<int>(v);
+    } else if (opt == "--inject-lookback-stall") {
+      long long v;
+      if (!parseLong(takeValue(i, opt), v) || v < 1 || v > 1000000LL)
+        fail("bad --inject-lookback-stall");
+      inject_lookback_stall = static_cast<long>(v);
     } else if (opt == "--tuning-table") {
       tuning_table_file = takeValue(i, opt);
     } else if (opt == "--autotune") {
@@ -281,6 +291,14 @@ std::string RunParams::usage() {
       "                               them to FILE as a tuning table\n"
       "  --graph-batch [R]            capture every kernel's R-rep loop into\n"
       "                               one CUDA graph and compare with launches\n"
+      "  --wait-limit-us U            limit of the kernels' bounded device-side\n"
+      "                               waits (0 = library default: 2 s, GEMM 1 s)\n"
+      "  --inject-lookback-stall K    test option: before each run of SCAN and\n"
+      "                               INDEXLIST(_3LOOP) mark K tile tickets as\n"
+      "                               taken, so that the first tile's lookback\n"
+      "                               waits for tiles nobody processes until its\n"
+      "                               wait limit runs out (the run then fails\n"
+      "                               with the device-side timeout)\n"
       "  -od DIR, -of PREFIX          report directory and file prefix\n"
       "  --dryrun, --show-progress, --disable-warmup, -h\n";
 }

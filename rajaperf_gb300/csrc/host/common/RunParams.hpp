@@ -44,6 +44,11 @@ class RunParams {
   double getInitLo() const { return init_lo; }
   double getInitHi() const { return init_hi; }
 
+  // Limit of the bounded device-side waits (b200_tune.wait_limit_us; 0 =
+  // library default) and the test option that makes a lookback wait run out.
+  int getWaitLimitUs() const { return wait_limit_us; }
+  long getInjectLookbackStall() const { return inject_lookback_stall; }
+
   // -1 when the kernel's own time-step count applies.
   long getPolybenchTsteps() const { return polybench_tsteps; }
 
@@ -96,6 +101,8 @@ class RunParams {
   double init_lo = 0.5;
   double init_hi = 1.5;
   long polybench_tsteps = -1;
+  int wait_limit_us = 0;
+  long inject_lookback_stall = 0;
   long multi_reduce_num_bins = 10;
   long halo_width = 1;
   long halo_num_vars = 3;

@@ -48,6 +48,7 @@ void POLYBENCH_3MM::setUp(VariantID vid, size_t tune_idx) {
                                    b200_gemm_split_workspace_bytes(m_nj, m_nl, m_nm, nullptr)),
                           b200_gemm_split_workspace_bytes(m_ni, m_nl, m_nj, nullptr));
     m_ws = allocDeviceBytes(m_ws_bytes);
+    zeroDeviceBytes(m_ws, m_ws_bytes);
   }
   allocAndInitData(m_A, m_ni * m_nk, vid);
   allocAndInitData(m_B, m_nk * m_nj, vid);
@@ -63,11 +64,11 @@ KernelBase::RepBody POLYBENCH_3MM::makeRepBody(size_t tune_idx) {
   if (isSplit(tune_idx)) {
     return [=](b200_stream_t s) {
       checkB200(b200_gemm_split(m_A, m_B, m_E, m_ni, m_nj, m_nk, 1.0, 0.0, m_ws, m_ws_bytes,
-                                nullptr, s), "b200_gemm_split");
+                                &tn, s), "b200_gemm_split");
       checkB200(b200_gemm_split(m_C, m_D, m_F, m_nj, m_nl, m_nm, 1.0, 0.0, m_ws, m_ws_bytes,
-                                nullptr, s), "b200_gemm_split");
+                                &tn, s), "b200_gemm_split");
       checkB200(b200_gemm_split(m_E, m_F, m_G, m_ni, m_nl, m_nj, 1.0, 0.0, m_ws, m_ws_bytes,
-                                nullptr, s), "b200_gemm_split");
+                                &tn, s), "b200_gemm_split");
     };
   }
   return [=](b200_stream_t s) {
@@ -76,6 +77,8 @@ KernelBase::RepBody POLYBENCH_3MM::makeRepBody(size_t tune_idx) {
               "b200_polybench_3mm");
   };
 }
+
+void POLYBENCH_3MM::finishRun(size_t) { checkWorkspace(m_ws, m_ws_bytes, "Polybench_3MM"); }
 
 void POLYBENCH_3MM::updateChecksum(VariantID vid, size_t tune_idx) {
   checksum[vid][tune_idx] += calcChecksum(m_G, m_ni * m_nl, checksum_scale_factor, vid);

@@ -45,6 +45,7 @@ void POLYBENCH_GEMM::setUp(VariantID vid, size_t tune_idx) {
   if (isSplit(tune_idx)) {
     m_ws_bytes = b200_gemm_split_workspace_bytes(m_ni, m_nj, m_nk, nullptr);
     m_ws = allocDeviceBytes(m_ws_bytes);
+    zeroDeviceBytes(m_ws, m_ws_bytes);
   }
 }
 
@@ -54,7 +55,7 @@ KernelBase::RepBody POLYBENCH_GEMM::makeRepBody(size_t tune_idx) {
     // C = alpha*A*B (the suite's beta scaling is overwritten by BODY4)
     return [=](b200_stream_t s) {
       checkB200(b200_gemm_split(m_A, m_B, m_C, m_ni, m_nj, m_nk, m_alpha, 0.0, m_ws,
-                                m_ws_bytes, nullptr, s),
+                                m_ws_bytes, &tn, s),
                 "b200_gemm_split");
     };
   }
@@ -62,6 +63,10 @@ KernelBase::RepBody POLYBENCH_GEMM::makeRepBody(size_t tune_idx) {
     checkB200(b200_polybench_gemm(m_A, m_B, m_C, m_ni, m_nj, m_nk, m_alpha, &tn, s),
               "b200_polybench_gemm");
   };
+}
+
+void POLYBENCH_GEMM::finishRun(size_t) {
+  checkWorkspace(m_ws, m_ws_bytes, "Polybench_GEMM");
 }
 
 void POLYBENCH_GEMM::updateChecksum(VariantID vid, size_t tune_idx) {

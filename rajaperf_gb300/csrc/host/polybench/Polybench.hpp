@@ -29,6 +29,8 @@ RAJAPERF_GB300_KERNEL(POLYBENCH_FDTD_2D,
 // "split_bf16"/"split_bf16_graph" run the split-precision tensor-core GEMM
 // (b200_gemm_split; inner dimensions up to 8192).
 RAJAPERF_GB300_KERNEL(POLYBENCH_GEMM,
+ public:
+  void finishRun(size_t tune_idx) override;
  private:
   bool isSplit(size_t tune_idx) const;
   Index_type m_ni = 0, m_nj = 0, m_nk = 0;
@@ -38,6 +40,8 @@ RAJAPERF_GB300_KERNEL(POLYBENCH_GEMM,
   size_t m_ws_bytes = 0;)
 
 RAJAPERF_GB300_KERNEL(POLYBENCH_3MM,
+ public:
+  void finishRun(size_t tune_idx) override;
  private:
   bool isSplit(size_t tune_idx) const;
   Index_type m_ni = 0, m_nj = 0, m_nk = 0, m_nl = 0, m_nm = 0;

@@ -27,13 +27,17 @@ def run_split(A, B, C, alpha, beta, slices=None, engine=0):
     t = rp.Tune(items=slices or 0, algo=engine)
     tp = ctypes.byref(t)
     ws_bytes = L.b200_gemm_split_workspace_bytes(m, n, k, tp)
+    # stale bytes everywhere but the 256-byte header, which a workspace
+    # starts with zeroed (its error word is at byte 16)
     ws = torch.full((ws_bytes,), 0xAB, dtype=torch.uint8, device="cuda")
+    ws[:256].zero_()
     dA, dB, dC = gu.dev(A.ravel()), gu.dev(B.ravel()), gu.dev(C.ravel())
     rp.check(L.b200_gemm_split(dA.data_ptr(), dB.data_ptr(), dC.data_ptr(), m, n, k, alpha,
                                beta, ws.data_ptr(), ws_bytes, tp, gu.stream()), "gemm_split")
     got = gu.host(dC).reshape(m, n)
     if engine == 0:
-        assert int(gu.host(ws[:4]).view(np.uint32)[0]) == 0, "a bounded wait gave up"
+        assert L.b200_workspace_status(ws.data_ptr(), ws_bytes, gu.stream()) == rp.B200_OK, \
+            "a bounded wait gave up"
     return got
 
 

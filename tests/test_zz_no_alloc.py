@@ -51,6 +51,47 @@ def test_dot_static_matches_workspace_dot(n):
     assert abs(got - 2 * (0.25 + float(np.sum(a * b)))) <= bound
 
 
+def test_dot_static_full_scratch_and_no_device_allocation():
+    """A launch of exactly the 4096 CTAs the static scratch holds (its last
+    partial slot used) agrees with the workspace DOT, and calls after the
+    first one in this context leave the device's free memory unchanged (the
+    first call may load the library's device module, which the driver does
+    once per context)."""
+    torch = gu.torch_cuda()
+    L = rp.b200()
+    n = 4096 * 64 * 3 + 17
+    rng = np.random.default_rng(7)
+    a, b = rng.uniform(0.5, 1.5, n), rng.uniform(0.5, 1.5, n)
+    da, db = gu.dev(a), gu.dev(b)
+    t = rp.Tune(block_size=64, items=1, grid_blocks=4096)
+    ws_bytes = L.b200_reduce_workspace_bytes(n, ctypes.byref(t))
+    assert ws_bytes == L.b200_stream_dot_static_max_scratch_bytes()
+    ws = torch.zeros(ws_bytes, dtype=torch.uint8, device="cuda")
+    acc_ref = torch.zeros(1, dtype=torch.float64, device="cuda")
+    acc_static = torch.zeros(1, dtype=torch.float64, device="cuda")
+    static = _static_fn()
+    s = gu.stream()
+    rp.check(static(da.data_ptr(), db.data_ptr(), n, 0.0, acc_static.data_ptr(),
+                    ctypes.byref(t), s), "b200_stream_dot_static")
+    torch.cuda.synchronize()
+    free0, _ = torch.cuda.mem_get_info()
+    for _ in range(3):
+        rp.check(static(da.data_ptr(), db.data_ptr(), n, 0.0, acc_static.data_ptr(),
+                        ctypes.byref(t), s), "b200_stream_dot_static")
+    torch.cuda.synchronize()
+    free1, _ = torch.cuda.mem_get_info()
+    assert free1 == free0
+    for _ in range(4):
+        rp.check(L.b200_stream_dot(da.data_ptr(), db.data_ptr(), n, 0.0, acc_ref.data_ptr(),
+                                   ws.data_ptr(), ws_bytes, ctypes.byref(t), s),
+                 "b200_stream_dot")
+    got = float(gu.host(acc_static)[0])
+    want = float(gu.host(acc_ref)[0])
+    bound = gu.reduction_bound(n, 4, 4.0 * float(np.sum(a * b)))
+    assert abs(got - want) <= bound, (got, want)
+    assert abs(got - 4 * float(np.sum(a * b))) <= bound
+
+
 def test_dot_static_rejects_oversized_shape():
     torch = gu.torch_cuda()
     x = torch.ones(1 << 20, dtype=torch.float64, device="cuda")
