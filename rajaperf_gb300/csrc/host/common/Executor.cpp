@@ -2,6 +2,7 @@
 
 #include "Autotuner.hpp"
 #include "GraphRepRunner.hpp"
+#include "Reports.hpp"
 #include "TuningTable.hpp"
 
 #include <cuda_runtime.h>
@@ -264,74 +265,76 @@ void Executor::outputRunData() {
       << batch_.error << "\"}\n";
     return;
   }
-  writeTimingCSV(base + "-timing-Average.csv", 0);
-  writeTimingCSV(base + "-timing-Minimum.csv", 1);
-  writeTimingCSV(base + "-timing-Maximum.csv", 2);
-  writeChecksumReport(base + "-checksum.txt");
-  writeKernelsCSV(base + "-kernels.csv");
+  const reports::ReportData d = reportData();
+  std::vector<std::string> combiners = run_params.getNpassesCombiners();
+  if (combiners.empty()) combiners.push_back("Average");  // the suite's default
+  for (const std::string& c : combiners) {
+    const reports::Combiner m = c == "Minimum"   ? reports::Combiner::Minimum
+                                : c == "Maximum" ? reports::Combiner::Maximum
+                                                 : reports::Combiner::Average;
+    {
+      std::ofstream f(base + "-timing-" + c + ".csv");
+      reports::writeTimingReport(f, d, m);
+    }
+    if (d.reference_variant >= 0) {
+      std::ofstream f(base + "-speedup-" + c + ".csv");
+      reports::writeSpeedupReport(f, d, m);
+    }
+  }
+  {
+    std::ofstream f(base + "-checksum.txt");
+    reports::writeChecksumReport(f, d);
+  }
+  if (reports::hasFOMGroups(d)) {
+    std::ofstream f(base + "-fom.csv");
+    reports::writeFOMReport(f, d);
+  }
+  {
+    std::ofstream f(base + "-kernels.csv");
+    reports::writeKernelInfo(f, d);
+  }
   writeRooflineJSON(base + "-roofline.json");
 }
 
-// Layout of Executor.cpp:901-997: title line, variant line, tuning line, one
-// row per kernel.
-void Executor::writeTimingCSV(const std::string& fname, int mode) const {
-  std::ofstream f(fname);
-  const char* title[] = {"Mean Runtime Report (sec.) ", "Min Runtime Report (sec.) ",
-                         "Max Runtime Report (sec.) "};
-  const std::string sep(" , ");
-  f << title[mode];
-  for (size_t t = 0; t < tuning_names_.size(); ++t) f << sep;
-  f << "\n" << std::left << std::setw(24) << "Kernel  ";
-  for (size_t t = 0; t < tuning_names_.size(); ++t) f << sep << getVariantName(Base_GB300);
-  f << "\n" << std::left << std::setw(24) << "Kernel  ";
-  for (const auto& tn : tuning_names_) f << sep << tn;
-  f << "\n";
+// The run's results as the report writers' table: one variant (Base_GB300)
+// whose columns are the selected tunings in first-seen order.
+reports::ReportData Executor::reportData() const {
+  reports::ReportData d;
+  d.variants.push_back(getVariantName(Base_GB300));
+  d.tunings.push_back(tuning_names_);
+  d.npasses = run_params.getNumPasses();
+  d.pf_tolerance = run_params.getPFTolerance();
+  d.reference_variant = run_params.getReferenceVariant().empty() ? -1 : 0;
   for (size_t i = 0; i < kernels_.size(); ++i) {
     const KernelBase* k = kernels_[i].get();
-    f << std::left << std::setw(24) << k->getName();
-    for (const auto& tn : tuning_names_) {
-      size_t t = k->getVariantTuningIndex(Base_GB300, tn);
-      f << sep;
-      if (t == KernelBase::getUnknownTuningIdx() || !k->wasVariantTuningRun(Base_GB300, t)) {
-        f << "Not run";
-      } else {
-        int ne = k->getNumExec(Base_GB300, t);
-        double v = mode == 0 ? k->getTotTime(Base_GB300, t) / ne
-                 : mode == 1 ? k->getMinTime(Base_GB300, t)
-                             : k->getMaxTime(Base_GB300, t);
-        f << std::setprecision(9) << std::fixed << v;
+    reports::KernelRow row;
+    row.name = k->getName();
+    row.problem_size = k->getActualProblemSize();
+    row.reps = k->getRunReps();
+    row.its_per_rep = k->getItsPerRep();
+    row.kernels_per_rep = k->getKernelsPerRep();
+    row.bytes_per_rep = k->getBytesPerRep();
+    row.flops_per_rep = k->getFLOPsPerRep();
+    row.bytes_read_per_rep = k->getBytesReadPerRep();
+    row.bytes_written_per_rep = k->getBytesWrittenPerRep();
+    row.bytes_atomic_modify_written_per_rep = k->getBytesAtomicModifyWrittenPerRep();
+    row.cells.resize(1);
+    for (const std::string& tn : tuning_names_) {
+      reports::Cell c;
+      const size_t t = k->getVariantTuningIndex(Base_GB300, tn);
+      c.defined = t != KernelBase::getUnknownTuningIdx();
+      c.run = c.defined && k->wasVariantTuningRun(Base_GB300, t);
+      if (c.run) {
+        c.tot_time = k->getTotTime(Base_GB300, t);
+        c.min_time = k->getMinTime(Base_GB300, t);
+        c.max_time = k->getMaxTime(Base_GB300, t);
+        c.checksum = k->getChecksum(Base_GB300, t);
       }
+      row.cells[0].push_back(c);
     }
-    f << "\n";
+    d.kernels.push_back(std::move(row));
   }
-}
-
-// Executor.cpp:1281-1512: checksum per kernel / variant / tuning.
-void Executor::writeChecksumReport(const std::string& fname) const {
-  std::ofstream f(fname);
-  f << "********************************************************************\n"
-    << "Checksum Report (Base_GB300)\n"
-    << "********************************************************************\n\n";
-  f << std::left << std::setw(24) << "Kernel" << std::setw(28) << "Variant" << "Checksum\n";
-  for (const RunResult& r : results_) {
-    f << std::left << std::setw(24) << r.kernel << std::setw(28)
-      << (r.variant + "-" + r.tuning) << std::setprecision(20) << std::scientific
-      << r.checksum << (r.error.empty() ? "" : "  (failed: " + r.error + ")") << "\n";
-  }
-}
-
-// Executor.cpp:508-642: kernel details.
-void Executor::writeKernelsCSV(const std::string& fname) const {
-  std::ofstream f(fname);
-  f << "Kernel , Problem size , Reps , Iterations/rep , Kernels/rep , "
-       "Bytes/rep , FLOPS/rep\n";
-  for (const auto& kp : kernels_) {
-    const KernelBase* k = kp.get();
-    f << k->getName() << " , " << k->getActualProblemSize() << " , "
-      << k->getRunReps() << " , " << k->getItsPerRep() << " , "
-      << k->getKernelsPerRep() << " , " << k->getBytesPerRep() << " , "
-      << k->getFLOPsPerRep() << "\n";
-  }
+  return d;
 }
 
 // Bandwidth and FLOP rate as scripts/caliper_graph/plot.py:15-31 derives

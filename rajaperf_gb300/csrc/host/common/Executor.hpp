@@ -3,9 +3,10 @@
 // Same five steps as the suite's driver (RAJAPerfSuiteDriver.cpp:36-49 and
 // common/Executor.hpp:45-51): setupSuite, reportRunSummary, runSuite,
 // outputRunData.  runSuite runs every selected kernel x tuning for npasses
-// (Executor.cpp:645-724).  outputRunData writes the timing CSVs, the checksum
-// report and the kernel-details CSV in the suite's layout, plus a roofline
-// JSON with achieved GB/s and GFLOP/s per kernel and tuning.
+// (Executor.cpp:645-724).  outputRunData writes the suite's reports
+// (Reports.hpp: timing and speedup CSVs per npasses combiner, checksum
+// report, FOM report, kernel details) plus a roofline JSON with achieved
+// GB/s and GFLOP/s per kernel and tuning.
 //
 // Graph batching (--graph-batch): the rep loops of all selected kernels are
 // captured together into one CUDA graph and timed against the same work
@@ -14,6 +15,7 @@
 
 #include "Autotuner.hpp"
 #include "KernelBase.hpp"
+#include "Reports.hpp"
 #include "RunParams.hpp"
 
 #include <iosfwd>
@@ -72,9 +74,7 @@ class Executor {
   void runAutotune();
   void runGraphBatch();
   void collectResults();
-  void writeTimingCSV(const std::string& fname, int mode) const;
-  void writeChecksumReport(const std::string& fname) const;
-  void writeKernelsCSV(const std::string& fname) const;
+  reports::ReportData reportData() const;
   void writeRooflineJSON(const std::string& fname) const;
 
   RunParams run_params;

@@ -75,6 +75,7 @@ class KernelBase {
   }
   Index_type getBytesReadPerRep() const { return bytes_read_per_rep; }
   Index_type getBytesWrittenPerRep() const { return bytes_written_per_rep; }
+  Index_type getBytesAtomicModifyWrittenPerRep() const { return bytes_atomic_per_rep; }
   Index_type getFLOPsPerRep() const { return flops_per_rep; }
   Complexity getComplexity() const { return complexity; }
   bool usesFeature(FeatureID fid) const { return uses_feature[fid]; }

@@ -158,6 +158,22 @@ RunParams::RunParams(int argc, const char* const* argv) {
           size_map[kid] = v;
         }
       }
+    } else if (opt == "--npasses-combiners") {
+      std::vector<std::string> items;
+      takeList(i, items);
+      for (const std::string& c : items) {
+        if (c != "Average" && c != "Minimum" && c != "Maximum")
+          fail("bad --npasses-combiners entry " + c + " (Average|Minimum|Maximum)");
+        else if (std::find(npasses_combiners.begin(), npasses_combiners.end(), c) ==
+                 npasses_combiners.end())
+          npasses_combiners.push_back(c);
+      }
+    } else if (opt == "--refvar" || opt == "-rv") {
+      reference_variant = takeValue(i, opt);
+    } else if (opt == "--pass-fail-tol" || opt == "-pftol") {
+      double v;
+      if (!parseDouble(takeValue(i, opt), v) || v < 0) fail("bad --pass-fail-tol");
+      pf_tolerance = v;
     } else if (opt == "--wait-limit-us") {
       long long v;
       if (!parseLong(takeValue(i, opt), v) || v < 0 || v > 2000000000LL)
@@ -248,6 +264,8 @@ RunParams::RunParams(int argc, const char* const* argv) {
       else fail("variant " + v + " is not available in this build");
     }
   }
+  if (!reference_variant.empty() && reference_variant != getVariantName(Base_GB300))
+    fail("reference variant " + reference_variant + " is not available in this build");
 
   if (input_state == Undefined) input_state = PerfRun;
 }
@@ -300,6 +318,10 @@ std::string RunParams::usage() {
       "                               wait limit runs out (the run then fails\n"
       "                               with the device-side timeout)\n"
       "  -od DIR, -of PREFIX          report directory and file prefix\n"
+      "  --npasses-combiners C...     timing/speedup reports to write:\n"
+      "                               Average Minimum Maximum (Average)\n"
+      "  -rv/--refvar VARIANT         write speedup reports against VARIANT\n"
+      "  -pftol/--pass-fail-tol T     FOM report OVER_TOL threshold (0.1)\n"
       "  --dryrun, --show-progress, --disable-warmup, -h\n";
 }
 

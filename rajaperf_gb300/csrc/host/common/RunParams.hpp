@@ -47,6 +47,12 @@ class RunParams {
   // Limit of the bounded device-side waits (b200_tune.wait_limit_us; 0 =
   // library default) and the test option that makes a lookback wait run out.
   int getWaitLimitUs() const { return wait_limit_us; }
+  // Reports: npasses combiners of the timing/speedup CSVs (the suite's
+  // --npasses-combiners, default Average), the speedup reference variant
+  // (--refvar; none by default) and the FOM tolerance (--pass-fail-tol).
+  const std::vector<std::string>& getNpassesCombiners() const { return npasses_combiners; }
+  const std::string& getReferenceVariant() const { return reference_variant; }
+  double getPFTolerance() const { return pf_tolerance; }
   long getInjectLookbackStall() const { return inject_lookback_stall; }
 
   // -1 when the kernel's own time-step count applies.
@@ -102,6 +108,9 @@ class RunParams {
   double init_hi = 1.5;
   long polybench_tsteps = -1;
   int wait_limit_us = 0;
+  std::vector<std::string> npasses_combiners;
+  std::string reference_variant;
+  double pf_tolerance = 0.1;
   long inject_lookback_stall = 0;
   long multi_reduce_num_bins = 10;
   long halo_width = 1;

@@ -151,3 +151,32 @@ def test_autotune_table_and_graph_batch(tmp_path):
         res = rp.run_suite(["--size", rec["size"], "--checkrun", rec["reps"], "-k", kernel,
                             "-t", "default", "--disable-warmup", "--tuning-table", str(table)])
         _check(kernel, rec, res[0])
+
+
+def test_report_files(tmp_path):
+    """-od writes the suite's report set: timing and speedup CSVs per
+    --npasses-combiners entry, the checksum report whose difference column
+    is against the first tuning run, the FOM report and the kernel details."""
+    out = tmp_path / "rep"
+    res = rp.run_suite(["--size", 65537, "--checkrun", 2, "-k", "Stream_TRIAD", "Stream_DOT",
+                        "-t", "default", "graph", "--disable-warmup", "--npasses", 2,
+                        "--npasses-combiners", "Average", "Minimum", "--refvar", "Base_GB300",
+                        "-od", str(out), "-of", "R"])
+    names = sorted(p.name for p in out.iterdir())
+    assert names == sorted(["R-timing-Average.csv", "R-timing-Minimum.csv",
+                            "R-speedup-Average.csv", "R-speedup-Minimum.csv", "R-checksum.txt",
+                            "R-fom.csv", "R-kernels.csv", "R-roofline.json"])
+    timing = (out / "R-timing-Average.csv").read_text().splitlines()
+    assert timing[0].startswith("Mean Runtime Report (sec.) ")
+    assert [c.strip() for c in timing[2].split(" , ")[1:]] == ["default", "graph"]
+    speed = (out / "R-speedup-Average.csv").read_text().splitlines()
+    for row in speed[3:]:
+        vals = [float(c) for c in row.split(" , ")[1:]]
+        assert vals[0] == 1.0 and vals[1] > 0
+    ck = (out / "R-checksum.txt").read_text()
+    for r in res:
+        assert f"Base_GB300-{r['tuning']}" in ck
+    fom = (out / "R-fom.csv").read_text().splitlines()
+    assert "base_ref" in fom[3]
+    with pytest.raises(RuntimeError, match="not available"):
+        rp.run_suite(["--size", 100, "-k", "Stream_TRIAD", "--refvar", "Base_Seq"])
