@@ -338,6 +338,24 @@ int b200_polybench_fdtd_2d(double* ex, double* ey, double* hz,
                            int64_t tsteps, const b200_tune* tune,
                            b200_stream_t stream);
 
+/* Workspace for b200_polybench_fdtd_2d_ws: two snapshots of the tile edges
+ * (about 6 doubles per 32 x 128 tile edge point, 3-8% of one array). */
+size_t b200_fdtd_2d_workspace_bytes(int64_t nx, int64_t ny);
+
+/* The same tsteps of FDTD_2D with one launch per time step: every CTA
+ * updates ex and ey (BODY1-3) and then hz (BODY4) of its 32 x 128 tile in
+ * place, taking the old values across tile edges from a snapshot of the
+ * edges in the workspace (one extra small launch per call takes the first
+ * snapshot).  48 bytes per point and step instead of 72; bit-identical to
+ * b200_polybench_fdtd_2d.  tune->algo 1 runs b200_polybench_fdtd_2d instead
+ * (no workspace needed).  The workspace needs no initialisation.
+ *   -- polybench/POLYBENCH_FDTD_2D.hpp:52-69, -Cuda.cpp:164-190             */
+int b200_polybench_fdtd_2d_ws(double* ex, double* ey, double* hz,
+                              const double* fict, int64_t nx, int64_t ny,
+                              int64_t tsteps, void* workspace,
+                              size_t workspace_bytes, const b200_tune* tune,
+                              b200_stream_t stream);
+
 /* C[i][j] = sum_k (alpha*A[i][k]) * B[k][j], row-major, FP64 (the suite's
  * GEMM: its beta scaling is overwritten by BODY4)
  *   -- polybench/POLYBENCH_GEMM.hpp:40-56, -Cuda.cpp:27-59                  */
@@ -366,8 +384,9 @@ size_t b200_gemm_split_workspace_bytes(int64_t m, int64_t n, int64_t k,
  * rows of A / columns of B are scaled by powers of two and cut into
  * tune->items (default 11) balanced 5-bit integer slices held exactly in
  * bf16; slice products of equal weight accumulate exactly in FP32 on the
- * tensor cores; the weighted sum is formed in FP64.  k <= 8192 (the bound
- * under which the FP32 accumulation stays exact).  tune->algo picks the
+ * tensor cores over chunks of at most 8192 values of k (the bound under which
+ * the FP32 accumulation stays exact), each chunk folded into an FP64
+ * accumulator; the weighted sum is formed in FP64.  k <= 524288.  tune->algo picks the
  * engine: 0 (default) tcgen05 MMA with TMA-fed operands and tensor-memory
  * accumulators, 1 the legacy mma.sync path.  Zero the workspace once before
  * its first use.  The 32-bit word at byte offset 16 of the workspace is set

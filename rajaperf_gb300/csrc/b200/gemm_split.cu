@@ -9,13 +9,15 @@
 //     bf16, which holds them exactly.  B is cut the same way and stored
 //     transposed (N x K).
 //  3. For every digit weight w = s + t the products A_s * B_t are summed over
-//     k on the tensor cores in one FP32 accumulator.  Each product is an
-//     integer of magnitude <= 289 and K <= kMaxK, so every partial sum is an
-//     integer below 2^24 whenever at most 7 slice pairs share a weight: the
-//     tensor-core accumulation is exact for the weights that carry the result
-//     (larger weights contribute below 2^-45 of it).
-//  4. The epilogue adds 2^(-5w) * acc_w into an FP64 accumulator, and finally
-//     C = alpha * 2^(Ea+Eb-10S) * acc64 + beta * C in FP64.
+//     a chunk of k on the tensor cores in one FP32 accumulator.  Each product
+//     is an integer of magnitude <= 289 and a chunk holds at most kChunkK = 8192
+//     values of k, so every partial sum is an integer below 2^24 whenever at
+//     most 7 slice pairs share a weight: the tensor-core accumulation is exact
+//     for the weights that carry the result (larger weights contribute below
+//     2^-45 of it).  Longer K is cut into balanced chunks of at most kChunkK.
+//  4. The epilogue adds 2^(-5w) * acc_(w,chunk) into an FP64 accumulator after
+//     every chunk, and finally C = alpha * 2^(Ea+Eb-10S) * acc64 + beta * C in
+//     FP64.
 // Only weights w <= S + 1 are formed (the dropped products lie below the
 // slicing error).  The error against an FP64 GEMM is measured per size by the
 // tests and bench.
@@ -51,7 +53,9 @@ namespace {
 constexpr int kSliceBits = 5;
 constexpr int kMaxSlices = 12;
 constexpr int kDefaultSlices = 11;
-constexpr int64_t kMaxK = 8192;  // exactness bound of the FP32 accumulation
+constexpr int64_t kChunkK = 8192;  // exactness bound of one FP32 accumulation
+// Longest K: 64 chunks (the chunk arithmetic and TMA coordinates stay in int).
+constexpr int64_t kMaxK = 64 * kChunkK;
 constexpr int TM = 128, TN = 128, TK = 32;
 constexpr int kLds = TK + 8;     // padded smem row (80 bytes): conflict-free ldmatrix
 constexpr int kPadK = 64;        // K padding of the slice arrays (one TMA row = 128 B)
@@ -176,7 +180,6 @@ struct SplitArgs {
   int64_t M, N, Mp, Np, Kp;
   double alpha, beta;
   int S;
-  uint64_t limit_ns;  // limit of every bounded wait
 };
 
 __global__ void __launch_bounds__(256, 1) ozaki_mma_kernel(SplitArgs g) {
@@ -210,10 +213,17 @@ __global__ void __launch_bounds__(256, 1) ozaki_mma_kernel(SplitArgs g) {
     cp_async_commit();
   };
 
-  for (int w = 2; w <= g.S + 1; ++w) {
+  // K in balanced chunks of at most kChunkK (whole TK steps), each summed
+  // exactly in FP32 and folded into the FP64 accumulator
+  const int64_t nchunks = (ksteps * TK + kChunkK - 1) / kChunkK;
+  const int64_t chunk_steps = (ksteps + nchunks - 1) / nchunks;
+  for (int pass = 0; pass < (g.S) * static_cast<int>(nchunks); ++pass) {
+    const int w = 2 + pass / static_cast<int>(nchunks);
+    const int64_t c0 = (pass % nchunks) * chunk_steps;
+    const int64_t csteps = (c0 + chunk_steps < ksteps) ? chunk_steps : ksteps - c0;
     const int s_lo = (w - g.S > 1) ? w - g.S : 1;
     const int s_hi = (w - 1 < g.S) ? w - 1 : g.S;
-    const int64_t iters = static_cast<int64_t>(s_hi - s_lo + 1) * ksteps;
+    const int64_t iters = static_cast<int64_t>(s_hi - s_lo + 1) * csteps;
     float acc[4][4][4];
 #pragma unroll
     for (int a = 0; a < 4; ++a)
@@ -222,15 +232,15 @@ __global__ void __launch_bounds__(256, 1) ozaki_mma_kernel(SplitArgs g) {
 #pragma unroll
         for (int c = 0; c < 4; ++c) acc[a][b][c] = 0.f;
 
-    load_stage(0, s_lo - 1, w - s_lo - 1, 0);
+    load_stage(0, s_lo - 1, w - s_lo - 1, c0 * TK);
     for (int64_t it = 0; it < iters; ++it) {
       const int buf = static_cast<int>(it & 1);
       cp_async_wait0();
       __syncthreads();
       if (it + 1 < iters) {
         const int64_t nx = it + 1;
-        const int s = s_lo + static_cast<int>(nx / ksteps);
-        load_stage(buf ^ 1, s - 1, w - s - 1, (nx % ksteps) * TK);
+        const int s = s_lo + static_cast<int>(nx / csteps);
+        load_stage(buf ^ 1, s - 1, w - s - 1, (c0 + nx % csteps) * TK);
       }
 #pragma unroll
       for (int kk = 0; kk < TK; kk += 16) {
@@ -466,18 +476,27 @@ ozaki_tc_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__
 
   const int S = g.S;
   const int nkb = static_cast<int>(g.Kp / BK);
+  // K in balanced chunks of at most kChunkK (whole k blocks); a pass is one
+  // (weight, chunk): its slice products accumulate in one FP32 buffer, which
+  // the epilogue folds into the FP64 accumulator
+  const int nch = static_cast<int>((static_cast<int64_t>(nkb) * BK + kChunkK - 1) / kChunkK);
+  const int ckb = (nkb + nch - 1) / nch;
+  const int npass = S * nch;
   const int64_t i0 = static_cast<int64_t>(blockIdx.y) * BM;
   const int64_t j0 = static_cast<int64_t>(blockIdx.x) * BN;
 
   if (warp == 0) {
     if (lane == 0) {
-      // producer: (weight, slice pair, k block) in the MMA warp's order
+      // producer: (pass, slice pair, k block) in the MMA warp's order
       uint32_t it = 0;
       bool ok = true;
-      for (int w = 2; ok && w <= S + 1; ++w) {
+      for (int p = 0; ok && p < npass; ++p) {
+        const int w = 2 + p / nch;
+        const int kb0 = (p % nch) * ckb;
+        const int kb1 = (kb0 + ckb < nkb) ? kb0 + ckb : nkb;
         for (int s = 1; ok && s <= w - 1; ++s) {
           const int t = w - s;
-          for (int kb = 0; kb < nkb; ++kb, ++it) {
+          for (int kb = kb0; kb < kb1; ++kb, ++it) {
             const int st = static_cast<int>(it % kStages);
             const uint32_t ph = (it / kStages) & 1u;
             if (!mbar_wait(empty + st, ph ^ 1u, abort_flag, g.limit_ns)) {
@@ -503,8 +522,10 @@ ozaki_tc_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__
     if (lane == 0) {
       uint32_t it = 0;
       bool ok = true;
-      int wi = 0;
-      for (int w = 2; ok && w <= S + 1; ++w, ++wi) {
+      for (int wi = 0; ok && wi < npass; ++wi) {
+        const int w = 2 + wi / nch;
+        const int kb0 = (wi % nch) * ckb;
+        const int kb1 = (kb0 + ckb < nkb) ? kb0 + ckb : nkb;
         const int buf = wi & 1;
         const uint32_t use = static_cast<uint32_t>(wi >> 1);
         if (!mbar_wait(acc_empty + buf, (use & 1u) ^ 1u, abort_flag, g.limit_ns)) {
@@ -515,7 +536,7 @@ ozaki_tc_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__
         const uint32_t d_acc = tmem + static_cast<uint32_t>(buf * BN);
         uint32_t accumulate = 0u;
         for (int s = 1; ok && s <= w - 1; ++s) {
-          for (int kb = 0; kb < nkb; ++kb, ++it) {
+          for (int kb = kb0; kb < kb1; ++kb, ++it) {
             const int st = static_cast<int>(it % kStages);
             if (!mbar_wait(full + st, (it / kStages) & 1u, abort_flag, g.limit_ns)) {
               ok = false;
@@ -544,8 +565,8 @@ ozaki_tc_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__
     const int q = warp & 3;
     const uint32_t lane_base = static_cast<uint32_t>(32 * q) << 16;
     bool ok = true;
-    int wi = 0;
-    for (int w = 2; w <= S + 1; ++w, ++wi) {
+    for (int wi = 0; wi < npass; ++wi) {
+      const int w = 2 + wi / nch;
       const int buf = wi & 1;
       const uint32_t use = static_cast<uint32_t>(wi >> 1);
       if (!mbar_wait(acc_full + buf, use & 1u, abort_flag, g.limit_ns)) {
@@ -694,8 +715,8 @@ int b200_gemm_split(const double* A, const double* B, double* C, int64_t m, int6
   const int engine = (tune && tune->algo) ? tune->algo : 0;
   if (engine != 0 && engine != 1) return invalid("b200_gemm_split: engine %d (0 or 1)", engine);
   if (k > kMaxK)
-    return invalid("b200_gemm_split: k = %lld exceeds %lld (FP32 exactness bound)",
-                   static_cast<long long>(k), static_cast<long long>(kMaxK));
+    return invalid("b200_gemm_split: k = %lld exceeds %lld", static_cast<long long>(k),
+                   static_cast<long long>(kMaxK));
   if (m == 0 || n == 0) return B200_OK;
   SplitLayout L = split_layout(m, n, k, S);
   if (!workspace || workspace_bytes < L.total) {

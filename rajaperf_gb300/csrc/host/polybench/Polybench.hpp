@@ -20,14 +20,19 @@ RAJAPERF_GB300_KERNEL(POLYBENCH_HEAT_3D,
   Index_type m_N = 0, m_tsteps = 0;
   Real_ptr m_A = nullptr, m_B = nullptr, m_Ainit = nullptr, m_Binit = nullptr;)
 
+// FDTD_2D runs one launch per time step (b200_polybench_fdtd_2d_ws, the
+// tile-edge snapshots in m_ws); a tuning with algo 1 runs the two-launch form.
 RAJAPERF_GB300_KERNEL(POLYBENCH_FDTD_2D,
  private:
   Index_type m_nx = 0, m_ny = 0, m_tsteps = 0;
-  Real_ptr m_fict = nullptr, m_ex = nullptr, m_ey = nullptr, m_hz = nullptr;)
+  Real_ptr m_fict = nullptr, m_ex = nullptr, m_ey = nullptr, m_hz = nullptr;
+  void* m_ws = nullptr;
+  size_t m_ws_bytes = 0;)
 
 // GEMM and 3MM tunings: "default"/"graph" run the native FP64 kernel;
 // "split_bf16"/"split_bf16_graph" run the split-precision tensor-core GEMM
-// (b200_gemm_split; inner dimensions up to 8192).
+// (b200_gemm_split; inner dimensions up to 524288, summed in exact chunks
+// of 8192).
 RAJAPERF_GB300_KERNEL(POLYBENCH_GEMM,
  public:
   void finishRun(size_t tune_idx) override;

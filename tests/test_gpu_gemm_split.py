@@ -102,12 +102,32 @@ def test_split_fewer_slices_is_less_accurate():
     assert 1e-9 < e4 < 1e-3
 
 
-def test_split_rejects_large_k():
+@pytest.mark.parametrize("engine", ENGINES)
+@pytest.mark.parametrize("m,n,k,positive", [(64, 96, 8193, False), (130, 72, 9830, False),
+                                            (32, 40, 20000, False), (64, 64, 9830, True),
+                                            (16, 24, 24577, True)])
+def test_split_k_beyond_one_chunk(m, n, k, positive, engine):
+    """K above 8192 runs in chunks of at most 8192 whose exact FP32 sums are
+    folded into the FP64 accumulator (the suite's GEMM shape has nk = 1.2 N,
+    9830 at N = 8192).  The reference is formed in long double."""
+    rng = np.random.default_rng(k + m)
+    lo = 0.0 if positive else -1.0
+    A, B = rng.uniform(lo, 1, (m, k)), rng.uniform(lo, 1, (k, n))
+    C = rng.uniform(-1, 1, (m, n))
+    got = run_split(A, B, C, 1.5, 1.2, engine=engine)
+    want = (1.5 * (A.astype(np.longdouble) @ B.astype(np.longdouble))
+            + 1.2 * C.astype(np.longdouble))
+    err = float(np.linalg.norm((got - want).astype(np.float64)) /
+                np.linalg.norm(want.astype(np.float64)))
+    assert err <= REL_FROB, err
+
+
+def test_split_rejects_too_large_k():
     torch = gu.torch_cuda()
     L = rp.b200()
     x = torch.zeros(16, dtype=torch.float64, device="cuda")
-    assert L.b200_gemm_split(x.data_ptr(), x.data_ptr(), x.data_ptr(), 1, 1, 8193, 1.0, 0.0,
-                             x.data_ptr(), 128, None, None) == rp.B200_ERR_INVALID_ARG
+    assert L.b200_gemm_split(x.data_ptr(), x.data_ptr(), x.data_ptr(), 1, 1, 64 * 8192 + 1,
+                             1.0, 0.0, x.data_ptr(), 128, None, None) == rp.B200_ERR_INVALID_ARG
 
 
 def test_engines_bit_identical_when_accumulation_is_exact():
