@@ -184,6 +184,193 @@ fdtd2d_h(const double* __restrict__ ex, const double* __restrict__ ey,
   }
 }
 
+// ---- FDTD_2D, one launch per time step ------------------------------------------
+// A CTA owns a tile of kFdtdRows rows x kFdtdCols columns (one thread per
+// column) and runs the whole time step on it in place: phase 1 updates ex
+// and ey (BODY1-3) of its points, keeping the new values in shared memory,
+// phase 2 updates hz (BODY4) from them.  H at the tile's last column and row
+// needs new ex one column to the right and new ey one row below; the tile
+// computes those from the neighbours' old values (a right halo column and a
+// bottom halo row, 2 FP64 instructions per halo point, issued as full warps).
+// Old values across tile edges cannot come from the arrays, since the
+// neighbouring tiles update theirs in place during the same launch: they come
+// from a snapshot of every tile's edges (its first row's hz and ey, its last
+// row's hz, its first column's hz and ex, its last column's hz) as they were
+// at the start of the step.  Each tile writes its new edges into the other
+// snapshot buffer for the next step, and a small kernel takes the first
+// snapshot.  Per point and step the kernel reads hz, ex, ey and writes them
+// once (48 bytes; the two-launch form moves 72) and issues the same 8 FP64
+// instructions per point in the same forms as fdtd2d_e / fdtd2d_h, so the
+// results are bit-identical.
+constexpr int kFdtdCols = 128;  // threads per CTA
+constexpr int kFdtdRows = 32;
+
+struct FdtdSnap {
+  double* top_hz;    // [tile rows][ny]: hz of each tile's first row
+  double* top_ey;    // [tile rows][ny]: ey of each tile's first row
+  double* bot_hz;    // [tile rows][ny]: hz of each tile's last row
+  double* left_hz;   // [tile cols][nx]: hz of each tile's first column
+  double* left_ex;   // [tile cols][nx]: ex of each tile's first column
+  double* right_hz;  // [tile cols][nx]: hz of each tile's last column
+};
+
+__global__ void fdtd2d_snap_init(const double* __restrict__ ex, const double* __restrict__ ey,
+                                 const double* __restrict__ hz, int64_t nx, int64_t ny,
+                                 int64_t ntx, int64_t nty, FdtdSnap s) {
+  const int64_t nrow = nty * ny, total = nrow + ntx * nx;
+  for (int64_t idx = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; idx < total;
+       idx += static_cast<int64_t>(gridDim.x) * blockDim.x) {
+    if (idx < nrow) {
+      const int64_t by = idx / ny, j = idx - by * ny;
+      const int64_t i0 = by * kFdtdRows;
+      const int64_t il = (i0 + kFdtdRows < nx ? i0 + kFdtdRows : nx) - 1;
+      s.top_hz[idx] = hz[i0 * ny + j];
+      s.top_ey[idx] = ey[i0 * ny + j];
+      s.bot_hz[idx] = hz[il * ny + j];
+    } else {
+      const int64_t k = idx - nrow;
+      const int64_t bx = k / nx, i = k - bx * nx;
+      const int64_t j0 = bx * kFdtdCols;
+      const int64_t jl = (j0 + kFdtdCols < ny ? j0 + kFdtdCols : ny) - 1;
+      s.left_hz[k] = hz[i * ny + j0];
+      s.left_ex[k] = ex[i * ny + j0];
+      s.right_hz[k] = hz[i * ny + jl];
+    }
+  }
+}
+
+__global__ void __launch_bounds__(kFdtdCols, 3)
+fdtd2d_step_fused(double* __restrict__ ex, double* __restrict__ ey, double* __restrict__ hz,
+                  const double* __restrict__ fict, int64_t t, int64_t nx, int64_t ny,
+                  FdtdSnap in, FdtdSnap out, int zero) {
+  extern __shared__ __align__(16) double s_fdtd[];
+  // new ex [rows][cols + 1] (column kFdtdCols: the right halo), new ey
+  // [rows + 1][cols] (row kFdtdRows: the bottom halo), new hz of the first
+  // and last column
+  double (*sEx)[kFdtdCols + 1] = reinterpret_cast<double (*)[kFdtdCols + 1]>(s_fdtd);
+  double (*sEy)[kFdtdCols] =
+      reinterpret_cast<double (*)[kFdtdCols]>(s_fdtd + kFdtdRows * (kFdtdCols + 1));
+  double* sHzFirst = s_fdtd + kFdtdRows * (kFdtdCols + 1) + (kFdtdRows + 1) * kFdtdCols;
+  double* sHzLast = sHzFirst + kFdtdRows;
+
+  const int tid = threadIdx.x, lane = tid & 31;
+  const int64_t bx = blockIdx.x, by = blockIdx.y;
+  const int64_t j0 = bx * kFdtdCols, i0 = by * kFdtdRows;
+  const int64_t j = j0 + tid;
+  const int rows = static_cast<int>(nx - i0 < kFdtdRows ? nx - i0 : kFdtdRows);
+  const int cols = static_cast<int>(ny - j0 < kFdtdCols ? ny - j0 : kFdtdCols);
+  const bool col_ok = tid < cols;
+  const fform::Regs fr = fform::regs(zero);
+  const double mhalf = fform::reg(-0.5, zero);
+  const double m07 = fform::reg(-0.7, zero);
+  const double f = ld(fict + t);
+
+  // ---- phase 1: BODY1-3 (ex, ey) ----
+  double h_old[kFdtdRows];
+  double hup = (i0 > 0 && col_ok) ? in.bot_hz[(by - 1) * ny + j] : 0.0;
+#pragma unroll
+  for (int r = 0; r < kFdtdRows; ++r) {
+    h_old[r] = 0.0;
+    if (r < rows) {
+      const int64_t i = i0 + r;
+      const int64_t c = i * ny + j;
+      double h = 0.0, exo = 0.0, eyo = 0.0;
+      if (col_ok) {
+        h = hz[c];
+        exo = ex[c];
+        eyo = ey[c];
+      }
+      double hl = __shfl_up_sync(0xffffffffu, h, 1);
+      if (lane == 0) {
+        if (tid == 0) hl = (j0 > 0) ? in.right_hz[(bx - 1) * nx + i] : 0.0;
+        else if (col_ok) hl = hz[c - 1];  // this tile's column, not yet rewritten
+      }
+      const double eyn = (i == 0) ? f : fma(mhalf, fform::sub(h, hup, fr), eyo);
+      const double exn = (j == 0) ? exo : fma(mhalf, fform::sub(h, hl, fr), exo);
+      if (col_ok) {
+        ex[c] = exn;
+        ey[c] = eyn;
+      }
+      sEx[r][tid] = exn;
+      sEy[r][tid] = eyn;
+      h_old[r] = h;
+      hup = h;
+    }
+  }
+  // bottom halo: new ey one row below the tile (needed when that row exists)
+  if (i0 + kFdtdRows < nx && col_ok) {
+    const int64_t k = (by + 1) * ny + j;
+    sEy[kFdtdRows][tid] = fma(mhalf, fform::sub(in.top_hz[k], h_old[kFdtdRows - 1], fr),
+                              in.top_ey[k]);
+  }
+  // right halo: new ex one column right of the tile, one row per lane of the
+  // last warp (full-warp FP64 instructions)
+  if (tid >= kFdtdCols - 32 && j0 + kFdtdCols < ny && lane < rows) {
+    const int64_t i = i0 + lane;
+    const int64_t k = (bx + 1) * nx + i;
+    const double hl = hz[i * ny + j0 + kFdtdCols - 1];  // old: read before phase 2
+    sEx[lane][kFdtdCols] = fma(mhalf, fform::sub(in.left_hz[k], hl, fr), in.left_ex[k]);
+  }
+  __syncthreads();
+
+  // ---- phase 2: BODY4 (hz) and the tile's new edges ----
+#pragma unroll
+  for (int r = 0; r < kFdtdRows; ++r) {
+    if (r < rows) {
+      const int64_t i = i0 + r;
+      double hn = h_old[r];
+      if (col_ok && i < nx - 1 && j < ny - 1) {
+        // hz - 0.7 (((ex1 - ex0) + ey1) - ey0), left to right as the suite writes it
+        hn = fma(m07,
+                 fform::sub(fform::add(fform::sub(sEx[r][tid + 1], sEx[r][tid], fr),
+                                       sEy[r + 1][tid], fr),
+                            sEy[r][tid], fr),
+                 h_old[r]);
+        hz[i * ny + j] = hn;
+      }
+      if (col_ok) {
+        if (r == 0) {
+          out.top_hz[by * ny + j] = hn;
+          out.top_ey[by * ny + j] = sEy[0][tid];
+        }
+        if (r == rows - 1) out.bot_hz[by * ny + j] = hn;
+        if (tid == 0) sHzFirst[r] = hn;
+        if (tid == cols - 1) sHzLast[r] = hn;
+      }
+    }
+  }
+  __syncthreads();
+  if (tid < 32 && lane < rows) {
+    const int64_t k = bx * nx + i0 + lane;
+    out.left_hz[k] = sHzFirst[lane];
+    out.left_ex[k] = sEx[lane][0];
+  } else if (tid >= 32 && tid < 64 && lane < rows) {
+    out.right_hz[bx * nx + i0 + lane] = sHzLast[lane];
+  }
+}
+
+constexpr size_t kFdtdSmem =
+    sizeof(double) * (kFdtdRows * (kFdtdCols + 1) + (kFdtdRows + 1) * kFdtdCols + 2 * kFdtdRows);
+
+int64_t fdtd_tile_rows(int64_t nx) { return (nx + kFdtdRows - 1) / kFdtdRows; }
+int64_t fdtd_tile_cols(int64_t ny) { return (ny + kFdtdCols - 1) / kFdtdCols; }
+// doubles of one snapshot
+int64_t fdtd_snap_doubles(int64_t nx, int64_t ny) {
+  return 3 * fdtd_tile_rows(nx) * ny + 3 * fdtd_tile_cols(ny) * nx;
+}
+
+FdtdSnap fdtd_snap_at(double* base, int64_t nx, int64_t ny) {
+  const int64_t rowv = fdtd_tile_rows(nx) * ny, colv = fdtd_tile_cols(ny) * nx;
+  FdtdSnap s;
+  s.top_hz = base;
+  s.top_ey = base + rowv;
+  s.bot_hz = base + 2 * rowv;
+  s.left_hz = base + 3 * rowv;
+  s.left_ex = base + 3 * rowv + colv;
+  s.right_hz = base + 3 * rowv + 2 * colv;
+  return s;
+}
+
 // ---- mixed FP64-pipe / integer-pipe stencils ----------------------------------
 // A CTA of 8 warps owns a tile of 32 contiguous columns.  Warps [0, E) compute
 // their rows with the integer-pipe emulation (b200_f64emu.cuh), warps [E, 8)
@@ -490,6 +677,45 @@ int b200_polybench_fdtd_2d(double* ex, double* ey, double* hz, const double* fic
   }
   int per = (nx > 1 && ny > 1) ? 2 : 1;
   return after_launch("b200_polybench_fdtd_2d", static_cast<int>(per * tsteps));
+}
+
+size_t b200_fdtd_2d_workspace_bytes(int64_t nx, int64_t ny) {
+  if (nx <= 0 || ny <= 0) return 0;
+  return 2 * static_cast<size_t>(fdtd_snap_doubles(nx, ny)) * sizeof(double);
+}
+
+int b200_polybench_fdtd_2d_ws(double* ex, double* ey, double* hz, const double* fict,
+                              int64_t nx, int64_t ny, int64_t tsteps, void* workspace,
+                              size_t workspace_bytes, const b200_tune* tune,
+                              b200_stream_t stream) {
+  if (!ex || !ey || !hz || !fict || nx < 0 || ny < 0 || tsteps < 0)
+    return invalid("b200_polybench_fdtd_2d_ws: bad args");
+  const int algo = tune ? tune->algo : 0;
+  if (algo != 0 && algo != 1) return invalid("b200_polybench_fdtd_2d_ws: algo %d (0 or 1)", algo);
+  if (algo == 1) return b200_polybench_fdtd_2d(ex, ey, hz, fict, nx, ny, tsteps, tune, stream);
+  if (nx == 0 || ny == 0 || tsteps == 0) return B200_OK;
+  if (fdtd_tile_rows(nx) > 65535) return invalid("b200_polybench_fdtd_2d_ws: nx too large");
+  const size_t need = b200_fdtd_2d_workspace_bytes(nx, ny);
+  if (!workspace || workspace_bytes < need) {
+    set_error("b200_polybench_fdtd_2d_ws: workspace %zu bytes, need %zu", workspace_bytes, need);
+    return B200_ERR_WORKSPACE;
+  }
+  const int rc = allow_dynamic_smem(reinterpret_cast<const void*>(fdtd2d_step_fused), kFdtdSmem,
+                                    "b200_polybench_fdtd_2d_ws");
+  if (rc != B200_OK) return rc;
+  cudaStream_t st = as_stream(stream);
+  double* w = static_cast<double*>(workspace);
+  const FdtdSnap snap[2] = {fdtd_snap_at(w, nx, ny),
+                            fdtd_snap_at(w + fdtd_snap_doubles(nx, ny), nx, ny)};
+  const int64_t ntx = fdtd_tile_cols(ny), nty = fdtd_tile_rows(nx);
+  const int64_t total = nty * ny + ntx * nx;
+  const unsigned ig = static_cast<unsigned>(std::min<int64_t>(ceil_div(total, 256), 4096));
+  fdtd2d_snap_init<<<ig, 256, 0, st>>>(ex, ey, hz, nx, ny, ntx, nty, snap[0]);
+  const dim3 g(static_cast<unsigned>(ntx), static_cast<unsigned>(nty));
+  for (int64_t t = 0; t < tsteps; ++t)
+    fdtd2d_step_fused<<<g, kFdtdCols, kFdtdSmem, st>>>(ex, ey, hz, fict, t, nx, ny, snap[t & 1],
+                                                       snap[(t + 1) & 1], 0);
+  return after_launch("b200_polybench_fdtd_2d_ws", static_cast<int>(1 + tsteps));
 }
 
 int b200_polybench_gemm(const double* A, const double* B, double* C, int64_t ni,

@@ -39,6 +39,9 @@ POLYBENCH_FDTD_2D::POLYBENCH_FDTD_2D(const RunParams& params)
                                    getActualProblemSize());
   setComplexity(Complexity::N);
   setUsesFeature(Kernel);
+  b200_tune two_launch{};
+  two_launch.algo = 1;  // BODY1-3 and BODY4 as two launches per time step
+  addTuning("two_launch", two_launch, false);
   setVariantDefined(Base_GB300);
 }
 
@@ -47,13 +50,16 @@ void POLYBENCH_FDTD_2D::setUp(VariantID vid, size_t) {
   allocAndInitData(m_ex, m_nx * m_ny, vid);
   allocAndInitData(m_ey, m_nx * m_ny, vid);
   allocAndInitData(m_fict, m_tsteps, vid);
+  m_ws_bytes = b200_fdtd_2d_workspace_bytes(m_nx, m_ny);
+  m_ws = m_ws_bytes ? allocDeviceBytes(m_ws_bytes) : nullptr;
 }
 
 KernelBase::RepBody POLYBENCH_FDTD_2D::makeRepBody(size_t tune_idx) {
   const b200_tune tn = getTune(tune_idx);
   return [=](b200_stream_t s) {
-    checkB200(b200_polybench_fdtd_2d(m_ex, m_ey, m_hz, m_fict, m_nx, m_ny, m_tsteps, &tn, s),
-              "b200_polybench_fdtd_2d");
+    checkB200(b200_polybench_fdtd_2d_ws(m_ex, m_ey, m_hz, m_fict, m_nx, m_ny, m_tsteps, m_ws,
+                                        m_ws_bytes, &tn, s),
+              "b200_polybench_fdtd_2d_ws");
   };
 }
 
@@ -66,6 +72,8 @@ void POLYBENCH_FDTD_2D::tearDown(VariantID vid, size_t) {
   deallocData(m_ex, vid);
   deallocData(m_ey, vid);
   deallocData(m_hz, vid);
+  deallocDeviceBytes(m_ws);
+  m_ws = nullptr;
 }
 
 }  // namespace polybench

@@ -164,6 +164,42 @@ def test_fdtd_2d(nx, ny, ts):
         close(gu.host(g), w)
 
 
+@pytest.mark.parametrize("nx,ny,ts", [(1, 1, 2), (1, 7, 2), (7, 1, 3), (2, 2, 1), (33, 129, 3),
+                                     (32, 128, 2), (64, 256, 4), (100, 300, 5), (257, 1000, 3)])
+def test_fdtd_2d_one_launch_per_step(nx, ny, ts):
+    """The fused step (one launch per time step, tile edges from snapshots) is
+    bit-identical to the two-launch form, tiles cut across rows and columns
+    and partial last tiles included, and the workspace needs no zeroing."""
+    rng = np.random.default_rng(nx * 1000 + ny)
+    ex, ey, hz = (rng.uniform(0.5, 1.5, nx * ny) for _ in range(3))
+    fict = rng.uniform(0.5, 1.5, ts)
+    d1 = [dev(a) for a in (ex, ey, hz)]
+    d2 = [dev(a) for a in (ex, ey, hz)]
+    df = dev(fict)
+    rp.check(lib().b200_polybench_fdtd_2d(d1[0].data_ptr(), d1[1].data_ptr(), d1[2].data_ptr(),
+                                          df.data_ptr(), nx, ny, ts, None, gu.stream()))
+    wb = lib().b200_fdtd_2d_workspace_bytes(nx, ny)
+    torch = gu.torch_cuda()
+    w = torch.full((wb,), 0x7F, dtype=torch.uint8, device="cuda")
+    rp.check(lib().b200_polybench_fdtd_2d_ws(d2[0].data_ptr(), d2[1].data_ptr(), d2[2].data_ptr(),
+                                             df.data_ptr(), nx, ny, ts, w.data_ptr(), wb, None,
+                                             gu.stream()))
+    for a, b in zip(d1, d2):
+        assert np.array_equal(gu.host(a), gu.host(b))
+    oracle.call("oracle_fdtd_2d", ex, ey, hz, fict, nx, ny, ts)
+    for g, w_ in zip(d2, (ex, ey, hz)):
+        close(gu.host(g), w_)
+
+
+def test_fdtd_2d_ws_rejects_small_workspace():
+    torch = gu.torch_cuda()
+    x = torch.zeros(64 * 64, dtype=torch.float64, device="cuda")
+    wb = lib().b200_fdtd_2d_workspace_bytes(64, 64)
+    assert lib().b200_polybench_fdtd_2d_ws(x.data_ptr(), x.data_ptr(), x.data_ptr(), x.data_ptr(),
+                                           64, 64, 1, x.data_ptr(), wb - 8, None,
+                                           None) == rp.B200_ERR_WORKSPACE
+
+
 SCAN_TUNES = {"pipelined": dict(), "tile4096": dict(algo=1, items=16),
               "tile8192": dict(algo=1, items=32)}
 
