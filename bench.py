@@ -12,9 +12,9 @@ of the suite).  One "step" runs every kernel of the workload once.
 * value: kernels timed with CUDA events on the launching stream, inputs
   resident in HBM, L2 flushed before every kernel (a 256 MiB write, then two
   256 MiB reads of another buffer so no dirty flush lines remain).
-* e2e: the same metric through the C ABI with host buffers: each step copies
-  the kernel's inputs from pinned host memory, runs it and reads the
-  result back, all inside the timed region.
+* e2e: the same metric through the Base_GB300 suite layer (rp_run) with the
+  kernels' arrays in pinned host memory (--host-data): every rep moves its
+  inputs from host memory and its outputs back inside the timed region.
 * cpu_baseline / --impl reference: the suite's Base_OpenMP loops (the CPU
   oracle's restatement) on all host cores, one rep per kernel at full size.
 Under torchrun (N>1) every rank runs its own replica (the path has no data
@@ -80,13 +80,7 @@ class Case:
     def zeros(self, n, dtype=None):
         return self.torch.zeros(n, dtype=dtype or self.torch.float64, device="cuda")
 
-    # subclasses define: inputs (list of device tensors copied H2D in e2e),
-    # outputs (tensors read back in e2e), bytes_per_rep, run(stream)
-    def inputs(self):
-        return []
-
-    def outputs(self):
-        return []
+    # subclasses define bytes_per_rep and run(stream)
 
 
 def _stream_cases():
@@ -101,11 +95,7 @@ def _stream_cases():
             self.c = self.uniform(n)
             self.bytes_per_rep = 24 * n
 
-        def inputs(self):
-            return [self.b, self.c]
 
-        def outputs(self):
-            return [self.a]
 
         def run(self, s):
             return self.L.b200_stream_triad(self.a.data_ptr(), self.b.data_ptr(),
@@ -121,11 +111,7 @@ def _stream_cases():
             self.c = self.zeros(n)
             self.bytes_per_rep = 16 * n
 
-        def inputs(self):
-            return [self.a]
 
-        def outputs(self):
-            return [self.c]
 
         def run(self, s):
             return self.L.b200_stream_copy(self.a.data_ptr(), self.c.data_ptr(), self.n,
@@ -141,11 +127,7 @@ def _stream_cases():
             self.c = self.uniform(n)
             self.bytes_per_rep = 16 * n
 
-        def inputs(self):
-            return [self.c]
 
-        def outputs(self):
-            return [self.b]
 
         def run(self, s):
             return self.L.b200_stream_mul(self.b.data_ptr(), self.c.data_ptr(), 0.5, self.n,
@@ -162,11 +144,7 @@ def _stream_cases():
             self.c = self.zeros(n)
             self.bytes_per_rep = 24 * n
 
-        def inputs(self):
-            return [self.a, self.b]
 
-        def outputs(self):
-            return [self.c]
 
         def run(self, s):
             return self.L.b200_stream_add(self.a.data_ptr(), self.b.data_ptr(),
@@ -185,11 +163,7 @@ def _stream_cases():
             self.ws = self.zeros(self.ws_bytes, dtype=torch.uint8)
             self.bytes_per_rep = 16 * n + 16
 
-        def inputs(self):
-            return [self.a, self.b]
 
-        def outputs(self):
-            return [self.acc]
 
         def run(self, s):
             return self.L.b200_stream_dot(self.a.data_ptr(), self.b.data_ptr(), self.n, 0.0,
@@ -238,12 +212,6 @@ def _bandwidth_cases():
             # integer and FP32 pipes), BODY2+BODY3 20 per point
             self.fp64_instr_per_rep = 30 * (kn - 2) * (jn - 2)
 
-        def inputs(self):
-            return self.arr[2:9]
-
-        def outputs(self):
-            return [self.arr[6], self.arr[7], self.arr[9], self.arr[10]]
-
         def run(self, s):
             a = [t.data_ptr() for t in self.arr]
             return self.L.b200_lcals_hydro_2d(*a, 0.0041, 0.0037, self.kn, self.jn, None, s)
@@ -260,11 +228,7 @@ def _bandwidth_cases():
             self.flops_per_rep = 16 * n
             self.fp64_instr_per_rep = 8 * n
 
-        def inputs(self):
-            return [self.y, self.z, self.u]
 
-        def outputs(self):
-            return [self.x]
 
         def run(self, s):
             return self.L.b200_lcals_eos(self.x.data_ptr(), self.y.data_ptr(), self.z.data_ptr(),
@@ -283,11 +247,7 @@ def _bandwidth_cases():
             self.flops_per_rep = n
             self.fp64_instr_per_rep = n
 
-        def inputs(self):
-            return [self.y]
 
-        def outputs(self):
-            return [self.x]
 
         def run(self, s):
             return self.L.b200_lcals_first_diff(self.x.data_ptr(), self.y.data_ptr(), self.n,
@@ -309,11 +269,7 @@ def _bandwidth_cases():
             self.flops_per_rep = 0
             self.fp64_instr_per_rep = 0
 
-        def inputs(self):
-            return [self.x]
 
-        def outputs(self):
-            return [self.loc]
 
         def run(self, s):
             return self.L.b200_lcals_first_min(self.x.data_ptr(), self.n, 0.5, 0,
@@ -339,11 +295,7 @@ def _bandwidth_cases():
             # products and + ptiny off the FP64 pipe
             self.fp64_instr_per_rep = 33 * self.nz
 
-        def inputs(self):
-            return [self.x, self.y, self.xdot, self.ydot, self.zones]
 
-        def outputs(self):
-            return [self.div]
 
         def run(self, s):
             return self.L.b200_apps_del_dot_vec_2d(
@@ -364,11 +316,7 @@ def _bandwidth_cases():
             self.flops_per_rep = tsteps * 10 * (N - 2) * (N - 2)
             self.fp64_instr_per_rep = tsteps * 8 * (N - 2) * (N - 2)  # 4 adds per point per half-step
 
-        def inputs(self):
-            return [self.A, self.B]
 
-        def outputs(self):
-            return [self.A, self.B]
 
         def run(self, s):
             return self.L.b200_polybench_jacobi_2d(self.A.data_ptr(), self.B.data_ptr(), self.N,
@@ -388,11 +336,7 @@ def _bandwidth_cases():
             self.flops_per_rep = tsteps * 30 * inner
             self.fp64_instr_per_rep = tsteps * 18 * inner  # 9 adds per point per half-step
 
-        def inputs(self):
-            return [self.A, self.B]
 
-        def outputs(self):
-            return [self.A, self.B]
 
         def run(self, s):
             return self.L.b200_polybench_heat_3d(self.A.data_ptr(), self.B.data_ptr(), self.N,
@@ -416,11 +360,7 @@ def _bandwidth_cases():
             self.flops_per_rep = tsteps * (3 * (nx - 1) * ny + 3 * nx * (ny - 1) +
                                            5 * (nx - 1) * (ny - 1))
 
-        def inputs(self):
-            return [self.ex, self.ey, self.hz, self.fict]
 
-        def outputs(self):
-            return [self.hz]
 
         def run(self, s):
             return self.L.b200_polybench_fdtd_2d(self.ex.data_ptr(), self.ey.data_ptr(),
@@ -442,11 +382,7 @@ def _bandwidth_cases():
             self.flops_per_rep = n
             self.fp64_instr_per_rep = 0
 
-        def inputs(self):
-            return [self.x]
 
-        def outputs(self):
-            return [self.y]
 
         def run(self, s):
             return self.L.b200_algorithm_scan_i64(self.x.data_ptr(), self.y.data_ptr(), self.n,
@@ -862,8 +798,8 @@ def run_gpu(args, rank, world):
     step_s = sum(p["ms"] for p in per_kernel) / 1e3
     value = 100.0 * geomean([p["frac"] for p in per_kernel])
 
-    # e2e through the C ABI with host buffers
-    e2e = None if args.no_e2e else run_e2e(torch, rp, cases, s, stream, args, peaks)
+    # e2e through the suite layer with host-resident data
+    e2e = None if args.no_e2e else run_e2e(torch, rp, args, peaks)
 
     dom = max(per_kernel, key=lambda p: p["ms"])
     tr = traffic.get(dom["kernel"])
@@ -901,7 +837,7 @@ def measure_gemm(torch, rp, stream, sizes=(1024, 4096, 8192), seed=4793):
     L = rp.b200()
     s = stream.cuda_stream
     legacy = rp.Tune(algo=1)  # the mma.sync engine, for comparison
-    slices = 11
+    slices = 10  # the library default (b200_gemm_split)
     pairs = slices * (slices + 1) // 2  # slice products formed per C element
     out = []
     for n in sizes:
@@ -941,6 +877,12 @@ def measure_gemm(torch, rp, stream, sizes=(1024, 4096, 8192), seed=4793):
             res[f"C_{name}"] = C
         err = (res["C_split"] - res["C_native"]).norm() / res["C_native"].norm()
         res["rel_err_vs_fp64"] = float(err)
+        # an independent FP64 result: cuBLAS DGEMM through torch.matmul
+        ref = torch.addmm(C0, A, B, beta=1.2, alpha=1.5)
+        rn = ref.norm()
+        res["rel_err_split_vs_cublas_fp64"] = float((res["C_split"] - ref).norm() / rn)
+        res["rel_err_native_vs_cublas_fp64"] = float((res["C_native"] - ref).norm() / rn)
+        del ref
         res["speedup"] = round(res["split_tflops"] / res["native_tflops"], 2)
         res["speedup_vs_mma_sync"] = round(res["split_tflops"] / res["split_mma_sync_tflops"], 2)
         # bf16 tensor work actually issued: `pairs` slice products of 2*n^3 each
@@ -957,10 +899,57 @@ def measure_gemm(torch, rp, stream, sizes=(1024, 4096, 8192), seed=4793):
                                        1.5, 1.2, ws.data_ptr(), ws_bytes, None, s))
             torch.cuda.synchronize()
             res["row_scaled_rel_err"] = float((Cs - Cn).norm() / Cn.norm())
+        st = L.b200_workspace_status(ws.data_ptr(), ws_bytes, s)
+        res["workspace_status"] = "ok" if st == 0 else f"error {st}: {rp.last_error()}"
         out.append(res)
         del A, B, C0, ws
         torch.cuda.empty_cache()
+    out.append(measure_gemm_suite_shape(torch, rp, stream, sizes[-1], seed))
     return out
+
+
+def measure_gemm_suite_shape(torch, rp, stream, n, seed):
+    """The suite's own GEMM shape (POLYBENCH_GEMM.cpp: nk = 1.2 ni) at ni = nj
+    = n: C = A*B with K = 1.2 n (9830 at n = 8192, two exact FP32 chunks),
+    split precision against native FP64 and cuBLAS FP64."""
+    L = rp.b200()
+    s = stream.cuda_stream
+    k = int(1.2 * n)
+    g = torch.Generator(device="cuda").manual_seed(seed + 7 * n)
+    A = torch.rand(n, k, dtype=torch.float64, device="cuda", generator=g) * 2 - 1
+    B = torch.rand(k, n, dtype=torch.float64, device="cuda", generator=g) * 2 - 1
+    wb = L.b200_gemm_split_workspace_bytes(n, n, k, None)
+    ws = torch.zeros(wb, dtype=torch.uint8, device="cuda")
+    res = {"m": n, "n": n, "k": k, "shape": "suite GEMM (nk = 1.2 ni)"}
+    Cs = torch.zeros(n, n, dtype=torch.float64, device="cuda")
+    Cn = torch.zeros(n, n, dtype=torch.float64, device="cuda")
+    for name, C, fn in (("split", Cs, lambda: L.b200_gemm_split(
+                            A.data_ptr(), B.data_ptr(), Cs.data_ptr(), n, n, k, 1.0, 0.0,
+                            ws.data_ptr(), wb, None, s)),
+                        ("native", Cn, lambda: L.b200_gemm_f64(
+                            A.data_ptr(), B.data_ptr(), Cn.data_ptr(), n, n, k, 1.0, 0.0,
+                            None, s))):
+        rp.check(fn(), name)
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        rp.check(fn(), name)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        t = e0.elapsed_time(e1) / 1e3
+        res[f"{name}_ms"] = round(t * 1e3, 3)
+        res[f"{name}_tflops"] = round(2.0 * n * n * k / t / 1e12, 3)
+    ref = torch.matmul(A, B)
+    rn = ref.norm()
+    res["rel_err_split_vs_cublas_fp64"] = float((Cs - ref).norm() / rn)
+    res["rel_err_native_vs_cublas_fp64"] = float((Cn - ref).norm() / rn)
+    res["rel_err_split_vs_native"] = float((Cs - Cn).norm() / Cn.norm())
+    res["speedup"] = round(res["split_tflops"] / res["native_tflops"], 2)
+    st = L.b200_workspace_status(ws.data_ptr(), wb, s)
+    res["workspace_status"] = "ok" if st == 0 else f"error {st}: {rp.last_error()}"
+    del A, B, Cs, Cn, ref, ws
+    torch.cuda.empty_cache()
+    return res
 
 
 def measure_3mm(torch, rp, stream, n=2048, seed=4793):
@@ -1094,35 +1083,90 @@ def measure_fp64_peak(torch, rp, stream):
             "probe_gflops": round(2.0 * probe / 1e9, 1), "dgemm_gflops": round(2.0 * gemm / 1e9, 1)}
 
 
-def run_e2e(torch, rp, cases, s, stream, args, peaks):
-    """Host buffers -> H2D -> kernel -> D2H, timed with events."""
-    host_in = [[x.cpu().pin_memory() for x in c.inputs()] for c in cases]
-    host_out = [[torch.empty(x.shape, dtype=x.dtype).pin_memory() for x in c.outputs()]
-                for c in cases]
-    h2d = sum(x.numel() * x.element_size() for hs in host_in for x in hs)
-    d2h = sum(x.numel() * x.element_size() for hs in host_out for x in hs)
-    steps = max(1, min(args.steps, 5))
-    times = [[0.0] * len(cases) for _ in range(steps)]
-    for k in range(-1, steps):
-        for i, c in enumerate(cases):
+# suite options of the e2e leg per kernel (tuning, time steps)
+E2E_SUITE_ARGS = {"Polybench_JACOBI_2D": ["-t", "default", "--polybench_tsteps", 50],
+                  "Polybench_HEAT_3D": ["-t", "default", "--polybench_tsteps", 20],
+                  "Polybench_FDTD_2D": ["-t", "default", "--polybench_tsteps", 100],
+                  "Algorithm_SCAN": ["-t", "int64"]}
+
+
+def host_link_info(torch):
+    """Copy-engine rates between pinned host memory and the device (256 MiB,
+    best of 3) and the host's NUMA layout, recorded beside the e2e number."""
+    nb = 256 << 20
+    h = torch.empty(nb, dtype=torch.uint8, pin_memory=True)
+    h2 = torch.empty(nb, dtype=torch.uint8, pin_memory=True)
+    d = torch.empty(nb, dtype=torch.uint8, device="cuda")
+    d2 = torch.empty(nb, dtype=torch.uint8, device="cuda")
+
+    def best(fn):
+        t = 1e9
+        for _ in range(3):
             e0 = torch.cuda.Event(enable_timing=True)
             e1 = torch.cuda.Event(enable_timing=True)
-            e0.record(stream)
-            for dst, src in zip(c.inputs(), host_in[i]):
-                dst.copy_(src, non_blocking=True)
-            rp.check(c.run(s), c.name)
-            for dst, src in zip(host_out[i], c.outputs()):
-                dst.copy_(src, non_blocking=True)
-            e1.record(stream)
             torch.cuda.synchronize()
-            if k >= 0:
-                times[k][i] = e0.elapsed_time(e1) / 1e3
-    fr = []
-    for i, c in enumerate(cases):
-        avg = sum(times[k][i] for k in range(steps)) / steps
-        fr.append(c.bytes_per_rep / avg / 1e9 / peaks["hbm_gbs"])
+            e0.record()
+            fn()
+            e1.record()
+            torch.cuda.synchronize()
+            t = min(t, e0.elapsed_time(e1) / 1e3)
+        return t
+
+    s1, s2 = torch.cuda.Stream(), torch.cuda.Stream()
+
+    def both():
+        cur = torch.cuda.current_stream()
+        s1.wait_stream(cur)
+        s2.wait_stream(cur)
+        with torch.cuda.stream(s1):
+            d.copy_(h, non_blocking=True)
+        with torch.cuda.stream(s2):
+            h2.copy_(d2, non_blocking=True)
+        cur.wait_stream(s1)
+        cur.wait_stream(s2)
+
+    info = {"h2d_gbs": round(nb / best(lambda: d.copy_(h, non_blocking=True)) / 1e9, 1),
+            "d2h_gbs": round(nb / best(lambda: h2.copy_(d, non_blocking=True)) / 1e9, 1),
+            "both_directions_gbs_each": round(nb / best(both) / 1e9, 1)}
+    try:
+        nodes = sorted(x for x in os.listdir("/sys/devices/system/node") if x.startswith("node"))
+        info["numa_nodes"] = len(nodes)
+        info["cpus_of_numa_nodes"] = {n: open(f"/sys/devices/system/node/{n}/cpulist").read().strip()
+                                      for n in nodes}
+    except OSError:
+        pass
+    del h, h2, d, d2
+    return info
+
+
+def run_e2e(torch, rp, args, peaks):
+    """The metric end to end through the Base_GB300 suite layer (rp_run, the
+    path a user of the suite calls) with host-resident data (--host-data):
+    the kernels' arrays live in pinned host memory and every rep's timed
+    work includes moving its inputs from host memory and its outputs back --
+    streaming kernels (EOS, FIRST_DIFF, FIRST_MIN, the int64 SCAN) read and
+    write host memory themselves, the others (HYDRO_2D, DEL_DOT_VEC_2D,
+    JACOBI_2D, HEAT_3D) copy their arrays in and out around each rep.  Time
+    per rep = the suite's rep-loop time / reps."""
+    reps = max(2, min(args.steps, 5))
+    fr, per, h2d, d2h = [], [], 0, 0
+    for kname, size in workload_kernels(args.workload, args.kernels):
+        opts = E2E_SUITE_ARGS.get(kname, ["-t", "default"])
+        r = rp.run_suite(["--size", size, "--checkrun", reps, "-k", kname, "--init", "uniform",
+                          "--seed", args.seed, "--host-data", "--disable-warmup", *opts])[0]
+        t = r["min_time_s"] / r["reps"]
+        f = r["bytes_per_rep"] / t / 1e9 / peaks["hbm_gbs"]
+        fr.append(f)
+        h2d += r["h2d_bytes_per_rep"]
+        d2h += r["d2h_bytes_per_rep"]
+        per.append({"kernel": kname, "ms": round(t * 1e3, 4), "frac": round(f, 5),
+                    "h2d_bytes": r["h2d_bytes_per_rep"], "d2h_bytes": r["d2h_bytes_per_rep"],
+                    "checksum": r["checksum"]})
     return {"value": round(100.0 * geomean(fr), 3), "unit": "%",
-            "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h}
+            "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+            "path": "rp_run --host-data (the Base_GB300 suite layer, arrays in pinned host "
+                    "memory)",
+            "link": host_link_info(torch), "per_kernel": per}
 
 
 # --------------------------------------------------------------------------

@@ -382,7 +382,7 @@ size_t b200_gemm_split_workspace_bytes(int64_t m, int64_t n, int64_t k,
 
 /* C = alpha*A*B + beta*C in FP64 by split precision on bf16 tensor cores:
  * rows of A / columns of B are scaled by powers of two and cut into
- * tune->items (default 11) balanced 5-bit integer slices held exactly in
+ * tune->items (default 10) balanced 5-bit integer slices held exactly in
  * bf16; slice products of equal weight accumulate exactly in FP32 on the
  * tensor cores over chunks of at most 8192 values of k (the bound under which
  * the FP32 accumulation stays exact), each chunk folded into an FP64

@@ -7,7 +7,10 @@
  * checksum (common/DataUtils.cpp:600-621), rep-loop times and the kernel's
  * Bytes/rep and FLOPs/rep (common/KernelBase.hpp:215-225).  Command-line
  * options are those of the suite's RunParams (--size, --checkrun, -k, -t,
- * ...) plus the GB300 options listed by --help.
+ * ...) plus the GB300 options listed by --help.  With --host-data the
+ * kernels' arrays live in pinned host memory (the suite's CudaPinned data
+ * space, --cuda-data-space in common/RunParams.cpp:907-957 of the suite) and
+ * each rep's timed work includes moving its data across the host link.
  */
 #ifndef RAJAPERF_GB300_H
 #define RAJAPERF_GB300_H
@@ -37,6 +40,10 @@ typedef struct rp_result {
   int64_t flops_per_rep;
   int32_t passes;
   int32_t failed;            /* nonzero when this kernel/tuning failed   */
+  int64_t h2d_bytes_per_rep; /* --host-data: bytes a rep moves from host
+                                memory to the device (copies, or the
+                                kernel's own reads of host memory)      */
+  int64_t d2h_bytes_per_rep; /* ... and back                            */
 } rp_result;
 
 typedef struct rp_batch_result {

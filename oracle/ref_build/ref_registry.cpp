@@ -127,13 +127,23 @@ const std::string& getVariantName(VariantID vid) {
     "Base_OMPTarget", "RAJA_OMPTarget",
     "Base_CUDA", "Lambda_CUDA", "RAJA_CUDA",
     "Base_HIP", "Lambda_HIP", "RAJA_HIP",
-    "Kokkos_Lambda", "Base_SYCL", "RAJA_SYCL"};
+    "Kokkos_Lambda", "Base_SYCL", "RAJA_SYCL",
+#if defined(RAJA_PERFSUITE_ENABLE_GB300)
+    "Base_GB300",
+#endif
+  };
   if (vid < 0 || vid >= NumVariants) return unknownName();
   return names[vid];
 }
 
+#if defined(RAJA_PERFSUITE_ENABLE_GB300)
+// the suite built with the Base_GB300 variant registered (integration.py)
+bool isVariantAvailable(VariantID vid) { return vid == Base_Seq || vid == Base_GB300; }
+bool isVariantGPU(VariantID vid) { return vid == Base_GB300; }
+#else
 bool isVariantAvailable(VariantID vid) { return vid == Base_Seq; }
 bool isVariantGPU(VariantID) { return false; }
+#endif
 
 const std::string& getFeatureName(FeatureID fid) {
   static const std::vector<std::string> names = {

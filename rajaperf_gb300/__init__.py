@@ -57,7 +57,8 @@ class RpResult(ctypes.Structure):
                 ("reps", ctypes.c_int64), ("actual_size", ctypes.c_int64),
                 ("its_per_rep", ctypes.c_int64), ("kernels_per_rep", ctypes.c_int64),
                 ("bytes_per_rep", ctypes.c_int64), ("flops_per_rep", ctypes.c_int64),
-                ("passes", ctypes.c_int32), ("failed", ctypes.c_int32)]
+                ("passes", ctypes.c_int32), ("failed", ctypes.c_int32),
+                ("h2d_bytes_per_rep", ctypes.c_int64), ("d2h_bytes_per_rep", ctypes.c_int64)]
 
 
 class RpBatchResult(ctypes.Structure):
@@ -193,7 +194,8 @@ def run_suite(args: list[str], capacity: int = 256) -> list[dict]:
             "avg_time_s": r.avg_time_s, "max_time_s": r.max_time_s, "reps": r.reps,
             "actual_size": r.actual_size, "its_per_rep": r.its_per_rep,
             "kernels_per_rep": r.kernels_per_rep, "bytes_per_rep": r.bytes_per_rep,
-            "flops_per_rep": r.flops_per_rep, "passes": r.passes})
+            "flops_per_rep": r.flops_per_rep, "passes": r.passes,
+            "h2d_bytes_per_rep": r.h2d_bytes_per_rep, "d2h_bytes_per_rep": r.d2h_bytes_per_rep})
     return res
 
 

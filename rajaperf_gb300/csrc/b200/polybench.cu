@@ -202,8 +202,9 @@ fdtd2d_h(const double* __restrict__ ex, const double* __restrict__ ey,
 // once (48 bytes; the two-launch form moves 72) and issues the same 8 FP64
 // instructions per point in the same forms as fdtd2d_e / fdtd2d_h, so the
 // results are bit-identical.
-constexpr int kFdtdCols = 128;  // threads per CTA
-constexpr int kFdtdRows = 32;
+constexpr int kFdtdCols = 128;     // threads per CTA
+constexpr int kFdtdMinRows = 8;    // the workspace holds snapshots for tiles this short
+constexpr int kFdtdDefaultRows = 16;
 
 struct FdtdSnap {
   double* top_hz;    // [tile rows][ny]: hz of each tile's first row
@@ -216,14 +217,14 @@ struct FdtdSnap {
 
 __global__ void fdtd2d_snap_init(const double* __restrict__ ex, const double* __restrict__ ey,
                                  const double* __restrict__ hz, int64_t nx, int64_t ny,
-                                 int64_t ntx, int64_t nty, FdtdSnap s) {
+                                 int64_t ntx, int64_t nty, int th, FdtdSnap s) {
   const int64_t nrow = nty * ny, total = nrow + ntx * nx;
   for (int64_t idx = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; idx < total;
        idx += static_cast<int64_t>(gridDim.x) * blockDim.x) {
     if (idx < nrow) {
       const int64_t by = idx / ny, j = idx - by * ny;
-      const int64_t i0 = by * kFdtdRows;
-      const int64_t il = (i0 + kFdtdRows < nx ? i0 + kFdtdRows : nx) - 1;
+      const int64_t i0 = by * th;
+      const int64_t il = (i0 + th < nx ? i0 + th : nx) - 1;
       s.top_hz[idx] = hz[i0 * ny + j];
       s.top_ey[idx] = ey[i0 * ny + j];
       s.bot_hz[idx] = hz[il * ny + j];
@@ -239,25 +240,26 @@ __global__ void fdtd2d_snap_init(const double* __restrict__ ex, const double* __
   }
 }
 
-__global__ void __launch_bounds__(kFdtdCols, 3)
+template <int TH>
+__global__ void __launch_bounds__(kFdtdCols, (TH <= 8 ? 8 : TH <= 16 ? 5 : 3))
 fdtd2d_step_fused(double* __restrict__ ex, double* __restrict__ ey, double* __restrict__ hz,
                   const double* __restrict__ fict, int64_t t, int64_t nx, int64_t ny,
                   FdtdSnap in, FdtdSnap out, int zero) {
   extern __shared__ __align__(16) double s_fdtd[];
   // new ex [rows][cols + 1] (column kFdtdCols: the right halo), new ey
-  // [rows + 1][cols] (row kFdtdRows: the bottom halo), new hz of the first
+  // [rows + 1][cols] (row TH: the bottom halo), new hz of the first
   // and last column
   double (*sEx)[kFdtdCols + 1] = reinterpret_cast<double (*)[kFdtdCols + 1]>(s_fdtd);
   double (*sEy)[kFdtdCols] =
-      reinterpret_cast<double (*)[kFdtdCols]>(s_fdtd + kFdtdRows * (kFdtdCols + 1));
-  double* sHzFirst = s_fdtd + kFdtdRows * (kFdtdCols + 1) + (kFdtdRows + 1) * kFdtdCols;
-  double* sHzLast = sHzFirst + kFdtdRows;
+      reinterpret_cast<double (*)[kFdtdCols]>(s_fdtd + TH * (kFdtdCols + 1));
+  double* sHzFirst = s_fdtd + TH * (kFdtdCols + 1) + (TH + 1) * kFdtdCols;
+  double* sHzLast = sHzFirst + TH;
 
   const int tid = threadIdx.x, lane = tid & 31;
   const int64_t bx = blockIdx.x, by = blockIdx.y;
-  const int64_t j0 = bx * kFdtdCols, i0 = by * kFdtdRows;
+  const int64_t j0 = bx * kFdtdCols, i0 = by * TH;
   const int64_t j = j0 + tid;
-  const int rows = static_cast<int>(nx - i0 < kFdtdRows ? nx - i0 : kFdtdRows);
+  const int rows = static_cast<int>(nx - i0 < TH ? nx - i0 : TH);
   const int cols = static_cast<int>(ny - j0 < kFdtdCols ? ny - j0 : kFdtdCols);
   const bool col_ok = tid < cols;
   const fform::Regs fr = fform::regs(zero);
@@ -266,10 +268,10 @@ fdtd2d_step_fused(double* __restrict__ ex, double* __restrict__ ey, double* __re
   const double f = ld(fict + t);
 
   // ---- phase 1: BODY1-3 (ex, ey) ----
-  double h_old[kFdtdRows];
+  double h_old[TH];
   double hup = (i0 > 0 && col_ok) ? in.bot_hz[(by - 1) * ny + j] : 0.0;
 #pragma unroll
-  for (int r = 0; r < kFdtdRows; ++r) {
+  for (int r = 0; r < TH; ++r) {
     h_old[r] = 0.0;
     if (r < rows) {
       const int64_t i = i0 + r;
@@ -298,9 +300,9 @@ fdtd2d_step_fused(double* __restrict__ ex, double* __restrict__ ey, double* __re
     }
   }
   // bottom halo: new ey one row below the tile (needed when that row exists)
-  if (i0 + kFdtdRows < nx && col_ok) {
+  if (i0 + TH < nx && col_ok) {
     const int64_t k = (by + 1) * ny + j;
-    sEy[kFdtdRows][tid] = fma(mhalf, fform::sub(in.top_hz[k], h_old[kFdtdRows - 1], fr),
+    sEy[TH][tid] = fma(mhalf, fform::sub(in.top_hz[k], h_old[TH - 1], fr),
                               in.top_ey[k]);
   }
   // right halo: new ex one column right of the tile, one row per lane of the
@@ -315,7 +317,7 @@ fdtd2d_step_fused(double* __restrict__ ex, double* __restrict__ ey, double* __re
 
   // ---- phase 2: BODY4 (hz) and the tile's new edges ----
 #pragma unroll
-  for (int r = 0; r < kFdtdRows; ++r) {
+  for (int r = 0; r < TH; ++r) {
     if (r < rows) {
       const int64_t i = i0 + r;
       double hn = h_old[r];
@@ -349,18 +351,19 @@ fdtd2d_step_fused(double* __restrict__ ex, double* __restrict__ ey, double* __re
   }
 }
 
-constexpr size_t kFdtdSmem =
-    sizeof(double) * (kFdtdRows * (kFdtdCols + 1) + (kFdtdRows + 1) * kFdtdCols + 2 * kFdtdRows);
-
-int64_t fdtd_tile_rows(int64_t nx) { return (nx + kFdtdRows - 1) / kFdtdRows; }
-int64_t fdtd_tile_cols(int64_t ny) { return (ny + kFdtdCols - 1) / kFdtdCols; }
-// doubles of one snapshot
-int64_t fdtd_snap_doubles(int64_t nx, int64_t ny) {
-  return 3 * fdtd_tile_rows(nx) * ny + 3 * fdtd_tile_cols(ny) * nx;
+constexpr size_t fdtd_smem(int th) {
+  return sizeof(double) * (th * (kFdtdCols + 1) + (th + 1) * kFdtdCols + 2 * th);
 }
 
-FdtdSnap fdtd_snap_at(double* base, int64_t nx, int64_t ny) {
-  const int64_t rowv = fdtd_tile_rows(nx) * ny, colv = fdtd_tile_cols(ny) * nx;
+int64_t fdtd_tile_rows(int64_t nx, int th) { return (nx + th - 1) / th; }
+int64_t fdtd_tile_cols(int64_t ny) { return (ny + kFdtdCols - 1) / kFdtdCols; }
+// doubles of one snapshot for tiles of th rows
+int64_t fdtd_snap_doubles(int64_t nx, int64_t ny, int th) {
+  return 3 * fdtd_tile_rows(nx, th) * ny + 3 * fdtd_tile_cols(ny) * nx;
+}
+
+FdtdSnap fdtd_snap_at(double* base, int64_t nx, int64_t ny, int th) {
+  const int64_t rowv = fdtd_tile_rows(nx, th) * ny, colv = fdtd_tile_cols(ny) * nx;
   FdtdSnap s;
   s.top_hz = base;
   s.top_ey = base + rowv;
@@ -369,6 +372,25 @@ FdtdSnap fdtd_snap_at(double* base, int64_t nx, int64_t ny) {
   s.left_ex = base + 3 * rowv + colv;
   s.right_hz = base + 3 * rowv + 2 * colv;
   return s;
+}
+
+template <int TH>
+int launch_fdtd_fused(double* ex, double* ey, double* hz, const double* fict, int64_t nx,
+                      int64_t ny, int64_t tsteps, double* w, cudaStream_t st) {
+  const int rc = allow_dynamic_smem(reinterpret_cast<const void*>(fdtd2d_step_fused<TH>),
+                                    fdtd_smem(TH), "b200_polybench_fdtd_2d_ws");
+  if (rc != B200_OK) return rc;
+  const FdtdSnap snap[2] = {fdtd_snap_at(w, nx, ny, TH),
+                            fdtd_snap_at(w + fdtd_snap_doubles(nx, ny, TH), nx, ny, TH)};
+  const int64_t ntx = fdtd_tile_cols(ny), nty = fdtd_tile_rows(nx, TH);
+  const int64_t total = nty * ny + ntx * nx;
+  const unsigned ig = static_cast<unsigned>(std::min<int64_t>(ceil_div(total, 256), 4096));
+  fdtd2d_snap_init<<<ig, 256, 0, st>>>(ex, ey, hz, nx, ny, ntx, nty, TH, snap[0]);
+  const dim3 g(static_cast<unsigned>(ntx), static_cast<unsigned>(nty));
+  for (int64_t t = 0; t < tsteps; ++t)
+    fdtd2d_step_fused<TH><<<g, kFdtdCols, fdtd_smem(TH), st>>>(ex, ey, hz, fict, t, nx, ny,
+                                                               snap[t & 1], snap[(t + 1) & 1], 0);
+  return B200_OK;
 }
 
 // ---- mixed FP64-pipe / integer-pipe stencils ----------------------------------
@@ -681,7 +703,7 @@ int b200_polybench_fdtd_2d(double* ex, double* ey, double* hz, const double* fic
 
 size_t b200_fdtd_2d_workspace_bytes(int64_t nx, int64_t ny) {
   if (nx <= 0 || ny <= 0) return 0;
-  return 2 * static_cast<size_t>(fdtd_snap_doubles(nx, ny)) * sizeof(double);
+  return 2 * static_cast<size_t>(fdtd_snap_doubles(nx, ny, kFdtdMinRows)) * sizeof(double);
 }
 
 int b200_polybench_fdtd_2d_ws(double* ex, double* ey, double* hz, const double* fict,
@@ -693,28 +715,22 @@ int b200_polybench_fdtd_2d_ws(double* ex, double* ey, double* hz, const double* 
   const int algo = tune ? tune->algo : 0;
   if (algo != 0 && algo != 1) return invalid("b200_polybench_fdtd_2d_ws: algo %d (0 or 1)", algo);
   if (algo == 1) return b200_polybench_fdtd_2d(ex, ey, hz, fict, nx, ny, tsteps, tune, stream);
+  const int th = (tune && tune->tile_y) ? tune->tile_y : kFdtdDefaultRows;
+  if (th != 8 && th != 16 && th != 32)
+    return invalid("b200_polybench_fdtd_2d_ws: tile_y %d (8, 16 or 32 rows)", th);
   if (nx == 0 || ny == 0 || tsteps == 0) return B200_OK;
-  if (fdtd_tile_rows(nx) > 65535) return invalid("b200_polybench_fdtd_2d_ws: nx too large");
+  if (fdtd_tile_rows(nx, th) > 65535) return invalid("b200_polybench_fdtd_2d_ws: nx too large");
   const size_t need = b200_fdtd_2d_workspace_bytes(nx, ny);
   if (!workspace || workspace_bytes < need) {
     set_error("b200_polybench_fdtd_2d_ws: workspace %zu bytes, need %zu", workspace_bytes, need);
     return B200_ERR_WORKSPACE;
   }
-  const int rc = allow_dynamic_smem(reinterpret_cast<const void*>(fdtd2d_step_fused), kFdtdSmem,
-                                    "b200_polybench_fdtd_2d_ws");
-  if (rc != B200_OK) return rc;
   cudaStream_t st = as_stream(stream);
   double* w = static_cast<double*>(workspace);
-  const FdtdSnap snap[2] = {fdtd_snap_at(w, nx, ny),
-                            fdtd_snap_at(w + fdtd_snap_doubles(nx, ny), nx, ny)};
-  const int64_t ntx = fdtd_tile_cols(ny), nty = fdtd_tile_rows(nx);
-  const int64_t total = nty * ny + ntx * nx;
-  const unsigned ig = static_cast<unsigned>(std::min<int64_t>(ceil_div(total, 256), 4096));
-  fdtd2d_snap_init<<<ig, 256, 0, st>>>(ex, ey, hz, nx, ny, ntx, nty, snap[0]);
-  const dim3 g(static_cast<unsigned>(ntx), static_cast<unsigned>(nty));
-  for (int64_t t = 0; t < tsteps; ++t)
-    fdtd2d_step_fused<<<g, kFdtdCols, kFdtdSmem, st>>>(ex, ey, hz, fict, t, nx, ny, snap[t & 1],
-                                                       snap[(t + 1) & 1], 0);
+  const int rc = th == 8    ? launch_fdtd_fused<8>(ex, ey, hz, fict, nx, ny, tsteps, w, st)
+                 : th == 16 ? launch_fdtd_fused<16>(ex, ey, hz, fict, nx, ny, tsteps, w, st)
+                            : launch_fdtd_fused<32>(ex, ey, hz, fict, nx, ny, tsteps, w, st);
+  if (rc != B200_OK) return rc;
   return after_launch("b200_polybench_fdtd_2d_ws", static_cast<int>(1 + tsteps));
 }
 

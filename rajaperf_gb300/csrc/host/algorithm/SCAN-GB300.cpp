@@ -54,10 +54,21 @@ void SCAN::setUp(VariantID vid, size_t tune_idx) {
   m_ws_bytes = b200_scan_workspace_bytes(n);
   m_ws = allocDeviceBytes(m_ws_bytes);
   zeroDeviceBytes(m_ws, m_ws_bytes);
+  // --host-data: one streaming pass on the host arrays, with the one-CTA-per-
+  // tile kernel (plain loads; the persistent kernel's bulk copies stay on
+  // device memory)
+  if (isInt64(tune_idx)) {
+    hostArray(m_xi, n, kIn);
+    hostArray(m_yi, n, kOut);
+  } else {
+    hostArray(m_x, n, kIn);
+    hostArray(m_y, n, kOut);
+  }
 }
 
 KernelBase::RepBody SCAN::makeRepBody(size_t tune_idx) {
-  const b200_tune tn = getTune(tune_idx);
+  b200_tune tn = getTune(tune_idx);
+  if (hostData()) tn.algo = 1;
   const Index_type n = getActualProblemSize();
   if (isInt64(tune_idx)) {
     return [=](b200_stream_t s) {

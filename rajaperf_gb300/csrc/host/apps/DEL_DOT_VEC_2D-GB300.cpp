@@ -45,6 +45,11 @@ void DEL_DOT_VEC_2D::setUp(VariantID vid, size_t) {
   allocAndInitData(m_xdot, m_array_length, vid);
   allocAndInitData(m_ydot, m_array_length, vid);
   allocAndInitDataConst(m_div, m_array_length, 0.0, vid);
+  // --host-data: the zones gather their corner nodes, so the arrays are
+  // staged (the zone list is an input like the node arrays)
+  for (Real_ptr* p : {&m_x, &m_y, &m_xdot, &m_ydot}) stageArray(*p, m_array_length, kIn);
+  stageArray(m_real_zones, m_domain->n_real_zones, kIn);
+  stageArray(m_div, m_array_length, kOut);
   m_ptiny = 1.0e-20;
   m_half = 0.5;
 }

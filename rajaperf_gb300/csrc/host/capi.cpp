@@ -64,6 +64,8 @@ int rp_run(int argc, const char* const* argv, rp_result* out, int capacity,
       o.flops_per_rep = r.flops_per_rep;
       o.passes = r.passes;
       o.failed = r.error.empty() ? 0 : 1;
+      o.h2d_bytes_per_rep = r.h2d_bytes_per_rep;
+      o.d2h_bytes_per_rep = r.d2h_bytes_per_rep;
     }
     if (count) *count = n;
     return status;

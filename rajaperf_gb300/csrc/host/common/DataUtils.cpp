@@ -54,16 +54,41 @@ void deallocDeviceBytes(void* p) {
   if (p) cudaFree(p);
 }
 
+void* allocPinnedBytes(Size_type nbytes) {
+  void* p = nullptr;
+  checkCuda(cudaHostAlloc(&p, nbytes ? nbytes : 256, cudaHostAllocMapped | cudaHostAllocPortable),
+            "cudaHostAlloc");
+  return p;
+}
+
+bool isHostMemory(const void* p) {
+  cudaPointerAttributes a{};
+  if (!p || cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
+  return a.type == cudaMemoryTypeHost;
+}
+
+void deallocDataBytes(void* p) {
+  if (!p) return;
+  if (isHostMemory(p)) cudaFreeHost(p);
+  else cudaFree(p);
+}
+
+// The copies name no direction: with unified addressing the runtime takes it
+// from the pointers, so the same helpers serve device arrays and the pinned
+// host arrays of --host-data.
 void copyToDevice(void* d, const void* h, Size_type nbytes) {
-  if (nbytes) checkCuda(cudaMemcpy(d, h, nbytes, cudaMemcpyHostToDevice), "H2D copy");
+  if (nbytes) checkCuda(cudaMemcpy(d, h, nbytes, cudaMemcpyDefault), "H2D copy");
 }
 
 void copyToHost(void* h, const void* d, Size_type nbytes) {
-  if (nbytes) checkCuda(cudaMemcpy(h, d, nbytes, cudaMemcpyDeviceToHost), "D2H copy");
+  if (nbytes) checkCuda(cudaMemcpy(h, d, nbytes, cudaMemcpyDefault), "D2H copy");
 }
 
 void copyDeviceToDevice(void* dst, const void* src, Size_type nbytes) {
-  if (nbytes) checkCuda(cudaMemcpy(dst, src, nbytes, cudaMemcpyDeviceToDevice), "D2D copy");
+  if (nbytes) checkCuda(cudaMemcpy(dst, src, nbytes, cudaMemcpyDefault), "D2D copy");
 }
 
 void zeroDeviceBytes(void* d, Size_type nbytes) {

@@ -34,6 +34,12 @@ void initData(Real_type& d);
 // Device allocation (cudaMalloc); throws std::runtime_error on failure.
 void* allocDeviceBytes(Size_type nbytes);
 void deallocDeviceBytes(void* p);
+// Pinned host memory mapped into the device's address space (the suite's
+// CudaPinned data space): kernels read and write it across the host link.
+void* allocPinnedBytes(Size_type nbytes);
+bool isHostMemory(const void* p);
+// Frees device or pinned host memory, whichever p is.
+void deallocDataBytes(void* p);
 
 // Fills a device array.  Each call bumps the data-init counter once.
 void initDeviceData(const RunParams& rp, Real_ptr d, Size_type len);

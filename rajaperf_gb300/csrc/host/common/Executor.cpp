@@ -156,6 +156,8 @@ void Executor::collectResults() {
       r.kernels_per_rep = k->getKernelsPerRep();
       r.bytes_per_rep = k->getBytesPerRep();
       r.flops_per_rep = k->getFLOPsPerRep();
+      r.h2d_bytes_per_rep = k->getH2DBytesPerRep();
+      r.d2h_bytes_per_rep = k->getD2HBytesPerRep();
       results_.push_back(r);
     }
   }

@@ -39,6 +39,8 @@ struct RunResult {
   long long kernels_per_rep = 0;
   long long bytes_per_rep = 0;
   long long flops_per_rep = 0;
+  long long h2d_bytes_per_rep = 0;  // --host-data: bytes crossing the host link
+  long long d2h_bytes_per_rep = 0;
   int passes = 0;
   std::string error;  // empty when the run succeeded
 };

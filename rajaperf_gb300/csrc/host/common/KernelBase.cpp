@@ -142,6 +142,7 @@ void KernelBase::execute(VariantID vid, size_t tune_idx) {
   running_variant = vid;
   running_tuning = tune_idx;
   resetTimer();
+  resetHostIO();
   detail::resetDataInitCount();
   try {
     setUp(vid, tune_idx);
@@ -165,8 +166,89 @@ void KernelBase::runKernel(VariantID vid, size_t tune_idx) {
 
 void KernelBase::runGB300Variant(VariantID, size_t tune_idx) {
   prepareRun(tune_idx);
-  runReps(tune_idx, getRunReps(), makeRepBody(tune_idx));
+  if (hostData() && !host_io_declared_)
+    throw std::runtime_error(name + " has no --host-data form");
+  if (hostData() && !staged_.empty()) {
+    swapStaged(true);
+    try {
+      runReps(tune_idx, getRunReps(), stagedBody(makeRepBody(tune_idx)));
+    } catch (...) {
+      swapStaged(false);
+      throw;
+    }
+    swapStaged(false);
+  } else {
+    runReps(tune_idx, getRunReps(), makeRepBody(tune_idx));
+  }
   finishRun(tune_idx);
+}
+
+bool KernelBase::hostData() const { return run_params.getHostData(); }
+
+void KernelBase::resetHostIO() {
+  for (Staged& st : staged_) {
+    if (*st.member == st.dev) *st.member = st.host;
+    deallocDeviceBytes(st.dev);
+  }
+  staged_.clear();
+  host_io_declared_ = false;
+  h2d_bytes_per_rep = 0;
+  d2h_bytes_per_rep = 0;
+}
+
+void KernelBase::stageBytes(void** member, Size_type bytes, unsigned io) {
+  if (!hostData()) return;
+  Staged st{member, *member, allocDeviceBytes(bytes), bytes, io};
+  staged_.push_back(st);
+  hostArrayBytes(bytes, io);
+}
+
+void KernelBase::hostArrayBytes(Size_type bytes, unsigned io) {
+  if (!hostData()) return;
+  host_io_declared_ = true;
+  if (io & kIn) h2d_bytes_per_rep += bytes;
+  if (io & kOut) d2h_bytes_per_rep += bytes;
+}
+
+void KernelBase::unstage(void** member) {
+  for (size_t k = 0; k < staged_.size(); ++k) {
+    if (staged_[k].member != member) continue;
+    if (*member == staged_[k].dev) *member = staged_[k].host;
+    deallocDeviceBytes(staged_[k].dev);
+    staged_.erase(staged_.begin() + static_cast<std::ptrdiff_t>(k));
+    return;
+  }
+}
+
+// During the timed loop the staged members point to their device buffers,
+// which start as copies of the host arrays (untimed): the parts of an array
+// that no rep writes (boundaries of a stencil's output, a zone list's
+// ghosts) then hold the host values, and scratch arrays start initialised.
+void KernelBase::swapStaged(bool to_device) {
+  for (Staged& st : staged_) {
+    if (to_device) copyToDevice(st.dev, st.host, st.bytes);
+    *st.member = to_device ? st.dev : st.host;
+  }
+}
+
+// One rep with host-resident data: the kIn arrays are copied in from pinned
+// host memory, the kernel runs on the device buffers, the kOut arrays are
+// copied back, all on the rep's stream (so a graph tuning captures the
+// copies with the kernels).
+KernelBase::RepBody KernelBase::stagedBody(RepBody inner) {
+  const std::vector<Staged> st = staged_;
+  return [st, inner](b200_stream_t s) {
+    cudaStream_t cs = reinterpret_cast<cudaStream_t>(s);
+    for (const Staged& a : st)
+      if (a.io & kIn)
+        checkCuda(cudaMemcpyAsync(a.dev, a.host, a.bytes, cudaMemcpyHostToDevice, cs),
+                  "host-data copy in");
+    inner(s);
+    for (const Staged& a : st)
+      if (a.io & kOut)
+        checkCuda(cudaMemcpyAsync(a.host, a.dev, a.bytes, cudaMemcpyDeviceToHost, cs),
+                  "host-data copy out");
+  };
 }
 
 void KernelBase::runReps(size_t tune_idx, Index_type reps,

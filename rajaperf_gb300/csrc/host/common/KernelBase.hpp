@@ -117,16 +117,45 @@ class KernelBase {
   void resetTimer() { timer_elapsed = 0.0; }
   void synchronize();
 
-  // ---- device data helpers ----
+  // ---- data helpers: device memory, or pinned host memory with --host-data ----
   template <typename T>
   void allocData(T*& ptr, Size_type len, VariantID) {
-    ptr = static_cast<T*>(allocDeviceBytes(len * sizeof(T)));
+    ptr = static_cast<T*>(hostData() ? allocPinnedBytes(len * sizeof(T))
+                                     : allocDeviceBytes(len * sizeof(T)));
   }
   template <typename T>
   void deallocData(T*& ptr, VariantID) {
-    deallocDeviceBytes(ptr);
+    unstage(reinterpret_cast<void**>(&ptr));
+    deallocDataBytes(ptr);
     ptr = nullptr;
   }
+
+  // ---- host-resident data (--host-data) ----
+  // The arrays allocated above live in pinned host memory, and each rep moves
+  // its data across the host link inside the timed loop.  A kernel that
+  // streams through its arrays once reads and writes them in host memory
+  // directly and declares them with hostArray() (for the byte counts only).
+  // One that iterates over them, or gathers, declares them with stageArray():
+  // during the timed loop the member then points to a device buffer, and each
+  // rep first copies the kIn arrays in from host memory and, after the
+  // kernel, copies the kOut arrays back (arrays with neither are device-only
+  // scratch the rep rewrites).  The device buffers start as copies of the
+  // host arrays, taken before the timed loop.  A kernel that declares no array has no
+  // host-data form, and its run fails with --host-data.
+  enum : unsigned { kIn = 1u, kOut = 2u };
+  bool hostData() const;
+  template <typename T>
+  void stageArray(T*& member, Size_type len, unsigned io) {
+    stageBytes(reinterpret_cast<void**>(&member), len * sizeof(T), io);
+  }
+  template <typename T>
+  void hostArray(const T* ptr, Size_type len, unsigned io) {
+    (void)ptr;
+    hostArrayBytes(len * sizeof(T), io);
+  }
+  // Bytes crossing the host link per rep in each direction (--host-data).
+  Index_type getH2DBytesPerRep() const { return h2d_bytes_per_rep; }
+  Index_type getD2HBytesPerRep() const { return d2h_bytes_per_rep; }
   void allocAndInitData(Real_ptr& ptr, Size_type len, VariantID vid);
   void allocAndInitDataConst(Real_ptr& ptr, Size_type len, Real_type val,
                              VariantID vid);
@@ -194,6 +223,24 @@ class KernelBase {
 
  private:
   void recordExecTime();
+
+  void stageBytes(void** member, Size_type bytes, unsigned io);
+  void hostArrayBytes(Size_type bytes, unsigned io);
+  void unstage(void** member);
+  void resetHostIO();
+  RepBody stagedBody(RepBody inner);
+  void swapStaged(bool to_device);
+
+  struct Staged {
+    void** member;   // the kernel's pointer member
+    void* host;      // its pinned host array
+    void* dev;       // the device buffer it points to during the timed loop
+    Size_type bytes;
+    unsigned io;
+  };
+  std::vector<Staged> staged_;
+  bool host_io_declared_ = false;
+  Index_type h2d_bytes_per_rep = 0, d2h_bytes_per_rep = 0;
 
   KernelID kernel_id;
   std::string name;

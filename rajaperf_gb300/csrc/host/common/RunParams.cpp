@@ -174,6 +174,8 @@ RunParams::RunParams(int argc, const char* const* argv) {
       double v;
       if (!parseDouble(takeValue(i, opt), v) || v < 0) fail("bad --pass-fail-tol");
       pf_tolerance = v;
+    } else if (opt == "--host-data") {
+      host_data = true;
     } else if (opt == "--wait-limit-us") {
       long long v;
       if (!parseLong(takeValue(i, opt), v) || v < 0 || v > 2000000000LL)
@@ -264,6 +266,9 @@ RunParams::RunParams(int argc, const char* const* argv) {
       else fail("variant " + v + " is not available in this build");
     }
   }
+  if (host_data && (graph_batch || !autotune_file.empty()))
+    fail("--host-data runs the suite's rep loops; it does not combine with --graph-batch "
+         "or --autotune");
   if (!reference_variant.empty() && reference_variant != getVariantName(Base_GB300))
     fail("reference variant " + reference_variant + " is not available in this build");
 
@@ -309,6 +314,11 @@ std::string RunParams::usage() {
       "                               them to FILE as a tuning table\n"
       "  --graph-batch [R]            capture every kernel's R-rep loop into\n"
       "                               one CUDA graph and compare with launches\n"
+      "  --host-data                  arrays in pinned host memory; every rep\n"
+      "                               moves its inputs and outputs across the\n"
+      "                               host link (streaming kernels read and write\n"
+      "                               host memory directly, iterating ones copy\n"
+      "                               their arrays in and out around the rep)\n"
       "  --wait-limit-us U            limit of the kernels' bounded device-side\n"
       "                               waits (0 = library default: 2 s, GEMM 1 s)\n"
       "  --inject-lookback-stall K    test option: before each run of SCAN and\n"

@@ -47,6 +47,9 @@ class RunParams {
   // Limit of the bounded device-side waits (b200_tune.wait_limit_us; 0 =
   // library default) and the test option that makes a lookback wait run out.
   int getWaitLimitUs() const { return wait_limit_us; }
+  // --host-data: the kernels' arrays live in pinned host memory (the suite's
+  // CudaPinned data space) and every rep moves its data across the host link.
+  bool getHostData() const { return host_data; }
   // Reports: npasses combiners of the timing/speedup CSVs (the suite's
   // --npasses-combiners, default Average), the speedup reference variant
   // (--refvar; none by default) and the FOM tolerance (--pass-fail-tol).
@@ -108,6 +111,7 @@ class RunParams {
   double init_hi = 1.5;
   long polybench_tsteps = -1;
   int wait_limit_us = 0;
+  bool host_data = false;
   std::vector<std::string> npasses_combiners;
   std::string reference_variant;
   double pf_tolerance = 0.1;

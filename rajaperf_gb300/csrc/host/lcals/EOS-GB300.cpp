@@ -28,6 +28,11 @@ void EOS::setUp(VariantID vid, size_t) {
   allocAndInitData(m_y, m_array_length, vid);
   allocAndInitData(m_z, m_array_length, vid);
   allocAndInitData(m_u, m_array_length, vid);
+  // --host-data: one streaming pass, on the host arrays directly
+  hostArray(m_x, getActualProblemSize(), kOut);
+  hostArray(m_y, getActualProblemSize(), kIn);
+  hostArray(m_z, getActualProblemSize(), kIn);
+  hostArray(m_u, m_array_length, kIn);
   initData(m_q, vid);
   initData(m_r, vid);
   initData(m_t, vid);

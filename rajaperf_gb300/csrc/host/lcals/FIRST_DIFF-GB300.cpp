@@ -24,6 +24,9 @@ FIRST_DIFF::FIRST_DIFF(const RunParams& params)
 void FIRST_DIFF::setUp(VariantID vid, size_t) {
   allocAndInitDataConst(m_x, m_N, 0.0, vid);
   allocAndInitData(m_y, m_N, vid);
+  // --host-data: one streaming pass, on the host arrays directly
+  hostArray(m_y, m_N, kIn);
+  hostArray(m_x, getActualProblemSize(), kOut);
 }
 
 KernelBase::RepBody FIRST_DIFF::makeRepBody(size_t tune_idx) {

@@ -44,6 +44,10 @@ void FIRST_MIN::setUp(VariantID vid, size_t tune_idx) {
   m_minloc = -1;
   allocData(m_dminloc, 1, vid);
   copyToDevice(m_dminloc, &m_minloc, sizeof(Index_type));
+  // --host-data: one streaming pass over x in host memory; the location is
+  // written to host memory by the kernel
+  hostArray(m_x, m_N, kIn);
+  hostArray(m_dminloc, 1, kOut);
   const b200_tune t = getTune(tune_idx);
   m_ws_bytes = b200_reduce_workspace_bytes(m_N, &t);
   m_ws = allocDeviceBytes(m_ws_bytes);

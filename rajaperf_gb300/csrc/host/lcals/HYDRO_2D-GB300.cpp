@@ -47,6 +47,15 @@ void HYDRO_2D::setUp(VariantID vid, size_t) {
   allocAndInitData(m_zu, m_array_length, vid);
   allocAndInitData(m_zv, m_array_length, vid);
   allocAndInitData(m_zz, m_array_length, vid);
+  // --host-data: two sweeps, so the arrays are staged; za and zb are
+  // rewritten by BODY1 before BODY2 reads them (device scratch)
+  for (Real_ptr* p : {&m_zp, &m_zq, &m_zr, &m_zm, &m_zz}) stageArray(*p, m_array_length, kIn);
+  stageArray(m_zu, m_array_length, kIn | kOut);
+  stageArray(m_zv, m_array_length, kIn | kOut);
+  stageArray(m_za, m_array_length, 0);
+  stageArray(m_zb, m_array_length, 0);
+  stageArray(m_zrout, m_array_length, kOut);
+  stageArray(m_zzout, m_array_length, kOut);
 }
 
 KernelBase::RepBody HYDRO_2D::makeRepBody(size_t tune_idx) {

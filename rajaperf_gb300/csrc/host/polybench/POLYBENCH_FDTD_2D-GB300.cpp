@@ -52,6 +52,11 @@ void POLYBENCH_FDTD_2D::setUp(VariantID vid, size_t) {
   allocAndInitData(m_fict, m_tsteps, vid);
   m_ws_bytes = b200_fdtd_2d_workspace_bytes(m_nx, m_ny);
   m_ws = m_ws_bytes ? allocDeviceBytes(m_ws_bytes) : nullptr;
+  // --host-data: all time steps of a rep run on staged copies of the fields
+  stageArray(m_ex, m_nx * m_ny, kIn | kOut);
+  stageArray(m_ey, m_nx * m_ny, kIn | kOut);
+  stageArray(m_hz, m_nx * m_ny, kIn | kOut);
+  stageArray(m_fict, m_tsteps, kIn);
 }
 
 KernelBase::RepBody POLYBENCH_FDTD_2D::makeRepBody(size_t tune_idx) {

@@ -37,6 +37,9 @@ void POLYBENCH_JACOBI_2D::setUp(VariantID vid, size_t) {
   allocAndInitData(m_Binit, m_N * m_N, vid);
   allocData(m_A, m_N * m_N, vid);
   allocData(m_B, m_N * m_N, vid);
+  // --host-data: all time steps of a rep run on staged copies of A and B
+  stageArray(m_A, m_N * m_N, kIn | kOut);
+  stageArray(m_B, m_N * m_N, kIn | kOut);
 }
 
 void POLYBENCH_JACOBI_2D::prepareRun(size_t) {

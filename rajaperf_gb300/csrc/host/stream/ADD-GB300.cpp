@@ -23,6 +23,10 @@ void ADD::setUp(VariantID vid, size_t) {
   allocAndInitData(m_a, getActualProblemSize(), vid);
   allocAndInitData(m_b, getActualProblemSize(), vid);
   allocAndInitDataConst(m_c, getActualProblemSize(), 0.0, vid);
+  // --host-data: one streaming pass, on the host arrays directly
+  hostArray(m_a, getActualProblemSize(), kIn);
+  hostArray(m_b, getActualProblemSize(), kIn);
+  hostArray(m_c, getActualProblemSize(), kOut);
 }
 
 KernelBase::RepBody ADD::makeRepBody(size_t tune_idx) {

@@ -23,6 +23,9 @@ COPY::COPY(const RunParams& params) : KernelBase(rajaperf::Stream_COPY, params) 
 void COPY::setUp(VariantID vid, size_t) {
   allocAndInitData(m_a, getActualProblemSize(), vid);
   allocAndInitDataConst(m_c, getActualProblemSize(), 0.0, vid);
+  // --host-data: one streaming pass, on the host arrays directly
+  hostArray(m_a, getActualProblemSize(), kIn);
+  hostArray(m_c, getActualProblemSize(), kOut);
 }
 
 KernelBase::RepBody COPY::makeRepBody(size_t tune_idx) {

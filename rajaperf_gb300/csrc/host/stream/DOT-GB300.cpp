@@ -30,6 +30,11 @@ void DOT::setUp(VariantID vid, size_t tune_idx) {
   m_dot_init = 0.0;
   allocData(m_ddot, 1, vid);
   copyToDevice(m_ddot, &m_dot, sizeof(Real_type));
+  // --host-data: one streaming pass over the host arrays; the sum is
+  // accumulated in host memory by the kernel
+  hostArray(m_a, getActualProblemSize(), kIn);
+  hostArray(m_b, getActualProblemSize(), kIn);
+  hostArray(m_ddot, 1, kIn | kOut);
   const b200_tune t = getTune(tune_idx);
   m_ws_bytes = b200_reduce_workspace_bytes(getActualProblemSize(), &t);
   m_ws = allocDeviceBytes(m_ws_bytes);

@@ -22,6 +22,9 @@ MUL::MUL(const RunParams& params) : KernelBase(rajaperf::Stream_MUL, params) {
 void MUL::setUp(VariantID vid, size_t) {
   allocAndInitDataConst(m_b, getActualProblemSize(), 0.0, vid);
   allocAndInitData(m_c, getActualProblemSize(), vid);
+  // --host-data: one streaming pass, on the host arrays directly
+  hostArray(m_b, getActualProblemSize(), kOut);
+  hostArray(m_c, getActualProblemSize(), kIn);
   initData(m_alpha, vid);
 }
 

@@ -26,6 +26,10 @@ void TRIAD::setUp(VariantID vid, size_t) {
   allocAndInitDataConst(m_a, getActualProblemSize(), 0.0, vid);
   allocAndInitData(m_b, getActualProblemSize(), vid);
   allocAndInitData(m_c, getActualProblemSize(), vid);
+  // --host-data: one streaming pass, on the host arrays directly
+  hostArray(m_a, getActualProblemSize(), kOut);
+  hostArray(m_b, getActualProblemSize(), kIn);
+  hostArray(m_c, getActualProblemSize(), kIn);
   initData(m_alpha, vid);
 }
 

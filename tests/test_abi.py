@@ -37,4 +37,22 @@ def test_python_signatures_cover_header():
 
 def test_tune_struct_layout():
     assert ctypes.sizeof(rp.Tune) == 12 * 4
-    assert ctypes.sizeof(rp.RpResult) == 64 + 32 + 64 + 5 * 8 + 6 * 8 + 8
+    assert ctypes.sizeof(rp.RpResult) == 64 + 32 + 64 + 5 * 8 + 6 * 8 + 8 + 2 * 8
+
+
+def test_struct_sizes_match_the_headers(tmp_path):
+    """The ctypes mirrors have the C structs' sizes and field offsets."""
+    import subprocess
+    src = tmp_path / "sizes.c"
+    src.write_text(
+        '#include <stdio.h>\n#include <stddef.h>\n#include "b200.h"\n#include "rajaperf_gb300.h"\n'
+        'int main(void) { printf("%zu %zu %zu %zu %zu\\n", sizeof(b200_tune), sizeof(rp_result), '
+        'offsetof(rp_result, h2d_bytes_per_rep), offsetof(b200_tune, wait_limit_us), '
+        'sizeof(rp_batch_result)); return 0; }\n')
+    exe = tmp_path / "sizes"
+    subprocess.run(["cc", "-I", rp.INCLUDE, str(src), "-o", str(exe)], check=True)
+    got = [int(x) for x in subprocess.run([str(exe)], capture_output=True, text=True,
+                                          check=True).stdout.split()]
+    assert got == [ctypes.sizeof(rp.Tune), ctypes.sizeof(rp.RpResult),
+                   rp.RpResult.h2d_bytes_per_rep.offset, rp.Tune.wait_limit_us.offset,
+                   ctypes.sizeof(rp.RpBatchResult)]

@@ -164,9 +164,10 @@ def test_fdtd_2d(nx, ny, ts):
         close(gu.host(g), w)
 
 
+@pytest.mark.parametrize("rows", [8, 16, 32])
 @pytest.mark.parametrize("nx,ny,ts", [(1, 1, 2), (1, 7, 2), (7, 1, 3), (2, 2, 1), (33, 129, 3),
                                      (32, 128, 2), (64, 256, 4), (100, 300, 5), (257, 1000, 3)])
-def test_fdtd_2d_one_launch_per_step(nx, ny, ts):
+def test_fdtd_2d_one_launch_per_step(nx, ny, ts, rows):
     """The fused step (one launch per time step, tile edges from snapshots) is
     bit-identical to the two-launch form, tiles cut across rows and columns
     and partial last tiles included, and the workspace needs no zeroing."""
@@ -181,9 +182,10 @@ def test_fdtd_2d_one_launch_per_step(nx, ny, ts):
     wb = lib().b200_fdtd_2d_workspace_bytes(nx, ny)
     torch = gu.torch_cuda()
     w = torch.full((wb,), 0x7F, dtype=torch.uint8, device="cuda")
+    t = rp.Tune(tile_y=rows)
     rp.check(lib().b200_polybench_fdtd_2d_ws(d2[0].data_ptr(), d2[1].data_ptr(), d2[2].data_ptr(),
-                                             df.data_ptr(), nx, ny, ts, w.data_ptr(), wb, None,
-                                             gu.stream()))
+                                             df.data_ptr(), nx, ny, ts, w.data_ptr(), wb,
+                                             ctypes.byref(t), gu.stream()))
     for a, b in zip(d1, d2):
         assert np.array_equal(gu.host(a), gu.host(b))
     oracle.call("oracle_fdtd_2d", ex, ey, hz, fict, nx, ny, ts)
