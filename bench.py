@@ -95,8 +95,6 @@ def _stream_cases():
             self.c = self.uniform(n)
             self.bytes_per_rep = 24 * n
 
-
-
         def run(self, s):
             return self.L.b200_stream_triad(self.a.data_ptr(), self.b.data_ptr(),
                                             self.c.data_ptr(), 0.5, self.n, None, s)
@@ -110,8 +108,6 @@ def _stream_cases():
             self.a = self.uniform(n)
             self.c = self.zeros(n)
             self.bytes_per_rep = 16 * n
-
-
 
         def run(self, s):
             return self.L.b200_stream_copy(self.a.data_ptr(), self.c.data_ptr(), self.n,
@@ -127,8 +123,6 @@ def _stream_cases():
             self.c = self.uniform(n)
             self.bytes_per_rep = 16 * n
 
-
-
         def run(self, s):
             return self.L.b200_stream_mul(self.b.data_ptr(), self.c.data_ptr(), 0.5, self.n,
                                           None, s)
@@ -143,8 +137,6 @@ def _stream_cases():
             self.b = self.uniform(n)
             self.c = self.zeros(n)
             self.bytes_per_rep = 24 * n
-
-
 
         def run(self, s):
             return self.L.b200_stream_add(self.a.data_ptr(), self.b.data_ptr(),
@@ -162,8 +154,6 @@ def _stream_cases():
             self.ws_bytes = self.L.b200_reduce_workspace_bytes(n, None)
             self.ws = self.zeros(self.ws_bytes, dtype=torch.uint8)
             self.bytes_per_rep = 16 * n + 16
-
-
 
         def run(self, s):
             return self.L.b200_stream_dot(self.a.data_ptr(), self.b.data_ptr(), self.n, 0.0,
@@ -228,8 +218,6 @@ def _bandwidth_cases():
             self.flops_per_rep = 16 * n
             self.fp64_instr_per_rep = 8 * n
 
-
-
         def run(self, s):
             return self.L.b200_lcals_eos(self.x.data_ptr(), self.y.data_ptr(), self.z.data_ptr(),
                                          self.u.data_ptr(), 0.0979, 0.1958, 0.0979, self.n,
@@ -246,8 +234,6 @@ def _bandwidth_cases():
             self.bytes_per_rep = 8 * (n + 1) + 8 * n
             self.flops_per_rep = n
             self.fp64_instr_per_rep = n
-
-
 
         def run(self, s):
             return self.L.b200_lcals_first_diff(self.x.data_ptr(), self.y.data_ptr(), self.n,
@@ -268,8 +254,6 @@ def _bandwidth_cases():
             self.bytes_per_rep = 8 + 8 + 8 * n + 8 + 8
             self.flops_per_rep = 0
             self.fp64_instr_per_rep = 0
-
-
 
         def run(self, s):
             return self.L.b200_lcals_first_min(self.x.data_ptr(), self.n, 0.5, 0,
@@ -295,8 +279,6 @@ def _bandwidth_cases():
             # products and + ptiny off the FP64 pipe
             self.fp64_instr_per_rep = 33 * self.nz
 
-
-
         def run(self, s):
             return self.L.b200_apps_del_dot_vec_2d(
                 self.x.data_ptr(), self.y.data_ptr(), self.xdot.data_ptr(),
@@ -316,8 +298,6 @@ def _bandwidth_cases():
             self.flops_per_rep = tsteps * 10 * (N - 2) * (N - 2)
             self.fp64_instr_per_rep = tsteps * 8 * (N - 2) * (N - 2)  # 4 adds per point per half-step
 
-
-
         def run(self, s):
             return self.L.b200_polybench_jacobi_2d(self.A.data_ptr(), self.B.data_ptr(), self.N,
                                                    self.tsteps, None, s)
@@ -335,8 +315,6 @@ def _bandwidth_cases():
             self.bytes_per_rep = (8 * (N ** 3 - 12 * (N - 2) - 8) * 2 + 8 * inner * 2) * tsteps
             self.flops_per_rep = tsteps * 30 * inner
             self.fp64_instr_per_rep = tsteps * 18 * inner  # 9 adds per point per half-step
-
-
 
         def run(self, s):
             return self.L.b200_polybench_heat_3d(self.A.data_ptr(), self.B.data_ptr(), self.N,
@@ -359,13 +337,19 @@ def _bandwidth_cases():
             self.bytes_per_rep = (rd + wr) * tsteps
             self.flops_per_rep = tsteps * (3 * (nx - 1) * ny + 3 * nx * (ny - 1) +
                                            5 * (nx - 1) * (ny - 1))
-
-
+            # FP64-pipe instructions: 2 per ey and ex update, 4 per hz update
+            self.fp64_instr_per_rep = tsteps * (2 * (nx - 1) * ny + 2 * nx * (ny - 1) +
+                                                4 * (nx - 1) * (ny - 1))
+            # one launch per time step (tile-edge snapshots in the workspace)
+            self.launches = 1 + tsteps
+            self.ws_bytes = self.L.b200_fdtd_2d_workspace_bytes(nx, ny)
+            self.ws = torch.empty(self.ws_bytes, dtype=torch.uint8, device="cuda")
 
         def run(self, s):
-            return self.L.b200_polybench_fdtd_2d(self.ex.data_ptr(), self.ey.data_ptr(),
-                                                 self.hz.data_ptr(), self.fict.data_ptr(),
-                                                 self.nx, self.ny, self.tsteps, None, s)
+            return self.L.b200_polybench_fdtd_2d_ws(self.ex.data_ptr(), self.ey.data_ptr(),
+                                                    self.hz.data_ptr(), self.fict.data_ptr(),
+                                                    self.nx, self.ny, self.tsteps,
+                                                    self.ws.data_ptr(), self.ws_bytes, None, s)
 
     class ScanI64(Case):
         name = "Algorithm_SCAN"
@@ -381,8 +365,6 @@ def _bandwidth_cases():
             self.bytes_per_rep = 16 * n
             self.flops_per_rep = n
             self.fp64_instr_per_rep = 0
-
-
 
         def run(self, s):
             return self.L.b200_algorithm_scan_i64(self.x.data_ptr(), self.y.data_ptr(), self.n,

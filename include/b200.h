@@ -339,14 +339,16 @@ int b200_polybench_fdtd_2d(double* ex, double* ey, double* hz,
                            b200_stream_t stream);
 
 /* Workspace for b200_polybench_fdtd_2d_ws: two snapshots of the tile edges
- * (about 6 doubles per 32 x 128 tile edge point, 3-8% of one array). */
+ * (three rows per tile row and three columns per tile column; for 8-row
+ * tiles about 0.8 of one nx x ny array). */
 size_t b200_fdtd_2d_workspace_bytes(int64_t nx, int64_t ny);
 
 /* The same tsteps of FDTD_2D with one launch per time step: every CTA
- * updates ex and ey (BODY1-3) and then hz (BODY4) of its 32 x 128 tile in
- * place, taking the old values across tile edges from a snapshot of the
- * edges in the workspace (one extra small launch per call takes the first
- * snapshot).  48 bytes per point and step instead of 72; bit-identical to
+ * updates ex and ey (BODY1-3) and then hz (BODY4) of its tile of
+ * tune->tile_y rows (8 by default, or 16, 32) x 128 columns in place, taking
+ * the old values across tile edges from a snapshot of the edges in the
+ * workspace (one extra small launch per call takes the first snapshot).
+ * 48 bytes per point and step instead of 72; bit-identical to
  * b200_polybench_fdtd_2d.  tune->algo 1 runs b200_polybench_fdtd_2d instead
  * (no workspace needed).  The workspace needs no initialisation.
  *   -- polybench/POLYBENCH_FDTD_2D.hpp:52-69, -Cuda.cpp:164-190             */

@@ -204,7 +204,10 @@ fdtd2d_h(const double* __restrict__ ex, const double* __restrict__ ey,
 // results are bit-identical.
 constexpr int kFdtdCols = 128;     // threads per CTA
 constexpr int kFdtdMinRows = 8;    // the workspace holds snapshots for tiles this short
-constexpr int kFdtdDefaultRows = 16;
+// 8192^2, 20 steps (GB300): 8 rows 0.965 ms per step (556 G FP64
+// instructions/s, 93% of the pipe), 16 rows 1.017, 32 rows 1.485 (the
+// two-launch form: 1.173); shorter tiles leave more CTAs resident per SM.
+constexpr int kFdtdDefaultRows = 8;
 
 struct FdtdSnap {
   double* top_hz;    // [tile rows][ny]: hz of each tile's first row

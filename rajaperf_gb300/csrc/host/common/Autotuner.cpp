@@ -16,7 +16,7 @@ namespace rajaperf {
 
 namespace {
 
-enum class Family { Map, Stream, Reduce, Scan, Hydro2D, Rows, Fixed };
+enum class Family { Map, Stream, Reduce, Scan, Hydro2D, Rows, Fdtd, Fixed };
 
 Family familyOf(KernelID kid) {
   switch (kid) {
@@ -30,6 +30,8 @@ Family familyOf(KernelID kid) {
       return Family::Hydro2D;
     case Polybench_JACOBI_2D:
       return Family::Rows;
+    case Polybench_FDTD_2D:
+      return Family::Fdtd;
     case Basic_DAXPY: case Basic_INIT3: case Basic_MULADDSUB: case Lcals_DIFF_PREDICT:
     case Lcals_EOS: case Lcals_FIRST_DIFF: case Lcals_HYDRO_1D: case Lcals_INT_PREDICT:
     case Lcals_PLANCKIAN: case Apps_DEL_DOT_VEC_2D: case Apps_ENERGY: case Apps_PRESSURE:
@@ -90,6 +92,17 @@ std::vector<b200_tune> autotuneCandidates(KernelID kid) {
       t.items = items;
       out.push_back(t);
     }
+    return out;
+  }
+  if (f == Family::Fdtd) {  // rows per tile of the one-launch step; algo 1: two launches
+    for (int rows : {8, 32}) {
+      b200_tune t{};
+      t.tile_y = rows;
+      out.push_back(t);
+    }
+    b200_tune t{};
+    t.algo = 1;
+    out.push_back(t);
     return out;
   }
   if (f == Family::Fixed) return out;
