@@ -23,6 +23,7 @@ exchange); value is summed over ranks.
 from __future__ import annotations
 
 import argparse
+import ctypes
 import json
 import math
 import os
@@ -80,6 +81,17 @@ class Case:
     def zeros(self, n, dtype=None):
         return self.torch.zeros(n, dtype=dtype or self.torch.float64, device="cuda")
 
+    # launch shape: a b200_tune from the committed tuning table, or None
+    # (the library default); cases with a reduction workspace re-size it
+    tp = None
+
+    def set_tune(self, tune):
+        self.tune = tune
+        self.tp = None if tune is None else ctypes.byref(tune)
+        if getattr(self, "ws_kind", None) == "reduce":
+            self.ws_bytes = self.L.b200_reduce_workspace_bytes(self.n, self.tp)
+            self.ws = self.torch.zeros(self.ws_bytes, dtype=self.torch.uint8, device="cuda")
+
     # subclasses define bytes_per_rep and run(stream)
 
 
@@ -97,7 +109,7 @@ def _stream_cases():
 
         def run(self, s):
             return self.L.b200_stream_triad(self.a.data_ptr(), self.b.data_ptr(),
-                                            self.c.data_ptr(), 0.5, self.n, None, s)
+                                            self.c.data_ptr(), 0.5, self.n, self.tp, s)
 
     class Copy(Case):
         name = "Stream_COPY"
@@ -111,7 +123,7 @@ def _stream_cases():
 
         def run(self, s):
             return self.L.b200_stream_copy(self.a.data_ptr(), self.c.data_ptr(), self.n,
-                                           None, s)
+                                           self.tp, s)
 
     class Mul(Case):
         name = "Stream_MUL"
@@ -125,7 +137,7 @@ def _stream_cases():
 
         def run(self, s):
             return self.L.b200_stream_mul(self.b.data_ptr(), self.c.data_ptr(), 0.5, self.n,
-                                          None, s)
+                                          self.tp, s)
 
     class Add(Case):
         name = "Stream_ADD"
@@ -140,7 +152,7 @@ def _stream_cases():
 
         def run(self, s):
             return self.L.b200_stream_add(self.a.data_ptr(), self.b.data_ptr(),
-                                          self.c.data_ptr(), self.n, None, s)
+                                          self.c.data_ptr(), self.n, self.tp, s)
 
     class Dot(Case):
         name = "Stream_DOT"
@@ -151,6 +163,7 @@ def _stream_cases():
             self.a = self.uniform(n)
             self.b = self.uniform(n)
             self.acc = self.zeros(1)
+            self.ws_kind = "reduce"
             self.ws_bytes = self.L.b200_reduce_workspace_bytes(n, None)
             self.ws = self.zeros(self.ws_bytes, dtype=torch.uint8)
             self.bytes_per_rep = 16 * n + 16
@@ -158,7 +171,7 @@ def _stream_cases():
         def run(self, s):
             return self.L.b200_stream_dot(self.a.data_ptr(), self.b.data_ptr(), self.n, 0.0,
                                           self.acc.data_ptr(), self.ws.data_ptr(),
-                                          self.ws_bytes, None, s)
+                                          self.ws_bytes, self.tp, s)
 
     return {"Stream_COPY": Copy, "Stream_MUL": Mul, "Stream_ADD": Add,
             "Stream_TRIAD": Triad, "Stream_DOT": Dot}
@@ -204,7 +217,7 @@ def _bandwidth_cases():
 
         def run(self, s):
             a = [t.data_ptr() for t in self.arr]
-            return self.L.b200_lcals_hydro_2d(*a, 0.0041, 0.0037, self.kn, self.jn, None, s)
+            return self.L.b200_lcals_hydro_2d(*a, 0.0041, 0.0037, self.kn, self.jn, self.tp, s)
 
     class Eos(Case):
         name = "Lcals_EOS"
@@ -221,7 +234,7 @@ def _bandwidth_cases():
         def run(self, s):
             return self.L.b200_lcals_eos(self.x.data_ptr(), self.y.data_ptr(), self.z.data_ptr(),
                                          self.u.data_ptr(), 0.0979, 0.1958, 0.0979, self.n,
-                                         None, s)
+                                         self.tp, s)
 
     class FirstDiff(Case):
         name = "Lcals_FIRST_DIFF"
@@ -237,7 +250,7 @@ def _bandwidth_cases():
 
         def run(self, s):
             return self.L.b200_lcals_first_diff(self.x.data_ptr(), self.y.data_ptr(), self.n,
-                                                None, s)
+                                                self.tp, s)
 
     class FirstMin(Case):
         name = "Lcals_FIRST_MIN"
@@ -249,6 +262,7 @@ def _bandwidth_cases():
             planted = int(np.random.default_rng(seed).integers(0, n))
             self.x[planted] = -0.5
             self.loc = self.zeros(1, dtype=torch.int64)
+            self.ws_kind = "reduce"
             self.ws_bytes = self.L.b200_reduce_workspace_bytes(n, None)
             self.ws = self.zeros(self.ws_bytes, dtype=torch.uint8)
             self.bytes_per_rep = 8 + 8 + 8 * n + 8 + 8
@@ -258,7 +272,7 @@ def _bandwidth_cases():
         def run(self, s):
             return self.L.b200_lcals_first_min(self.x.data_ptr(), self.n, 0.5, 0,
                                                self.loc.data_ptr(), None, self.ws.data_ptr(),
-                                               self.ws_bytes, None, s)
+                                               self.ws_bytes, self.tp, s)
 
     class DelDotVec2D(Case):
         name = "Apps_DEL_DOT_VEC_2D"
@@ -283,7 +297,7 @@ def _bandwidth_cases():
             return self.L.b200_apps_del_dot_vec_2d(
                 self.x.data_ptr(), self.y.data_ptr(), self.xdot.data_ptr(),
                 self.ydot.data_ptr(), self.div.data_ptr(), self.zones.data_ptr(), self.nz,
-                self.jp, 1e-20, 0.5, None, s)
+                self.jp, 1e-20, 0.5, self.tp, s)
 
     class Jacobi2D(Case):
         name = "Polybench_JACOBI_2D"
@@ -300,7 +314,7 @@ def _bandwidth_cases():
 
         def run(self, s):
             return self.L.b200_polybench_jacobi_2d(self.A.data_ptr(), self.B.data_ptr(), self.N,
-                                                   self.tsteps, None, s)
+                                                   self.tsteps, self.tp, s)
 
     class Heat3D(Case):
         name = "Polybench_HEAT_3D"
@@ -318,7 +332,7 @@ def _bandwidth_cases():
 
         def run(self, s):
             return self.L.b200_polybench_heat_3d(self.A.data_ptr(), self.B.data_ptr(), self.N,
-                                                 self.tsteps, None, s)
+                                                 self.tsteps, self.tp, s)
 
     class Fdtd2D(Case):
         name = "Polybench_FDTD_2D"
@@ -349,7 +363,7 @@ def _bandwidth_cases():
             return self.L.b200_polybench_fdtd_2d_ws(self.ex.data_ptr(), self.ey.data_ptr(),
                                                     self.hz.data_ptr(), self.fict.data_ptr(),
                                                     self.nx, self.ny, self.tsteps,
-                                                    self.ws.data_ptr(), self.ws_bytes, None, s)
+                                                    self.ws.data_ptr(), self.ws_bytes, self.tp, s)
 
     class ScanI64(Case):
         name = "Algorithm_SCAN"
@@ -368,7 +382,7 @@ def _bandwidth_cases():
 
         def run(self, s):
             return self.L.b200_algorithm_scan_i64(self.x.data_ptr(), self.y.data_ptr(), self.n,
-                                                  0, self.ws.data_ptr(), self.ws_bytes, None, s)
+                                                  0, self.ws.data_ptr(), self.ws_bytes, self.tp, s)
 
     return {"Lcals_HYDRO_2D": Hydro2D, "Lcals_EOS": Eos, "Lcals_FIRST_DIFF": FirstDiff,
             "Lcals_FIRST_MIN": FirstMin, "Apps_DEL_DOT_VEC_2D": DelDotVec2D,
@@ -611,13 +625,46 @@ def workload_kernels(workload, only=None):
     return ks
 
 
-def build_cases(torch, rp, workload, seed, only=None):
+TUNING_TABLE = os.path.join(ROOT, "rajaperf_gb300", "tuning", "gb300.txt")
+# kernels whose table entry was measured for a different form than the bench
+# runs (SCAN's entry is for the suite's default FP64 scan; the bench times the
+# int64 scan)
+TABLE_SKIP = {"Algorithm_SCAN"}
+
+
+def load_tuning_table(rp, path=TUNING_TABLE):
+    """{(kernel, size): b200_tune} from a tuning table (the suite layer's
+    --tuning-table format; exact-size entries, as the autotuner writes)."""
+    table = {}
+    if not os.path.exists(path):
+        return table
+    fields = {"block": "block_size", "items": "items", "vec": "vec", "grid": "grid_blocks",
+              "tile_x": "tile_x", "tile_y": "tile_y", "tile_z": "tile_z",
+              "time_block": "time_block", "algo": "algo"}
+    for ln in open(path):
+        ln = ln.split("#", 1)[0].split()
+        if len(ln) < 3:
+            continue
+        t = rp.Tune()
+        for kv in ln[3:]:
+            k, v = kv.split("=")
+            setattr(t, fields[k], int(v))
+        table[(ln[0], int(ln[1]))] = t
+    return table
+
+
+def build_cases(torch, rp, workload, seed, only=None, table=None):
     registry = {}
     registry.update(_stream_cases())
     registry.update(_bandwidth_cases())
     params = WORKLOADS[workload].get("params", {})
-    return [registry[k](torch, rp, seed, n, **params.get(k, {}))
-            for k, n in workload_kernels(workload, only)]
+    cases = []
+    for k, n in workload_kernels(workload, only):
+        c = registry[k](torch, rp, seed, n, **params.get(k, {}))
+        if table and k not in TABLE_SKIP and (k, n) in table:
+            c.set_tune(table[(k, n)])
+        cases.append(c)
+    return cases
 
 
 # --------------------------------------------------------------------------
@@ -714,7 +761,8 @@ def run_gpu(args, rank, world):
         dist.init_process_group("nccl")
     peaks = load_peaks()
     traffic = load_traffic()
-    cases = build_cases(torch, rp, args.workload, args.seed + rank, args.kernels)
+    table = load_tuning_table(rp) if args.tuning_table else {}
+    cases = build_cases(torch, rp, args.workload, args.seed + rank, args.kernels, table)
     stream = torch.cuda.current_stream()
     s = stream.cuda_stream
     # L2 flush before every kernel: a write of a 256 MiB buffer evicts the
@@ -1134,8 +1182,10 @@ def run_e2e(torch, rp, args, peaks):
     fr, per, h2d, d2h = [], [], 0, 0
     for kname, size in workload_kernels(args.workload, args.kernels):
         opts = E2E_SUITE_ARGS.get(kname, ["-t", "default"])
+        table = ["--tuning-table", TUNING_TABLE] if args.tuning_table else []
         r = rp.run_suite(["--size", size, "--checkrun", reps, "-k", kname, "--init", "uniform",
-                          "--seed", args.seed, "--host-data", "--disable-warmup", *opts])[0]
+                          "--seed", args.seed, "--host-data", "--disable-warmup", *table,
+                          *opts])[0]
         t = r["min_time_s"] / r["reps"]
         f = r["bytes_per_rep"] / t / 1e9 / peaks["hbm_gbs"]
         fr.append(f)
@@ -1194,6 +1244,9 @@ def main():
     ap.add_argument("--workload", default=DEFAULT_WORKLOAD, choices=sorted(WORKLOADS))
     ap.add_argument("--seed", type=int, default=4793)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--tuning-table", type=int, default=1,
+                    help="1 (default): launch shapes from rajaperf_gb300/tuning/gb300.txt "
+                         "(autotuned on GB300 for these sizes); 0: library defaults")
     ap.add_argument("--no-e2e", action="store_true",
                     help="skip the host-buffer end-to-end leg")
     ap.add_argument("--kernels", type=lambda s: s.split(","), default=None,
@@ -1219,7 +1272,9 @@ def main():
               "kernels": [k for k, _ in workload_kernels(args.workload, args.kernels)],
               "l2": "flushed before every kernel: 256 MiB write, then two 256 MiB reads "
                     "of a second buffer (no dirty flush lines left to write back)",
-              "init": f"uniform [0.5,1.5) seed {args.seed}"}
+              "init": f"uniform [0.5,1.5) seed {args.seed}",
+              "launch_shapes": ("rajaperf_gb300/tuning/gb300.txt (autotuned on GB300)"
+                                if args.tuning_table else "library defaults")}
     metric = "geomean % of measured HBM copy peak over kernels (suite Bytes/rep)"
 
     if args.impl == "reference":

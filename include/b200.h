@@ -410,12 +410,15 @@ int b200_gemm_split(const double* A, const double* B, double* C, int64_t m,
 size_t b200_scan_workspace_bytes(int64_t n);
 
 /* y[i] = init + sum_{j<i} x[j] (exclusive), single-pass decoupled lookback.
- * Default (tune->algo 0, x and y 16-byte aligned): one persistent CTA per SM
- * streams 4096-item tiles through a ring of shared-memory stages with bulk
- * copies (TMA), with warps dedicated to loading, tile aggregates, lookback
- * and the in-place scan.  tune->algo 1 (and unaligned pointers): one CTA per
- * tile with a dedicated lookback warp; tune->items selects its tile (32:
- * 8192 items, the default; 16: 4096)
+ * Two kernels: the ring (one persistent CTA per SM streams 4096-item tiles
+ * through a ring of shared-memory stages with bulk copies (TMA), with warps
+ * dedicated to loading, tile aggregates, lookback and the in-place scan) and
+ * the tile kernel (one CTA per tile with a dedicated lookback warp;
+ * tune->items selects its tile, 32: 8192 items, the default; 16: 4096).
+ * tune->algo 0 picks the ring for int64 and the tile kernel for FP64 (a
+ * ring tile's FP64 aggregate is summed by one warp, on one sub-partition's
+ * FP64 unit: 659 vs 466 us at 2^26); 1 forces the tile kernel, 2 the ring.
+ * Unaligned x or y take the tile kernel.
  *   -- algorithm/SCAN.hpp:23-36, SCAN-Cuda.cpp:143-300.  One launch.        */
 int b200_algorithm_scan(const double* x, double* y, int64_t n, double init,
                         void* workspace, size_t workspace_bytes,

@@ -18,6 +18,8 @@
 #include "b200_pipeline.cuh"
 #include "b200_reduce.cuh"
 
+#include <type_traits>
+
 using namespace b200;
 
 namespace {
@@ -394,7 +396,7 @@ int launch_scan(const char* name, const T* x, T* y, int64_t n, T init, void* ws,
   const int64_t slots = scan_tiles_max(n);
   if (slots > 0x7fffffffLL) return invalid("%s: n too large", name);
   const int algo = tune ? tune->algo : 0;
-  if (algo != 0 && algo != 1) return invalid("%s: algo %d (0 or 1)", name, algo);
+  if (algo < 0 || algo > 2) return invalid("%s: algo %d (0, 1 or 2)", name, algo);
   if (tune && tune->block_size && tune->block_size != kScanBlock)
     return invalid("%s: block size %d (only %d)", name, tune->block_size, kScanBlock);
   const int items = (tune && tune->items) ? tune->items : kScanItemsDefault;
@@ -409,7 +411,10 @@ int launch_scan(const char* name, const T* x, T* y, int64_t n, T init, void* ws,
   const bool vec = aligned16(x) && aligned16(y) && !(tune && tune->vec == 1);
   const uint64_t lim = wait_limit_ns(tune, kDefaultWaitNs);
   int rc;
-  if (algo == 0 && vec)
+  // the ring's aggregator warp sums a tile on one sub-partition's FP64 unit
+  // (FP64-bound at 4 us per tile), so FP64 takes the tile kernel by default
+  const bool ring = vec && (algo == 2 || (algo == 0 && std::is_same<T, long long>::value));
+  if (ring)
     rc = launch_scan_pipelined<T>(x, y, n, init, w, lim, st);
   else
     rc = (items == 16) ? (vec ? launch_scan_it<T, 16, true>(x, y, n, init, w, lim, st)

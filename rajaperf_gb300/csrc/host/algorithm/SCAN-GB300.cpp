@@ -88,7 +88,11 @@ void SCAN::prepareRun(size_t tune_idx) {
                               reinterpret_cast<uintptr_t>(m_yi) % 16 == 0)
                            : (reinterpret_cast<uintptr_t>(m_x) % 16 == 0 &&
                               reinterpret_cast<uintptr_t>(m_y) % 16 == 0);
-  injectLookbackStall(m_ws, m_ws_bytes, getTune(tune_idx), aligned);
+  // the ring kernel (algo 0 for int64, 2 for FP64) is the one the stall targets
+  b200_tune tn = getTune(tune_idx);
+  if (tn.algo == 2 || (tn.algo == 0 && isInt64(tune_idx))) tn.algo = 0;
+  else if (tn.algo == 0) tn.algo = 1;
+  injectLookbackStall(m_ws, m_ws_bytes, tn, aligned);
 }
 
 void SCAN::finishRun(size_t) { checkWorkspace(m_ws, m_ws_bytes, "Algorithm_SCAN"); }

@@ -202,7 +202,7 @@ def test_fdtd_2d_ws_rejects_small_workspace():
                                            None) == rp.B200_ERR_WORKSPACE
 
 
-SCAN_TUNES = {"pipelined": dict(), "tile4096": dict(algo=1, items=16),
+SCAN_TUNES = {"default": dict(), "ring": dict(algo=2), "tile4096": dict(algo=1, items=16),
               "tile8192": dict(algo=1, items=32)}
 
 
@@ -223,7 +223,7 @@ def test_scan_f64_and_i64(n, kind):
     dyi = torch.zeros(n, dtype=torch.int64, device="cuda")
     dx, dxi = dev(x), dev(xi)
     t = rp.Tune(**SCAN_TUNES[kind])
-    other = rp.Tune(algo=1, items=16) if kind == "pipelined" else rp.Tune()
+    other = rp.Tune(algo=1, items=16) if kind in ("default", "ring") else rp.Tune(algo=2)
     for rep in range(3):  # the workspace is reused across calls
         rp.check(lib().b200_algorithm_scan(dx.data_ptr(), dy.data_ptr(), n, 0.25,
                                            w.data_ptr(), wsb, ctypes.byref(other), gu.stream()))

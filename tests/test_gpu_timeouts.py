@@ -117,14 +117,21 @@ def test_workspace_status_ok_after_split_gemm_and_rejects_small_workspace():
 
 
 @pytest.mark.parametrize("kernel,tuning", [("Algorithm_SCAN", "int64"),
-                                           ("Algorithm_SCAN", "default"),
                                            ("Basic_INDEXLIST", "default")])
 def test_suite_run_fails_on_device_timeout(kernel, tuning):
     """rp_run marks the run failed (RP_ERR_RUN) with the timeout message; the
-    same command line without the stall passes."""
+    same command line without the stall passes.  (The FP64 scan's default,
+    the one-CTA-per-tile kernel, refuses the stall: its tile ids could pass
+    the tile count.)"""
     args = ["--size", 50 * TILE, "--checkrun", 2, "-k", kernel, "-t", tuning,
             "--disable-warmup", "--wait-limit-us", 1000]
     with pytest.raises(RuntimeError, match="device-side wait timed out"):
         rp.run_suite(args + ["--inject-lookback-stall", 3])
     res = rp.run_suite(args[:-2] + ["--wait-limit-us", 200000])
     assert len(res) == 1 and res[0]["tuning"] == tuning
+
+
+def test_stall_refused_by_the_tile_kernel():
+    with pytest.raises(RuntimeError, match="needs the pipelined"):
+        rp.run_suite(["--size", 50 * TILE, "--checkrun", 1, "-k", "Algorithm_SCAN", "-t",
+                      "default", "--disable-warmup", "--inject-lookback-stall", 3])
