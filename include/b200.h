@@ -382,19 +382,22 @@ int b200_gemm_f64(const double* A, const double* B, double* C, int64_t m,
 size_t b200_gemm_split_workspace_bytes(int64_t m, int64_t n, int64_t k,
                                        const b200_tune* tune);
 
-/* C = alpha*A*B + beta*C in FP64 by split precision on bf16 tensor cores:
+/* C = alpha*A*B + beta*C in FP64 by split precision on FP8 tensor cores:
  * rows of A / columns of B are scaled by powers of two and cut into
- * tune->items (default 10) balanced 5-bit integer slices held exactly in
- * bf16; slice products of equal weight accumulate exactly in FP32 on the
- * tensor cores over chunks of at most 8192 values of k (the bound under which
- * the FP32 accumulation stays exact), each chunk folded into an FP64
- * accumulator; the weighted sum is formed in FP64.  k <= 524288.  tune->algo picks the
- * engine: 0 (default) tcgen05 MMA with TMA-fed operands and tensor-memory
- * accumulators, 1 the legacy mma.sync path.  Zero the workspace once before
- * its first use.  The 32-bit word at byte offset 16 of the workspace is set
- * to 1 if a bounded wait of the tcgen05 engine gave up (C is then invalid);
- * it stays set until b200_workspace_status() reports and clears it.  Not in
- * the reference: the split-precision form of polybench/POLYBENCH_GEMM.hpp:40-56. */
+ * tune->items (default 10) balanced 5-bit integer slices (digits of
+ * magnitude <= 16, held exactly in e4m3 or bf16); slice products of equal
+ * weight accumulate exactly in FP32 on the tensor cores over chunks of at
+ * most 8192 values of k (the bound under which the FP32 accumulation stays
+ * exact), each chunk folded into an FP64 accumulator; the weighted sum is
+ * formed in FP64.  k <= 524288.  tune->algo picks the engine: 0 (default) =
+ * 3, tcgen05 MMA (kind::f8f6f4) on e4m3 slices with TMA-fed operands and
+ * tensor-memory accumulators; 2 the same on bf16 slices (kind::f16; the same
+ * digits, so the same result whenever the accumulation is exact); 1 the
+ * legacy mma.sync path.  Zero the workspace once before its first use.  The
+ * 32-bit word at byte offset 16 of the workspace is set to 1 if a bounded
+ * wait of a tcgen05 engine gave up (C is then invalid); it stays set until
+ * b200_workspace_status() reports and clears it.  Not in the reference: the
+ * split-precision form of polybench/POLYBENCH_GEMM.hpp:40-56. */
 int b200_gemm_split(const double* A, const double* B, double* C, int64_t m,
                     int64_t n, int64_t k, double alpha, double beta,
                     void* workspace, size_t workspace_bytes,

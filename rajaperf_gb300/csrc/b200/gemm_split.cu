@@ -1,18 +1,19 @@
-// Split-precision FP64 GEMM: C = alpha*A*B + beta*C on bf16 tensor cores.
+// Split-precision FP64 GEMM: C = alpha*A*B + beta*C on FP8 (or bf16) tensor
+// cores.
 //
 // Ozaki-style splitting with exact integer slices:
 //  1. Every row i of A gets a power-of-two scale 2^Ea(i) with
 //     |A(i,k)| < 2^(Ea(i)-1); every column j of B likewise 2^Eb(j).
 //  2. q = round(A(i,k) * 2^(5S - Ea(i))) is an integer with |q| <= 2^(5S-1)
 //     (S slices of 5 bits); its base-32 digits d_1..d_S (d_1 most
-//     significant; d_2..d_S balanced in [-16, 15], |d_1| <= 17) are stored as
-//     bf16, which holds them exactly.  B is cut the same way and stored
-//     transposed (N x K).
+//     significant; d_2..d_S balanced in [-16, 15], |d_1| <= 16) are stored as
+//     e4m3 bytes (or bf16), which hold every integer of magnitude <= 16
+//     exactly.  B is cut the same way and stored transposed (N x K).
 //  3. For every digit weight w = s + t the products A_s * B_t are summed over
 //     a chunk of k on the tensor cores in one FP32 accumulator.  Each product
-//     is an integer of magnitude <= 289 and a chunk holds at most kChunkK = 8192
-//     values of k, so every partial sum is an integer below 2^24 whenever at
-//     most 7 slice pairs share a weight: the tensor-core accumulation is exact
+//     is an integer of magnitude <= 256 and a chunk holds at most kChunkK = 8192
+//     values of k, so every partial sum is an integer of magnitude at most 2^24
+//     (exact in FP32) whenever at most 8 slice pairs share a weight: the tensor-core accumulation is exact
 //     for the weights that carry the result (larger weights contribute below
 //     2^-45 of it).  Longer K is cut into balanced chunks of at most kChunkK.
 //  4. The epilogue adds 2^(-5w) * acc_(w,chunk) into an FP64 accumulator after
@@ -20,21 +21,25 @@
 //     FP64.
 // Only weights w <= S + 1 are formed (the dropped products lie below the
 // slicing error).  The error against an FP64 GEMM is measured per size by the
-// tests and bench.
+// tests and bench.  The e4m3 and bf16 slices hold the same digits, so the
+// engines' results agree bit for bit whenever the accumulation is exact.
 //
-// Engines (tune->algo):
-//  0 (default) tcgen05: one 128x128 C tile per CTA.  Warp 0 streams 128x64
-//    slice tiles of A and B into a 6-stage shared-memory ring with TMA
-//    (128-byte swizzle); warp 1 issues tcgen05.mma (kind::f16, bf16 in, FP32
-//    out) into one of two FP32 accumulators in tensor memory, one per digit
-//    weight; warps 2-5 read a finished weight's accumulator with tcgen05.ld
-//    and fold it into an FP64 accumulator that also lives in tensor memory
-//    (two 32-bit columns per element), so weight w+1's MMAs overlap weight
-//    w's FP64 epilogue.  TMEM: 2 x 128 FP32 columns + 256 FP64 columns = 512.
+// Engines (tune->algo; 0 picks 3):
+//  3 tcgen05 on e4m3 slices, 2 the same on bf16 slices: one 128x128 C tile
+//    per CTA.  Warp 0 streams 128 x (128 bytes of k) slice tiles of A and B
+//    into a 6-stage shared-memory ring with TMA (128-byte swizzle); warp 1
+//    issues tcgen05.mma (kind::f8f6f4: 32 values of k per instruction, or
+//    kind::f16: 16; FP32 out) into one of two FP32 accumulators in tensor
+//    memory, one per digit weight; warps 2-5 read a finished weight's
+//    accumulator with tcgen05.ld and fold it into an FP64 accumulator that
+//    also lives in tensor memory (two 32-bit columns per element), so weight
+//    w+1's MMAs overlap weight w's FP64 epilogue.  TMEM: 2 x 128 FP32 columns
+//    + 256 FP64 columns = 512.  An e4m3 tile carries twice the k of a bf16
+//    tile in the same 16 KB, so the shared-memory traffic per MMA flop halves.
 //  1 mma.sync.m16n8k16 bf16 -> fp32, 128x128 C tile per CTA (8 warps of
 //    64x32), 32-wide K stages double-buffered through shared memory with
 //    cp.async (the legacy tensor-core path, kept for comparison).
-// Every wait of the tcgen05 engine is bounded (1 s by default,
+// Every wait of the tcgen05 engines is bounded (1 s by default,
 // b200_tune.wait_limit_us); one that gives up sets the error word at byte
 // offset 16 of the workspace and the CTA winds down.
 #include "b200_internal.cuh"
@@ -43,6 +48,7 @@
 #include <cuda.h>
 #include <cudaTypedefs.h>
 #include <cuda_bf16.h>
+#include <cuda_fp8.h>
 
 #include <mutex>
 
@@ -98,9 +104,10 @@ __global__ void col_scale_kernel(const double* __restrict__ B, int64_t K, int64_
   E[j] = scale_exponent(m);
 }
 
-// Base-32 digits of q = round(v * 2^shift), |q| <= 2^(5S-1): the S-1 low
-// digits are balanced (in [-16, 15]); the top digit takes what is left,
-// |d_0| <= 17 (balanced digits alone only reach 0.484 * 32^S).
+// Base-32 digits of q = round(v * 2^shift), |q| <= 2^(5S-1) = 16 * 32^(S-1):
+// the S-1 low digits are balanced (in [-16, 15], together within
+// [-0.52, 0.49] * 32^(S-1)); the top digit takes what is left, an integer of
+// magnitude below 16.52, so |d_0| <= 16.
 __device__ __forceinline__ void digits_of(double v, int shift, int S, float* d) {
   long long q = __double2ll_rn(scalbn(v, shift));
   for (int s = S - 1; s >= 1; --s) {
@@ -111,10 +118,21 @@ __device__ __forceinline__ void digits_of(double v, int shift, int S, float* d) 
   d[0] = static_cast<float>(q);
 }
 
+// A digit in the slice arrays' storage type: bf16 (exact for |d| <= 256) or
+// e4m3 (exact for the integers |d| <= 16; the conversion is exact for them).
+template <typename T> __device__ __forceinline__ T digit_store(float d);
+template <> __device__ __forceinline__ __nv_bfloat16 digit_store<__nv_bfloat16>(float d) {
+  return __float2bfloat16_rn(d);
+}
+template <> __device__ __forceinline__ uint8_t digit_store<uint8_t>(float d) {
+  return static_cast<uint8_t>(__nv_cvt_float_to_fp8(d, __NV_SATFINITE, __NV_E4M3));
+}
+
 // As[s][i][k] (Mp x Kp, zero padded) from A (M x K).
+template <typename T>
 __global__ void slice_a_kernel(const double* __restrict__ A, int64_t M, int64_t K,
                                const int* __restrict__ E, int S, int64_t Mp, int64_t Kp,
-                               __nv_bfloat16* __restrict__ As) {
+                               T* __restrict__ As) {
   const int64_t k = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
   const int64_t i = blockIdx.y;
   if (k >= Kp) return;
@@ -124,14 +142,15 @@ __global__ void slice_a_kernel(const double* __restrict__ A, int64_t M, int64_t 
   } else {
     for (int s = 0; s < S; ++s) d[s] = 0.f;
   }
-  for (int s = 0; s < S; ++s) As[(s * Mp + i) * Kp + k] = __float2bfloat16_rn(d[s]);
+  for (int s = 0; s < S; ++s) As[(s * Mp + i) * Kp + k] = digit_store<T>(d[s]);
 }
 
 // Bt[t][j][k] (Np x Kp) from B (K x N): a 32x32 tile transpose through smem.
+template <typename T>
 __global__ void slice_b_kernel(const double* __restrict__ B, int64_t K, int64_t N,
                                const int* __restrict__ E, int S, int64_t Np, int64_t Kp,
-                               __nv_bfloat16* __restrict__ Bt) {
-  __shared__ signed char tile[kMaxSlices][32][33];  // digits are in [-16, 15]
+                               T* __restrict__ Bt) {
+  __shared__ signed char tile[kMaxSlices][32][33];  // digits are in [-16, 16]
   const int64_t j0 = static_cast<int64_t>(blockIdx.x) * 32, k0 = static_cast<int64_t>(blockIdx.y) * 32;
   const int tx = threadIdx.x, ty = threadIdx.y;  // 32 x 8
   for (int r = ty; r < 32; r += 8) {
@@ -149,7 +168,7 @@ __global__ void slice_b_kernel(const double* __restrict__ B, int64_t K, int64_t 
     const int64_t j = j0 + r, k = k0 + tx;
     if (j < Np && k < Kp)
       for (int s = 0; s < S; ++s)
-        Bt[(s * Np + j) * Kp + k] = __float2bfloat16_rn(static_cast<float>(tile[s][tx][r]));
+        Bt[(s * Np + j) * Kp + k] = digit_store<T>(static_cast<float>(tile[s][tx][r]));
   }
 }
 
@@ -310,9 +329,12 @@ __global__ void __launch_bounds__(256, 1) ozaki_mma_kernel(SplitArgs g) {
 // ---- tcgen05 engine ------------------------------------------------------------
 namespace tc {
 
-constexpr int BM = 128, BN = 128, BK = 64;          // BK bf16 = one 128-byte swizzle row
+constexpr int BM = 128, BN = 128;
+constexpr int kRowBytes = 128;                      // one 128-byte swizzle row of K
+// k values per k block: 64 bf16 or 128 e4m3 (one swizzle row either way)
+template <bool F8> constexpr int kBK = F8 ? 128 : 64;
 constexpr int kStages = 6;
-constexpr uint32_t kTileBytes = BM * BK * 2;        // 16 KB per operand tile
+constexpr uint32_t kTileBytes = BM * kRowBytes;     // 16 KB per operand tile
 constexpr uint32_t kStageBytes = 2 * kTileBytes;    // A + B
 constexpr int kThreads = 192;                       // TMA, MMA, 4 epilogue warps
 constexpr uint32_t kTmemCols = 512;
@@ -320,11 +342,13 @@ constexpr uint32_t kAcc64Col = 2 * BN;              // FP64 accumulator columns 
 constexpr uint64_t kWaitLimitNs = 1000000000ull;    // default wait limit: 1 s
 constexpr size_t kSmemBytes = 1024 + kStages * kStageBytes + 256;
 
-// Instruction descriptor, kind::f16: D = F32 (bits 4-5 = 1), A = B = BF16
-// (bits 7-9, 10-12 = 1), both K-major, N >> 3 at bits 17-22, M >> 4 at 24-28.
-constexpr uint32_t kIdesc = (1u << 4) | (1u << 7) | (1u << 10) |
-                            (static_cast<uint32_t>(BN >> 3) << 17) |
-                            (static_cast<uint32_t>(BM >> 4) << 24);
+// Instruction descriptors: D = F32 (bits 4-5 = 1), both operands K-major,
+// N >> 3 at bits 17-22, M >> 4 at 24-28; A and B formats at bits 7-9 and
+// 10-12: kind::f16 BF16 = 1, kind::f8f6f4 E4M3 = 0 (A and B the same type).
+constexpr uint32_t kIdescShape = (1u << 4) | (static_cast<uint32_t>(BN >> 3) << 17) |
+                                 (static_cast<uint32_t>(BM >> 4) << 24);
+template <bool F8>
+constexpr uint32_t kIdesc = F8 ? kIdescShape : (kIdescShape | (1u << 7) | (1u << 10));
 static_assert(kSmemBytes <= 232448, "shared memory budget");
 
 // Waits for the phase of parity `parity` to complete.  Gives up after
@@ -371,14 +395,26 @@ __device__ __forceinline__ uint64_t sw128_desc(uint32_t saddr) {
   return static_cast<uint64_t>((saddr >> 4) & 0x3FFFu) | (1ull << 16) |
          (static_cast<uint64_t>(1024 >> 4) << 32) | (1ull << 46) | (2ull << 61);
 }
-__device__ __forceinline__ void umma_bf16(uint32_t d_tmem, uint64_t adesc, uint64_t bdesc,
-                                          uint32_t accumulate) {
-  asm volatile(
-      "{\n\t.reg .pred p;\n\t"
-      "setp.ne.b32 p, %4, 0;\n\t"
-      "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(d_tmem),
-      "l"(adesc), "l"(bdesc), "r"(kIdesc), "r"(accumulate)
-      : "memory");
+// One 128 x 128 x (32 bytes of K) MMA: 16 bf16 (kind::f16) or 32 e4m3
+// (kind::f8f6f4) values of k, FP32 accumulation in tensor memory.
+template <bool F8>
+__device__ __forceinline__ void umma(uint32_t d_tmem, uint64_t adesc, uint64_t bdesc,
+                                     uint32_t accumulate) {
+  if constexpr (F8) {
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "setp.ne.b32 p, %4, 0;\n\t"
+        "tcgen05.mma.cta_group::1.kind::f8f6f4 [%0], %1, %2, %3, p;\n\t}" ::"r"(d_tmem),
+        "l"(adesc), "l"(bdesc), "r"(kIdesc<true>), "r"(accumulate)
+        : "memory");
+  } else {
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "setp.ne.b32 p, %4, 0;\n\t"
+        "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(d_tmem),
+        "l"(adesc), "l"(bdesc), "r"(kIdesc<false>), "r"(accumulate)
+        : "memory");
+  }
 }
 __device__ __forceinline__ void umma_commit(uint64_t* bar) {
   asm volatile(
@@ -440,9 +476,11 @@ struct TcArgs {
   uint64_t limit_ns;  // limit of every bounded wait
 };
 
+template <bool F8>
 __global__ void __launch_bounds__(kThreads, 1)
 ozaki_tc_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
                 TcArgs g) {
+  constexpr int BK = kBK<F8>;
   extern __shared__ unsigned char smem_raw[];
   // stage ring aligned to 1024 B (the 128-byte swizzle atom), then barriers
   unsigned char* ring = smem_raw + ((1024u - (smem_u32(smem_raw) & 1023u)) & 1023u);
@@ -552,9 +590,9 @@ ozaki_tc_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__
             const uint32_t a_addr = smem_u32(ring + st * kStageBytes);
             const uint64_t ad = sw128_desc(a_addr), bd = sw128_desc(a_addr + kTileBytes);
 #pragma unroll
-            for (int kk = 0; kk < BK / 16; ++kk) {
-              // advance 16 bf16 (32 B) along K inside the swizzle atom
-              umma_bf16(d_acc, ad + 2u * kk, bd + 2u * kk, accumulate);
+            for (int kk = 0; kk < kRowBytes / 32; ++kk) {
+              // advance 32 bytes along K inside the swizzle atom
+              umma<F8>(d_acc, ad + 2u * kk, bd + 2u * kk, accumulate);
               accumulate = 1u;
             }
             umma_commit(empty + st);
@@ -666,37 +704,52 @@ PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
   return fn;
 }
 
-// 2-D bf16 view [rows][Kp] with a 64 x 128 box and 128-byte swizzle.
-bool encode_slices(CUtensorMap* map, const void* base, int64_t rows, int64_t Kp) {
+// 2-D view [rows][Kp] of the slices (bf16 or e4m3 bytes) with a box of
+// 128 bytes of K x 128 rows and 128-byte swizzle.
+bool encode_slices(CUtensorMap* map, const void* base, int64_t rows, int64_t Kp, bool f8) {
   PFN_cuTensorMapEncodeTiled_v12000 fn = encode_fn();
   if (!fn) return false;
+  const cuuint64_t esize = f8 ? 1u : 2u;
   cuuint64_t dims[2] = {static_cast<cuuint64_t>(Kp), static_cast<cuuint64_t>(rows)};
-  cuuint64_t strides[1] = {static_cast<cuuint64_t>(Kp) * 2u};
-  cuuint32_t box[2] = {static_cast<cuuint32_t>(BK), static_cast<cuuint32_t>(BM)};
+  cuuint64_t strides[1] = {static_cast<cuuint64_t>(Kp) * esize};
+  cuuint32_t box[2] = {static_cast<cuuint32_t>(kRowBytes / esize), static_cast<cuuint32_t>(BM)};
   cuuint32_t estr[2] = {1u, 1u};
-  return fn(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, const_cast<void*>(base), dims, strides,
+  return fn(map, f8 ? CU_TENSOR_MAP_DATA_TYPE_UINT8 : CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2,
+            const_cast<void*>(base), dims, strides,
             box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
             CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
 }
 
 }  // namespace tc
 
+// Engines (tune->algo): 0 the default (the tcgen05 e4m3 engine), 1 mma.sync,
+// 2 tcgen05 with bf16 slices, 3 tcgen05 with e4m3 slices.
+enum Engine { kEngineDefault = 0, kEngineMmaSync = 1, kEngineTcBf16 = 2, kEngineTcE4m3 = 3 };
+
+int engine_of(const b200_tune* t) {
+  const int e = (t && t->algo) ? t->algo : kEngineDefault;
+  return e == kEngineDefault ? kEngineTcE4m3 : e;
+}
+
 struct SplitLayout {
   int64_t Mp, Np, Kp;
+  int esize;  // bytes per stored digit
   size_t off_err, off_ea, off_eb, off_as, off_bt, total;
 };
 
-SplitLayout split_layout(int64_t m, int64_t n, int64_t k, int S) {
+// The slice arrays' K is padded to one 128-byte TMA row (64 bf16 or 128 e4m3).
+SplitLayout split_layout(int64_t m, int64_t n, int64_t k, int S, int engine) {
   SplitLayout L;
+  L.esize = engine == kEngineTcE4m3 ? 1 : 2;
   L.Mp = round_up(m > 0 ? m : 1, TM);
   L.Np = round_up(n > 0 ? n : 1, TN);
-  L.Kp = round_up(k > 0 ? k : 1, kPadK);
+  L.Kp = round_up(k > 0 ? k : 1, engine == kEngineTcE4m3 ? 128 : kPadK);
   L.off_err = 16;  // the error word, at the same offset as in the scan workspaces
   L.off_ea = 256;
   L.off_eb = L.off_ea + round_up(L.Mp * 4, 256);
   L.off_as = L.off_eb + round_up(L.Np * 4, 256);
-  L.off_bt = L.off_as + round_up(static_cast<int64_t>(S) * L.Mp * L.Kp * 2, 256);
-  L.total = L.off_bt + round_up(static_cast<int64_t>(S) * L.Np * L.Kp * 2, 256);
+  L.off_bt = L.off_as + round_up(static_cast<int64_t>(S) * L.Mp * L.Kp * L.esize, 256);
+  L.total = L.off_bt + round_up(static_cast<int64_t>(S) * L.Np * L.Kp * L.esize, 256);
   return L;
 }
 
@@ -704,12 +757,26 @@ int slices_of(const b200_tune* t) {
   return (t && t->items) ? t->items : kDefaultSlices;
 }
 
+template <typename T>
+void launch_slicing(const double* A, const double* B, int64_t m, int64_t n, int64_t k,
+                    const SplitLayout& L, int S, int* Ea, int* Eb, T* As, T* Bt,
+                    cudaStream_t st) {
+  row_scale_kernel<<<static_cast<unsigned>(ceil_div(m, 8)), 256, 0, st>>>(A, m, k, Ea);
+  col_scale_kernel<<<static_cast<unsigned>(ceil_div(n, 256)), 256, 0, st>>>(B, k, n, Eb);
+  slice_a_kernel<T><<<dim3(static_cast<unsigned>(ceil_div(L.Kp, 256)),
+                           static_cast<unsigned>(L.Mp)),
+                      256, 0, st>>>(A, m, k, Ea, S, L.Mp, L.Kp, As);
+  slice_b_kernel<T><<<dim3(static_cast<unsigned>(ceil_div(L.Np, 32)),
+                           static_cast<unsigned>(ceil_div(L.Kp, 32))),
+                      dim3(32, 8), 0, st>>>(B, k, n, Eb, S, L.Np, L.Kp, Bt);
+}
+
 }  // namespace
 
 extern "C" {
 
 size_t b200_gemm_split_workspace_bytes(int64_t m, int64_t n, int64_t k, const b200_tune* tune) {
-  return split_layout(m, n, k, slices_of(tune)).total;
+  return split_layout(m, n, k, slices_of(tune), engine_of(tune)).total;
 }
 
 int b200_gemm_split(const double* A, const double* B, double* C, int64_t m, int64_t n,
@@ -718,51 +785,58 @@ int b200_gemm_split(const double* A, const double* B, double* C, int64_t m, int6
   if (!A || !B || !C || m < 0 || n < 0 || k < 0) return invalid("b200_gemm_split: bad args");
   const int S = slices_of(tune);
   if (S < 2 || S > kMaxSlices) return invalid("b200_gemm_split: slices %d not in [2, %d]", S, kMaxSlices);
-  const int engine = (tune && tune->algo) ? tune->algo : 0;
-  if (engine != 0 && engine != 1) return invalid("b200_gemm_split: engine %d (0 or 1)", engine);
+  const int engine = engine_of(tune);
+  if (engine < kEngineMmaSync || engine > kEngineTcE4m3)
+    return invalid("b200_gemm_split: engine %d (0 to 3)", engine);
   if (k > kMaxK)
     return invalid("b200_gemm_split: k = %lld exceeds %lld", static_cast<long long>(k),
                    static_cast<long long>(kMaxK));
   if (m == 0 || n == 0) return B200_OK;
-  SplitLayout L = split_layout(m, n, k, S);
+  const SplitLayout L = split_layout(m, n, k, S, engine);
   if (!workspace || workspace_bytes < L.total) {
     set_error("b200_gemm_split: workspace %zu bytes, need %zu", workspace_bytes, L.total);
     return B200_ERR_WORKSPACE;
   }
-  if (L.Mp / TM > 65535) return invalid("b200_gemm_split: m too large");
-  if (engine == 0 && device_info().cc_major < 10)
-    return unsupported("b200_gemm_split: the tcgen05 engine needs compute capability 10.x");
+  if (L.Mp > 65535) return invalid("b200_gemm_split: m too large");
+  if (engine != kEngineMmaSync && device_info().cc_major < 10)
+    return unsupported("b200_gemm_split: the tcgen05 engines need compute capability 10.x");
   char* w = static_cast<char*>(workspace);
   unsigned int* err = reinterpret_cast<unsigned int*>(w + L.off_err);
   int* Ea = reinterpret_cast<int*>(w + L.off_ea);
   int* Eb = reinterpret_cast<int*>(w + L.off_eb);
-  __nv_bfloat16* As = reinterpret_cast<__nv_bfloat16*>(w + L.off_as);
-  __nv_bfloat16* Bt = reinterpret_cast<__nv_bfloat16*>(w + L.off_bt);
   cudaStream_t st = as_stream(stream);
+  const bool f8 = engine == kEngineTcE4m3;
   // zero-sized k: C = beta*C through the same epilogue (all digits zero)
-  row_scale_kernel<<<static_cast<unsigned>(ceil_div(m, 8)), 256, 0, st>>>(A, m, k, Ea);
-  col_scale_kernel<<<static_cast<unsigned>(ceil_div(n, 256)), 256, 0, st>>>(B, k, n, Eb);
-  if (L.Mp > 65535) return invalid("b200_gemm_split: m too large");
-  slice_a_kernel<<<dim3(static_cast<unsigned>(ceil_div(L.Kp, 256)), static_cast<unsigned>(L.Mp)),
-                   256, 0, st>>>(A, m, k, Ea, S, L.Mp, L.Kp, As);
-  slice_b_kernel<<<dim3(static_cast<unsigned>(ceil_div(L.Np, 32)), static_cast<unsigned>(ceil_div(L.Kp, 32))),
-                   dim3(32, 8), 0, st>>>(B, k, n, Eb, S, L.Np, L.Kp, Bt);
-  if (engine == 1) {
-    SplitArgs g{As, Bt, Ea, Eb, C, m, n, L.Mp, L.Np, L.Kp, alpha, beta, S};
+  if (f8)
+    launch_slicing(A, B, m, n, k, L, S, Ea, Eb, reinterpret_cast<uint8_t*>(w + L.off_as),
+                   reinterpret_cast<uint8_t*>(w + L.off_bt), st);
+  else
+    launch_slicing(A, B, m, n, k, L, S, Ea, Eb,
+                   reinterpret_cast<__nv_bfloat16*>(w + L.off_as),
+                   reinterpret_cast<__nv_bfloat16*>(w + L.off_bt), st);
+  if (engine == kEngineMmaSync) {
+    SplitArgs g{reinterpret_cast<const __nv_bfloat16*>(w + L.off_as),
+                reinterpret_cast<const __nv_bfloat16*>(w + L.off_bt),
+                Ea, Eb, C, m, n, L.Mp, L.Np, L.Kp, alpha, beta, S};
     ozaki_mma_kernel<<<dim3(static_cast<unsigned>(L.Np / TN), static_cast<unsigned>(L.Mp / TM)),
                        256, 0, st>>>(g);
     return after_launch("b200_gemm_split", 5);
   }
   CUtensorMap tmA, tmB;
-  if (!tc::encode_slices(&tmA, As, S * L.Mp, L.Kp) || !tc::encode_slices(&tmB, Bt, S * L.Np, L.Kp))
+  if (!tc::encode_slices(&tmA, w + L.off_as, S * L.Mp, L.Kp, f8) ||
+      !tc::encode_slices(&tmB, w + L.off_bt, S * L.Np, L.Kp, f8))
     return unsupported("b200_gemm_split: cuTensorMapEncodeTiled unavailable or rejected the slices");
-  const int attr = allow_dynamic_smem(reinterpret_cast<const void*>(tc::ozaki_tc_kernel),
-                                      tc::kSmemBytes, "b200_gemm_split");
+  const void* kern = f8 ? reinterpret_cast<const void*>(tc::ozaki_tc_kernel<true>)
+                        : reinterpret_cast<const void*>(tc::ozaki_tc_kernel<false>);
+  const int attr = allow_dynamic_smem(kern, tc::kSmemBytes, "b200_gemm_split");
   if (attr != B200_OK) return attr;
   tc::TcArgs g{Ea, Eb, C, err, m, n, L.Mp, L.Np, L.Kp, alpha, beta, S,
                wait_limit_ns(tune, tc::kWaitLimitNs)};
-  tc::ozaki_tc_kernel<<<dim3(static_cast<unsigned>(L.Np / tc::BN), static_cast<unsigned>(L.Mp / tc::BM)),
-                        tc::kThreads, tc::kSmemBytes, st>>>(tmA, tmB, g);
+  const dim3 grid(static_cast<unsigned>(L.Np / tc::BN), static_cast<unsigned>(L.Mp / tc::BM));
+  if (f8)
+    tc::ozaki_tc_kernel<true><<<grid, tc::kThreads, tc::kSmemBytes, st>>>(tmA, tmB, g);
+  else
+    tc::ozaki_tc_kernel<false><<<grid, tc::kThreads, tc::kSmemBytes, st>>>(tmA, tmB, g);
   return after_launch("b200_gemm_split", 5);
 }
 

@@ -16,7 +16,8 @@ pytestmark = pytest.mark.gpu
 REL_FROB = 1e-13
 
 
-ENGINES = [0, 1]  # tcgen05 (default), mma.sync
+# 0 the default, 1 mma.sync, 2 tcgen05 on bf16 slices, 3 tcgen05 on e4m3 slices
+ENGINES = [0, 1, 2, 3]
 
 
 def run_split(A, B, C, alpha, beta, slices=None, engine=0):
@@ -35,7 +36,7 @@ def run_split(A, B, C, alpha, beta, slices=None, engine=0):
     rp.check(L.b200_gemm_split(dA.data_ptr(), dB.data_ptr(), dC.data_ptr(), m, n, k, alpha,
                                beta, ws.data_ptr(), ws_bytes, tp, gu.stream()), "gemm_split")
     got = gu.host(dC).reshape(m, n)
-    if engine == 0:
+    if engine != 1:
         assert L.b200_workspace_status(ws.data_ptr(), ws_bytes, gu.stream()) == rp.B200_OK, \
             "a bounded wait gave up"
     return got
@@ -131,14 +132,33 @@ def test_split_rejects_too_large_k():
 
 
 def test_engines_bit_identical_when_accumulation_is_exact():
-    """For k <= 1024 every FP32 partial sum is an integer below 2^24, so both
-    engines form identical weight sums and identical FP64 results."""
+    """For k <= 1024 every FP32 partial sum is an integer below 2^24, and the
+    e4m3 and bf16 slices hold the same digits, so every engine forms the
+    same weight sums and the same FP64 results."""
     rng = np.random.default_rng(21)
     A, B = rng.uniform(-1, 1, (200, 1024)), rng.uniform(-1, 1, (1024, 300))
     C = rng.uniform(-1, 1, (200, 300))
-    a = run_split(A, B, C, 0.75, -0.5, engine=0)
-    b = run_split(A, B, C, 0.75, -0.5, engine=1)
-    assert np.array_equal(a, b)
+    got = [run_split(A, B, C, 0.75, -0.5, engine=e) for e in ENGINES]
+    for e, g in zip(ENGINES[1:], got[1:]):
+        assert np.array_equal(got[0], g), e
+
+
+@pytest.mark.parametrize("engine", ENGINES)
+@pytest.mark.parametrize("k,positive", [(8192, True), (8192, False), (20000, True)])
+def test_integer_data_is_exact(engine, k, positive):
+    """Integer A and B below 2^14: every slice product sum, every chunk fold
+    and the final scaling are exact, so C = A B bit for bit (the products
+    stay below 2^53).  The all-positive case drives the FP32 partial sums of
+    a chunk (up to 8192 values of k) toward 2^24: any loss in the tensor
+    cores' accumulation (of bf16 or e4m3 products) shows here."""
+    rng = np.random.default_rng(k + 3 * positive)
+    lo = 0 if positive else -(2 ** 14) + 1
+    m, n = 136, 200
+    A = rng.integers(lo, 2 ** 14, (m, k)).astype(np.float64)
+    B = rng.integers(lo, 2 ** 14, (k, n)).astype(np.float64)
+    want = (A.astype(np.int64) @ B.astype(np.int64)).astype(np.float64)
+    got = run_split(A, B, np.zeros((m, n)), 1.0, 0.0, engine=engine)
+    assert np.array_equal(got, want), float(np.max(np.abs(got - want)))
 
 
 def test_split_rejects_unknown_engine():
