@@ -36,6 +36,7 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 HBM_FALLBACK_GBS = 6800.0
+BF16_FALLBACK_TFLOPS = 1900.0
 L2_FLUSH_BYTES = 256 << 20
 
 
@@ -43,8 +44,11 @@ def load_peaks() -> dict:
     p = os.path.join(ROOT, "MEASURED_PEAKS.json")
     if os.path.exists(p):
         d = json.load(open(p))
-        return {"hbm_gbs": float(d["hbm_gbs"]), "source": "measured"}
-    return {"hbm_gbs": HBM_FALLBACK_GBS, "source": "fallback"}
+        return {"hbm_gbs": float(d["hbm_gbs"]),
+                "bf16_tflops": float(d.get("bf16_tflops", BF16_FALLBACK_TFLOPS)),
+                "source": "measured"}
+    return {"hbm_gbs": HBM_FALLBACK_GBS, "bf16_tflops": BF16_FALLBACK_TFLOPS,
+            "source": "fallback"}
 
 
 def load_traffic() -> dict:
@@ -572,8 +576,11 @@ def measure_bw27(torch, rp, stream, peaks, fp64_instr_rate, seed, n=1 << 27, ste
                      "pct_hbm": round(100 * gbs / peaks["hbm_gbs"], 2), "bound": bound,
                      "fp64_instr_per_byte": round(ipe / bpe, 4),
                      "pct_of_own_bound": round(100 * t_floor / t, 2)})
+        # the arrays go back to torch's cache, not to the driver: memory the
+        # driver takes back is cleaned in the background, which took 18-30%
+        # of the bandwidth of the kernel timed next (measured after the 14 GB
+        # of INT_PREDICT's arrays), so no cache is emptied between kernels
         del run, keep
-        torch.cuda.empty_cache()
     hbm_rows = [r for r in rows if r["bound"] == "hbm"]
     return {
         "n": n, "balance_fp64_instr_per_byte": round(balance, 4),
@@ -858,15 +865,47 @@ def run_gpu(args, rank, world):
     }
 
 
+def measure_fp8_peak(torch, n=8192):
+    """Dense e4m3 GEMM throughput of cuBLASLt (torch._scaled_mm, FP32 scales,
+    bf16 out) at n^3, best of 10: the denominator for the split GEMM's FP8
+    tensor work.  None where torch lacks the call."""
+    try:
+        a = torch.randn(n, n, device="cuda").to(torch.float8_e4m3fn)
+        b = torch.randn(n, n, device="cuda").to(torch.float8_e4m3fn).t()
+        one = torch.ones((), device="cuda")
+        f = lambda: torch._scaled_mm(a, b, scale_a=one, scale_b=one, out_dtype=torch.bfloat16)
+        for _ in range(3):
+            f()
+        best = None
+        for _ in range(10):
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record()
+            f()
+            e1.record()
+            torch.cuda.synchronize()
+            t = e0.elapsed_time(e1) / 1e3
+            best = t if best is None else min(best, t)
+        del a, b
+        torch.cuda.empty_cache()
+        return round(2.0 * n ** 3 / best / 1e12, 1)
+    except (RuntimeError, AttributeError, TypeError):
+        return None
+
+
 def measure_gemm(torch, rp, stream, sizes=(1024, 4096, 8192), seed=4793):
     """Square C = 1.5*A*B + 1.2*C, entries uniform in [-1, 1): native FP64
-    (b200_gemm_f64) against split precision (b200_gemm_split), TFLOP/s at
-    2*N^3 and the split result's relative Frobenius error against the native
-    FP64 result; plus a variant with rows of A scaled by 2^k, k in [-20, 20]."""
+    (b200_gemm_f64) against split precision (b200_gemm_split: the default
+    e4m3 tcgen05 engine with paired digit weights, the single-weight e4m3 and
+    bf16 tcgen05 engines and the legacy mma.sync engine), TFLOP/s at 2*N^3 and the split result's relative Frobenius error
+    against the native FP64 result and cuBLAS FP64; plus a variant with rows
+    of A scaled by 2^k, k in [-20, 20]."""
     import ctypes
     L = rp.b200()
     s = stream.cuda_stream
     legacy = rp.Tune(algo=1)  # the mma.sync engine, for comparison
+    bf16 = rp.Tune(algo=2)    # the same digits on bf16 tensor cores
+    single = rp.Tune(algo=3)  # e4m3, one digit weight per 128x128 MMA
     slices = 10  # the library default (b200_gemm_split)
     pairs = slices * (slices + 1) // 2  # slice products formed per C element
     out = []
@@ -875,22 +914,24 @@ def measure_gemm(torch, rp, stream, sizes=(1024, 4096, 8192), seed=4793):
         A = torch.rand(n, n, dtype=torch.float64, device="cuda", generator=g) * 2 - 1
         B = torch.rand(n, n, dtype=torch.float64, device="cuda", generator=g) * 2 - 1
         C0 = torch.rand(n, n, dtype=torch.float64, device="cuda", generator=g) * 2 - 1
-        ws_bytes = L.b200_gemm_split_workspace_bytes(n, n, n, None)
+        ws_bytes = max(L.b200_gemm_split_workspace_bytes(n, n, n, t)
+                       for t in (None, ctypes.byref(legacy), ctypes.byref(bf16)))
         ws = torch.zeros(ws_bytes, dtype=torch.uint8, device="cuda")
         res = {"n": n}
+
+        def split(tune):
+            return lambda C: L.b200_gemm_split(A.data_ptr(), B.data_ptr(), C.data_ptr(), n, n,
+                                               n, 1.5, 1.2, ws.data_ptr(), ws_bytes, tune, s)
         for name, fn in (("native", lambda C: L.b200_gemm_f64(A.data_ptr(), B.data_ptr(),
                                                              C.data_ptr(), n, n, n, 1.5, 1.2,
                                                              None, s)),
-                         ("split", lambda C: L.b200_gemm_split(A.data_ptr(), B.data_ptr(),
-                                                               C.data_ptr(), n, n, n, 1.5, 1.2,
-                                                               ws.data_ptr(), ws_bytes, None,
-                                                               s)),
-                         ("split_mma_sync", lambda C: L.b200_gemm_split(
-                             A.data_ptr(), B.data_ptr(), C.data_ptr(), n, n, n, 1.5, 1.2,
-                             ws.data_ptr(), ws_bytes, ctypes.byref(legacy), s))):
+                         ("split", split(None)),
+                         ("split_e4m3_single_weight", split(ctypes.byref(single))),
+                         ("split_bf16", split(ctypes.byref(bf16))),
+                         ("split_mma_sync", split(ctypes.byref(legacy)))):
             C = C0.clone()
             rp.check(fn(C), name)  # warm-up
-            reps = 1 if (name != "split" and n >= 8192) else 3
+            reps = 1 if (name in ("native", "split_mma_sync") and n >= 8192) else 3
             best = None
             for _ in range(reps):
                 C = C0.clone()
@@ -912,12 +953,20 @@ def measure_gemm(torch, rp, stream, sizes=(1024, 4096, 8192), seed=4793):
         rn = ref.norm()
         res["rel_err_split_vs_cublas_fp64"] = float((res["C_split"] - ref).norm() / rn)
         res["rel_err_native_vs_cublas_fp64"] = float((res["C_native"] - ref).norm() / rn)
+        res["split_fp8_equals_split_bf16"] = bool(torch.equal(res["C_split"],
+                                                              res["C_split_bf16"]))
         del ref
         res["speedup"] = round(res["split_tflops"] / res["native_tflops"], 2)
+        res["speedup_vs_bf16_engine"] = round(res["split_tflops"] / res["split_bf16_tflops"], 2)
         res["speedup_vs_mma_sync"] = round(res["split_tflops"] / res["split_mma_sync_tflops"], 2)
-        # bf16 tensor work actually issued: `pairs` slice products of 2*n^3 each
-        res["split_bf16_tflops"] = round(res["split_tflops"] * pairs, 1)
-        del res["C_split"], res["C_native"], res["C_split_mma_sync"]
+        # tensor work actually issued: `pairs` slice products of 2*n^3 each
+        # (e4m3 for the default engine, bf16 for the bf16 engine)
+        res["split_fp8_work_tflops"] = round(res["split_tflops"] * pairs, 1)
+        res["split_bf16_work_tflops"] = round(res["split_bf16_tflops"] * pairs, 1)
+        res["split_equals_single_weight"] = bool(torch.equal(res["C_split"],
+                                                             res["C_split_e4m3_single_weight"]))
+        del res["C_split"], res["C_native"], res["C_split_mma_sync"], res["C_split_bf16"]
+        del res["C_split_e4m3_single_weight"]
         if n == sizes[-1] or n <= 4096:
             # row-scaled variant (accuracy only)
             k = torch.randint(-20, 21, (n, 1), device="cuda", generator=g).to(torch.float64)
@@ -1311,6 +1360,15 @@ def main():
         import rajaperf_gb300 as rp
         gemm = measure_gemm(torch, rp, torch.cuda.current_stream(), sizes=args.gemm_sizes)
         mm3 = measure_3mm(torch, rp, torch.cuda.current_stream())
+        fp8_peak = measure_fp8_peak(torch)
+        for row in gemm:
+            row["cublaslt_fp8_dense_tflops"] = fp8_peak
+            if fp8_peak and "split_fp8_work_tflops" in row:
+                row["split_fp8_work_frac_of_cublaslt_fp8"] = round(
+                    row["split_fp8_work_tflops"] / fp8_peak, 3)
+            if "split_bf16_work_tflops" in row:
+                row["split_bf16_work_frac_of_measured_bf16"] = round(
+                    row["split_bf16_work_tflops"] / peaks["bf16_tflops"], 3)
     bw27 = batch = None
     extras = args.extras
     if extras == "auto":

@@ -390,10 +390,12 @@ size_t b200_gemm_split_workspace_bytes(int64_t m, int64_t n, int64_t k,
  * most 8192 values of k (the bound under which the FP32 accumulation stays
  * exact), each chunk folded into an FP64 accumulator; the weighted sum is
  * formed in FP64.  k <= 524288.  tune->algo picks the engine: 0 (default) =
- * 3, tcgen05 MMA (kind::f8f6f4) on e4m3 slices with TMA-fed operands and
- * tensor-memory accumulators; 2 the same on bf16 slices (kind::f16; the same
- * digits, so the same result whenever the accumulation is exact); 1 the
- * legacy mma.sync path.  Zero the workspace once before its first use.  The
+ * 4, tcgen05 MMA (kind::f8f6f4) on e4m3 slices with TMA-fed operands and
+ * tensor-memory accumulators, digit weights w and w+1 formed together by
+ * 128x256 MMAs; 3 the same with one weight at a time (128x128 MMAs); 2 that on
+ * bf16 slices (kind::f16); 1 the legacy mma.sync path.  Every engine forms
+ * the same digits, so all agree bit for bit whenever the accumulation is
+ * exact and k <= 8192 (beyond, chunk sums are folded in a different order).  Zero the workspace once before its first use.  The
  * 32-bit word at byte offset 16 of the workspace is set to 1 if a bounded
  * wait of a tcgen05 engine gave up (C is then invalid); it stays set until
  * b200_workspace_status() reports and clears it.  Not in the reference: the

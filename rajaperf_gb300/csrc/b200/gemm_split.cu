@@ -24,10 +24,14 @@
 // tests and bench.  The e4m3 and bf16 slices hold the same digits, so the
 // engines' results agree bit for bit whenever the accumulation is exact.
 //
-// Engines (tune->algo; 0 picks 3):
+// Engines (tune->algo; 0 picks 4):
+//  4 tcgen05 on e4m3 slices with the digit weights in pairs (128 x 256 MMAs;
+//    see the paired-weight engine below): the default.
 //  3 tcgen05 on e4m3 slices, 2 the same on bf16 slices: one 128x128 C tile
-//    per CTA.  Warp 0 streams 128 x (128 bytes of k) slice tiles of A and B
-//    into a 6-stage shared-memory ring with TMA (128-byte swizzle); warp 1
+//    per CTA (CTAs ordered in groups of 8 tile rows, so that resident CTAs
+//    share operand tiles in L2).  Warp 0 streams 128 x (128 bytes of k) slice
+//    tiles of A and B into a 7-stage shared-memory ring with TMA (128-byte
+//    swizzle); warp 1
 //    issues tcgen05.mma (kind::f8f6f4: 32 values of k per instruction, or
 //    kind::f16: 16; FP32 out) into one of two FP32 accumulators in tensor
 //    memory, one per digit weight; warps 2-5 read a finished weight's
@@ -95,80 +99,152 @@ __global__ void row_scale_kernel(const double* __restrict__ A, int64_t M, int64_
   if (lane == 0) E[i] = scale_exponent(m);
 }
 
-__global__ void col_scale_kernel(const double* __restrict__ B, int64_t K, int64_t N,
-                                 int* __restrict__ E) {
-  const int64_t j = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
-  if (j >= N) return;
+// Column maxima of |B| (K x N): 32 columns x kColRows rows per CTA (32 x 8
+// threads, coalesced along the row), folded into bmax[j] with one atomicMax
+// per column and CTA (the bits of non-negative doubles order as unsigned
+// integers).  bmax starts zeroed.
+constexpr int kColRows = 256;
+__global__ void __launch_bounds__(256)
+col_max_kernel(const double* __restrict__ B, int64_t K, int64_t N,
+               unsigned long long* __restrict__ bmax) {
+  __shared__ double part[8][33];
+  const int tx = threadIdx.x, ty = threadIdx.y;
+  const int64_t j = static_cast<int64_t>(blockIdx.x) * 32 + tx;
+  const int64_t k0 = static_cast<int64_t>(blockIdx.y) * kColRows;
+  const int64_t k1 = (k0 + kColRows < K) ? k0 + kColRows : K;
   double m = 0.0;
-  for (int64_t k = 0; k < K; ++k) m = fmax(m, fabs(__ldg(B + k * N + j)));
-  E[j] = scale_exponent(m);
+  if (j < N)
+    for (int64_t k = k0 + ty; k < k1; k += 8) m = fmax(m, fabs(__ldg(B + k * N + j)));
+  part[ty][tx] = m;
+  __syncthreads();
+  if (ty == 0 && j < N) {
+#pragma unroll
+    for (int r = 1; r < 8; ++r) m = fmax(m, part[r][tx]);
+    atomicMax(bmax + j, static_cast<unsigned long long>(__double_as_longlong(m)));
+  }
 }
 
 // Base-32 digits of q = round(v * 2^shift), |q| <= 2^(5S-1) = 16 * 32^(S-1):
 // the S-1 low digits are balanced (in [-16, 15], together within
 // [-0.52, 0.49] * 32^(S-1)); the top digit takes what is left, an integer of
 // magnitude below 16.52, so |d_0| <= 16.
-__device__ __forceinline__ void digits_of(double v, int shift, int S, float* d) {
-  long long q = __double2ll_rn(scalbn(v, shift));
-  for (int s = S - 1; s >= 1; --s) {
-    long long r = ((q + 16) & 31) - 16;   // in [-16, 15]
-    d[s] = static_cast<float>(r);
-    q = (q - r) >> kSliceBits;
-  }
-  d[0] = static_cast<float>(q);
-}
 
-// A digit in the slice arrays' storage type: bf16 (exact for |d| <= 256) or
-// e4m3 (exact for the integers |d| <= 16; the conversion is exact for them).
-template <typename T> __device__ __forceinline__ T digit_store(float d);
-template <> __device__ __forceinline__ __nv_bfloat16 digit_store<__nv_bfloat16>(float d) {
-  return __float2bfloat16_rn(d);
-}
-template <> __device__ __forceinline__ uint8_t digit_store<uint8_t>(float d) {
-  return static_cast<uint8_t>(__nv_cvt_float_to_fp8(d, __NV_SATFINITE, __NV_E4M3));
-}
-
-// As[s][i][k] (Mp x Kp, zero padded) from A (M x K).
+// Digit e (0-based) of a 16-byte word of slice digits in the arrays'
+// storage type: e4m3 bytes (exact for the integers |d| <= 16) or bf16.
 template <typename T>
-__global__ void slice_a_kernel(const double* __restrict__ A, int64_t M, int64_t K,
-                               const int* __restrict__ E, int S, int64_t Mp, int64_t Kp,
-                               T* __restrict__ As) {
-  const int64_t k = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
-  const int64_t i = blockIdx.y;
-  if (k >= Kp) return;
-  float d[kMaxSlices];
-  if (i < M && k < K) {
-    digits_of(__ldg(A + i * K + k), kSliceBits * S - E[i], S, d);
+__device__ __forceinline__ void pack_digit(uint32_t (&w)[4], int e, int d) {
+  if constexpr (sizeof(T) == 1) {
+    const uint32_t b = static_cast<uint32_t>(
+        __nv_cvt_float_to_fp8(static_cast<float>(d), __NV_SATFINITE, __NV_E4M3));
+    w[e >> 2] |= b << (8 * (e & 3));
   } else {
-    for (int s = 0; s < S; ++s) d[s] = 0.f;
+    const uint32_t h = __bfloat16_as_ushort(__float2bfloat16_rn(static_cast<float>(d)));
+    w[e >> 1] |= h << (16 * (e & 1));
   }
-  for (int s = 0; s < S; ++s) As[(s * Mp + i) * Kp + k] = digit_store<T>(d[s]);
 }
 
-// Bt[t][j][k] (Np x Kp) from B (K x N): a 32x32 tile transpose through smem.
+// The S digits of q = round(v * 2^shift) (as digits_of), slice s into w[s]
+// at position e; slices are indexed at compile time (kept in registers).
 template <typename T>
-__global__ void slice_b_kernel(const double* __restrict__ B, int64_t K, int64_t N,
-                               const int* __restrict__ E, int S, int64_t Np, int64_t Kp,
-                               T* __restrict__ Bt) {
-  __shared__ signed char tile[kMaxSlices][32][33];  // digits are in [-16, 16]
-  const int64_t j0 = static_cast<int64_t>(blockIdx.x) * 32, k0 = static_cast<int64_t>(blockIdx.y) * 32;
-  const int tx = threadIdx.x, ty = threadIdx.y;  // 32 x 8
-  for (int r = ty; r < 32; r += 8) {
-    const int64_t k = k0 + r, j = j0 + tx;
-    float d[kMaxSlices];
-    if (k < K && j < N) {
-      digits_of(__ldg(B + k * N + j), kSliceBits * S - E[j], S, d);
-    } else {
-      for (int s = 0; s < S; ++s) d[s] = 0.f;
+__device__ __forceinline__ void put_digits(double v, int shift, int S, int e,
+                                           uint32_t (&w)[kMaxSlices][4]) {
+  long long q = __double2ll_rn(scalbn(v, shift));
+#pragma unroll
+  for (int s = kMaxSlices - 1; s >= 1; --s) {
+    if (s < S) {
+      const long long r = ((q + 16) & 31) - 16;   // in [-16, 15]
+      pack_digit<T>(w[s], e, static_cast<int>(r));
+      q = (q - r) >> kSliceBits;
     }
-    for (int s = 0; s < S; ++s) tile[s][r][tx] = static_cast<signed char>(d[s]);
+  }
+  pack_digit<T>(w[0], e, static_cast<int>(q));
+}
+
+// As[s][i][k] (Mp x Kp, zero padded) from A (M x K): a thread forms the digits
+// of 16 bytes' worth of consecutive k of one row (16 e4m3 or 8 bf16 digits
+// per slice) and writes one 16-byte word to every slice.
+template <typename T>
+__global__ void __launch_bounds__(128)
+slice_a_kernel(const double* __restrict__ A, int64_t M, int64_t K, const int* __restrict__ E,
+               int S, int64_t Mp, int64_t Kp, T* __restrict__ As) {
+  constexpr int kPer = 16 / static_cast<int>(sizeof(T));
+  const int64_t k0 = (static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x) * kPer;
+  const int64_t i = blockIdx.y;
+  if (k0 >= Kp) return;
+  const bool row = i < M;
+  const int shift = row ? kSliceBits * S - E[i] : 0;
+  uint32_t w[kMaxSlices][4];
+#pragma unroll
+  for (int s = 0; s < kMaxSlices; ++s) w[s][0] = w[s][1] = w[s][2] = w[s][3] = 0u;
+#pragma unroll
+  for (int e = 0; e < kPer; ++e) {
+    const int64_t k = k0 + e;
+    const double v = (row && k < K) ? __ldg(A + i * K + k) : 0.0;
+    put_digits<T>(v, shift, S, e, w);
+  }
+#pragma unroll
+  for (int s = 0; s < kMaxSlices; ++s)
+    if (s < S)
+      *reinterpret_cast<uint4*>(As + (s * Mp + i) * Kp + k0) =
+          make_uint4(w[s][0], w[s][1], w[s][2], w[s][3]);
+}
+
+// Bt[t][j][k] (Np x Kp) from B (K x N): a 32 (k) x 64 (j) tile per CTA of
+// 256 threads.  Reads run along B's rows (coalesced); the digits go through
+// shared memory (row stride 36 bytes: a warp's byte stores hit 32 banks) and
+// leave as 16-byte words along Bt's rows.  The CTAs of the first k tile also
+// write the column exponents Eb from the column maxima.
+constexpr int kBtK = 32, kBtJ = 64;
+template <typename T>
+__global__ void __launch_bounds__(256)
+slice_b_kernel(const double* __restrict__ B, int64_t K, int64_t N,
+               const unsigned long long* __restrict__ bmax, int* __restrict__ Eb, int S,
+               int64_t Np, int64_t Kp, T* __restrict__ Bt) {
+  constexpr int kPer = 16 / static_cast<int>(sizeof(T));
+  constexpr int kChunks = kBtK / kPer;  // 16-byte words per Bt row of the tile
+  __shared__ __align__(16) signed char dig[kMaxSlices][kBtJ][kBtK + 4];
+  __shared__ int sE[kBtJ];
+  const int tid = threadIdx.x;
+  const int64_t j0 = static_cast<int64_t>(blockIdx.x) * kBtJ;
+  const int64_t k0 = static_cast<int64_t>(blockIdx.y) * kBtK;
+  if (tid < kBtJ) {
+    const int64_t j = j0 + tid;
+    int e = 0;
+    if (j < N) {
+      e = scale_exponent(__longlong_as_double(static_cast<long long>(bmax[j])));
+      if (blockIdx.y == 0) Eb[j] = e;
+    }
+    sE[tid] = e;
   }
   __syncthreads();
-  for (int r = ty; r < 32; r += 8) {
-    const int64_t j = j0 + r, k = k0 + tx;
-    if (j < Np && k < Kp)
-      for (int s = 0; s < S; ++s)
-        Bt[(s * Np + j) * Kp + k] = digit_store<T>(static_cast<float>(tile[s][tx][r]));
+  const int jj = tid & (kBtJ - 1);
+  const int64_t j = j0 + jj;
+  const int shift = kSliceBits * S - sE[jj];
+#pragma unroll 2
+  for (int r = 0; r < kBtK / 4; ++r) {
+    const int kk = (tid >> 6) + 4 * r;
+    const int64_t k = k0 + kk;
+    const double v = (k < K && j < N) ? __ldg(B + k * N + j) : 0.0;
+    long long q = __double2ll_rn(scalbn(v, shift));
+#pragma unroll
+    for (int s = kMaxSlices - 1; s >= 1; --s) {
+      if (s < S) {
+        const long long d = ((q + 16) & 31) - 16;
+        dig[s][jj][kk] = static_cast<signed char>(d);
+        q = (q - d) >> kSliceBits;
+      }
+    }
+    dig[0][jj][kk] = static_cast<signed char>(q);
+  }
+  __syncthreads();
+  for (int c = tid; c < S * kBtJ * kChunks; c += 256) {
+    const int s = c / (kBtJ * kChunks), rem = c % (kBtJ * kChunks);
+    const int row = rem / kChunks, ch = rem % kChunks;
+    uint32_t w[4] = {0u, 0u, 0u, 0u};
+#pragma unroll
+    for (int e = 0; e < kPer; ++e) pack_digit<T>(w, e, dig[s][row][ch * kPer + e]);
+    *reinterpret_cast<uint4*>(Bt + (s * Np + j0 + row) * Kp + k0 + ch * kPer) =
+        make_uint4(w[0], w[1], w[2], w[3]);
   }
 }
 
@@ -333,8 +409,9 @@ constexpr int BM = 128, BN = 128;
 constexpr int kRowBytes = 128;                      // one 128-byte swizzle row of K
 // k values per k block: 64 bf16 or 128 e4m3 (one swizzle row either way)
 template <bool F8> constexpr int kBK = F8 ? 128 : 64;
-constexpr int kStages = 6;
+constexpr int kStages = 7;                          // 7 x 32 KB of operand tiles in flight
 constexpr uint32_t kTileBytes = BM * kRowBytes;     // 16 KB per operand tile
+constexpr int kRasterRows = 8;                      // tile rows per raster group
 constexpr uint32_t kStageBytes = 2 * kTileBytes;    // A + B
 constexpr int kThreads = 192;                       // TMA, MMA, 4 epilogue warps
 constexpr uint32_t kTmemCols = 512;
@@ -465,6 +542,19 @@ __device__ __forceinline__ double pair_to_double(uint32_t lo, uint32_t hi) {
   return __hiloint2double(static_cast<int>(hi), static_cast<int>(lo));
 }
 
+// This CTA's tile row (rows = true) or column under the grouped raster: CTA
+// id c = blockIdx.y * gridDim.x + blockIdx.x; group g = c / (G * nx) covers
+// tile rows [g G, g G + G) (fewer in the last group), column-major inside.
+__device__ __forceinline__ int raster_tile(bool rows) {
+  const int nx = static_cast<int>(gridDim.x), ny = static_cast<int>(gridDim.y);
+  const int c = static_cast<int>(blockIdx.y) * nx + static_cast<int>(blockIdx.x);
+  const int group = kRasterRows * nx;
+  const int first = (c / group) * kRasterRows;
+  const int rows_in = (ny - first < kRasterRows) ? ny - first : kRasterRows;
+  const int r = c % group;
+  return rows ? first + r % rows_in : r / rows_in;
+}
+
 struct TcArgs {
   const int* Ea;
   const int* Eb;
@@ -526,8 +616,10 @@ ozaki_tc_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__
   const int nch = static_cast<int>((static_cast<int64_t>(nkb) * BK + kChunkK - 1) / kChunkK);
   const int ckb = (nkb + nch - 1) / nch;
   const int npass = S * nch;
-  const int64_t i0 = static_cast<int64_t>(blockIdx.y) * BM;
-  const int64_t j0 = static_cast<int64_t>(blockIdx.x) * BN;
+  // Raster: consecutive CTAs walk groups of kRasterRows tile rows column by
+  // column, so the CTAs resident together share A rows and B columns in L2.
+  const int64_t i0 = static_cast<int64_t>(raster_tile(true)) * BM;
+  const int64_t j0 = static_cast<int64_t>(raster_tile(false)) * BN;
 
   if (warp == 0) {
     if (lane == 0) {
@@ -690,6 +782,276 @@ ozaki_tc_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__
   }
 }
 
+// ---- paired-weight engine ------------------------------------------------------
+// The same slices and chunks, with the digit weights taken in pairs (w, w+1),
+// w = 2, 4, ...: for s = 1 .. w-1 one 128 x 256 MMA multiplies A_s by the
+// stacked [B_(w-s); B_(w+1-s)] (256 rows of B in one shared-memory operand),
+// so its two 128-column halves accumulate weight w and weight w+1 at once;
+// A_w * B_1 (weight w+1 only) follows as a 128 x 128 MMA into the upper half.
+// A stage holds A_s and two B tiles (48 KB, 4 stages): 1.5x the bytes of a
+// 128 x 128 stage for 2x its MMA work, which lowers the operand bytes each SM
+// must receive per tensor cycle by a quarter.  TMEM: the pair's FP32
+// accumulator (256 columns) and the FP64 accumulator (256 columns).  Eight
+// epilogue warps (two per TMEM lane quadrant, 64 columns each) copy the
+// pair's FP32 sums to registers and release the accumulator at once, then
+// fold weight w and then weight w+1 into the FP64 accumulator (the order of
+// the single-weight engine, so results agree bit for bit when k <= 8192).
+constexpr int kPStages = 4;
+constexpr uint32_t kPStageBytes = 3 * kTileBytes;   // A, B_lo, B_hi
+constexpr int kPThreads = 320;                      // TMA, MMA, 8 epilogue warps
+constexpr uint32_t kPAcc64Col = 256;
+constexpr size_t kPSmemBytes = 1024 + kPStages * kPStageBytes + 256;
+static_assert(kPSmemBytes <= 232448, "shared memory budget");
+
+template <bool F8, int N>
+__device__ __forceinline__ void umma_n(uint32_t d_tmem, uint64_t adesc, uint64_t bdesc,
+                                       uint32_t accumulate) {
+  constexpr uint32_t idesc = (1u << 4) | (static_cast<uint32_t>(N >> 3) << 17) |
+                             (static_cast<uint32_t>(BM >> 4) << 24) |
+                             (F8 ? 0u : ((1u << 7) | (1u << 10)));
+  if constexpr (F8) {
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "setp.ne.b32 p, %4, 0;\n\t"
+        "tcgen05.mma.cta_group::1.kind::f8f6f4 [%0], %1, %2, %3, p;\n\t}" ::"r"(d_tmem),
+        "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate)
+        : "memory");
+  } else {
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "setp.ne.b32 p, %4, 0;\n\t"
+        "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(d_tmem),
+        "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate)
+        : "memory");
+  }
+}
+
+template <bool F8>
+__global__ void __launch_bounds__(kPThreads, 1)
+ozaki_tc_paired_kernel(const __grid_constant__ CUtensorMap tmA,
+                       const __grid_constant__ CUtensorMap tmB, TcArgs g) {
+  constexpr int BK = kBK<F8>;
+  extern __shared__ unsigned char smem_raw[];
+  unsigned char* ring = smem_raw + ((1024u - (smem_u32(smem_raw) & 1023u)) & 1023u);
+  uint64_t* full = reinterpret_cast<uint64_t*>(ring + kPStages * kPStageBytes);
+  uint64_t* empty = full + kPStages;
+  uint64_t* acc_full = empty + kPStages;
+  uint64_t* acc_empty = acc_full + 1;
+  uint64_t* mma_done = acc_empty + 1;
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(mma_done + 1);
+  volatile int* abort_flag = reinterpret_cast<volatile int*>(tmem_slot + 1);
+
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  if (threadIdx.x == 0) {
+    for (int st = 0; st < kPStages; ++st) {
+      mbar_init(full + st, 1);
+      mbar_init(empty + st, 1);
+    }
+    mbar_init(acc_full, 1);
+    mbar_init(acc_empty, 8);  // one arrival per epilogue warp
+    mbar_init(mma_done, 1);
+    *abort_flag = 0;
+    mbar_init_fence();
+  }
+  if (warp == 1) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
+                     smem_u32(tmem_slot)),
+                 "r"(kTmemCols)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem = *tmem_slot;
+
+  const int S = g.S;
+  const int nkb = static_cast<int>(g.Kp / BK);
+  const int nch = static_cast<int>((static_cast<int64_t>(nkb) * BK + kChunkK - 1) / kChunkK);
+  const int ckb = (nkb + nch - 1) / nch;
+  const int npairs = (S + 1) / 2;   // weights 2 .. S+1 in pairs
+  const int npass = npairs * nch;
+  const int64_t i0 = static_cast<int64_t>(raster_tile(true)) * BM;
+  const int64_t j0 = static_cast<int64_t>(raster_tile(false)) * BN;
+
+  if (warp == 0) {
+    if (lane == 0) {
+      // producer: (pass, slice step, k block) in the MMA warp's order
+      uint32_t it = 0;
+      bool ok = true;
+      for (int p = 0; ok && p < npass; ++p) {
+        const int wlo = 2 + 2 * (p / nch);
+        const bool hi = wlo + 1 <= S + 1;
+        const int kb0 = (p % nch) * ckb;
+        const int kb1 = (kb0 + ckb < nkb) ? kb0 + ckb : nkb;
+        const int smax = hi ? wlo : wlo - 1;
+        for (int sl = 1; ok && sl <= smax; ++sl) {
+          const bool extra = sl == wlo;          // A_w * B_1, weight w+1 only
+          const bool wide = hi && !extra;        // A_s * [B_(w-s); B_(w+1-s)]
+          const int tlo = extra ? 1 : wlo - sl;
+          for (int kb = kb0; kb < kb1; ++kb, ++it) {
+            const int st = static_cast<int>(it % kPStages);
+            const uint32_t ph = (it / kPStages) & 1u;
+            if (!mbar_wait(empty + st, ph ^ 1u, abort_flag, g.limit_ns)) {
+              ok = false;
+              break;
+            }
+            unsigned char* a = ring + st * kPStageBytes;
+            mbar_arrive_expect_tx(full + st, wide ? 3 * kTileBytes : 2 * kTileBytes);
+            tma_load_2d(a, &tmA, full + st, kb * BK, static_cast<int>((sl - 1) * g.Mp + i0));
+            tma_load_2d(a + kTileBytes, &tmB, full + st, kb * BK,
+                        static_cast<int>((tlo - 1) * g.Np + j0));
+            if (wide)
+              tma_load_2d(a + 2 * kTileBytes, &tmB, full + st, kb * BK,
+                          static_cast<int>((tlo) * g.Np + j0));  // B_(w+1-s) = B_(tlo+1)
+          }
+        }
+      }
+      if (!ok) {
+        const uint32_t first = it > static_cast<uint32_t>(kPStages) ? it - kPStages : 0u;
+        for (uint32_t j = first; j < it; ++j)
+          mbar_wait_drain(full + (j % kPStages), (j / kPStages) & 1u, g.limit_ns);
+      }
+    }
+  } else if (warp == 1) {
+    if (lane == 0) {
+      uint32_t it = 0;
+      bool ok = true;
+      for (int p = 0; ok && p < npass; ++p) {
+        const int wlo = 2 + 2 * (p / nch);
+        const bool hi = wlo + 1 <= S + 1;
+        const int kb0 = (p % nch) * ckb;
+        const int kb1 = (kb0 + ckb < nkb) ? kb0 + ckb : nkb;
+        const int smax = hi ? wlo : wlo - 1;
+        if (!mbar_wait(acc_empty, (static_cast<uint32_t>(p) & 1u) ^ 1u, abort_flag, g.limit_ns)) {
+          ok = false;
+          break;
+        }
+        tc_fence_after();
+        uint32_t accumulate = 0u;
+        for (int sl = 1; ok && sl <= smax; ++sl) {
+          const bool extra = sl == wlo;
+          const bool wide = hi && !extra;
+          for (int kb = kb0; kb < kb1; ++kb, ++it) {
+            const int st = static_cast<int>(it % kPStages);
+            if (!mbar_wait(full + st, (it / kPStages) & 1u, abort_flag, g.limit_ns)) {
+              ok = false;
+              break;
+            }
+            tc_fence_after();
+            const uint32_t a_addr = smem_u32(ring + st * kPStageBytes);
+            const uint64_t ad = sw128_desc(a_addr), bd = sw128_desc(a_addr + kTileBytes);
+#pragma unroll
+            for (int kk = 0; kk < kRowBytes / 32; ++kk) {
+              // advance 32 bytes along K inside the swizzle atom
+              if (wide) {
+                umma_n<F8, 256>(tmem, ad + 2u * kk, bd + 2u * kk, accumulate);
+                accumulate = 1u;
+              } else if (extra) {
+                umma_n<F8, 128>(tmem + 128u, ad + 2u * kk, bd + 2u * kk, 1u);
+              } else {
+                umma_n<F8, 128>(tmem, ad + 2u * kk, bd + 2u * kk, accumulate);
+                accumulate = 1u;
+              }
+            }
+            umma_commit(empty + st);
+          }
+        }
+        if (ok) umma_commit(acc_full);
+      }
+      umma_commit(mma_done);
+      mbar_wait_drain(mma_done, 0u, g.limit_ns);
+    }
+  } else {
+    // epilogue warps 2..9: TMEM lane quadrant q = warp % 4, columns
+    // [64 h, 64 h + 64) of each weight of the pair
+    const int q = warp & 3, h = (warp - 2) >> 2;
+    const uint32_t lane_base = static_cast<uint32_t>(32 * q) << 16;
+    const uint32_t col0 = static_cast<uint32_t>(64 * h);
+    bool ok = true;
+    for (int p = 0; p < npass; ++p) {
+      const int wlo = 2 + 2 * (p / nch);
+      const bool hi = wlo + 1 <= S + 1;
+      if (!mbar_wait(acc_full, static_cast<uint32_t>(p) & 1u, abort_flag, g.limit_ns)) {
+        ok = false;
+        break;
+      }
+      tc_fence_after();
+      uint32_t flo[64], fhi[64];
+#pragma unroll
+      for (int c = 0; c < 64; c += 16) {
+        tmem_ld16(tmem + lane_base + col0 + c, *reinterpret_cast<uint32_t(*)[16]>(flo + c));
+        tmem_ld16(tmem + lane_base + 128u + col0 + c,
+                  *reinterpret_cast<uint32_t(*)[16]>(fhi + c));
+      }
+      // wait for the loads, tied to every loaded register (no use of them is
+      // scheduled before the wait)
+      tmem_ld_wait(*reinterpret_cast<uint32_t(*)[16]>(flo));
+#pragma unroll
+      for (int c = 16; c < 64; c += 16) tmem_keep(*reinterpret_cast<uint32_t(*)[16]>(flo + c));
+#pragma unroll
+      for (int c = 0; c < 64; c += 16) tmem_keep(*reinterpret_cast<uint32_t(*)[16]>(fhi + c));
+      tc_fence_before();
+      __syncwarp();
+      if (lane == 0) mbar_arrive(acc_empty);  // the MMA warp may start the next pair
+      const double slo = scalbn(1.0, -kSliceBits * wlo);
+      const double shi = scalbn(1.0, -kSliceBits * (wlo + 1));
+#pragma unroll
+      for (int c = 0; c < 64; c += 8) {
+        uint32_t d[16];
+        if (p > 0) {
+          tmem_ld16(tmem + lane_base + kPAcc64Col + 2u * (col0 + c), d);
+          tmem_ld_wait(d);
+        } else {
+#pragma unroll
+          for (int e = 0; e < 16; ++e) d[e] = 0u;
+        }
+#pragma unroll
+        for (int e = 0; e < 8; ++e) {
+          double v = pair_to_double(d[2 * e], d[2 * e + 1]);
+          v = fma(static_cast<double>(__uint_as_float(flo[c + e])), slo, v);
+          if (hi) v = fma(static_cast<double>(__uint_as_float(fhi[c + e])), shi, v);
+          d[2 * e] = static_cast<uint32_t>(__double2loint(v));
+          d[2 * e + 1] = static_cast<uint32_t>(__double2hiint(v));
+        }
+        tmem_st16(tmem + lane_base + kPAcc64Col + 2u * (col0 + c), d);
+      }
+      tmem_st_wait();
+    }
+    if (ok) {
+      // C = alpha * 2^(Ea+Eb) * acc64 + beta * C
+      const int64_t i = i0 + 32 * q + lane;
+      const bool row_ok = i < g.M;
+      const int ea = row_ok ? g.Ea[i] : 0;
+      for (int c = 0; c < 64; c += 8) {
+        uint32_t d[16];
+        tmem_ld16(tmem + lane_base + kPAcc64Col + 2u * (col0 + c), d);
+        tmem_ld_wait(d);
+        if (row_ok) {
+#pragma unroll
+          for (int e = 0; e < 8; ++e) {
+            const int64_t j = j0 + col0 + c + e;
+            if (j < g.N) {
+              const double ab = scalbn(pair_to_double(d[2 * e], d[2 * e + 1]), ea + g.Eb[j]);
+              double* ptr = g.C + i * g.N + j;
+              *ptr = (g.beta == 0.0) ? g.alpha * ab : g.alpha * ab + g.beta * (*ptr);
+            }
+          }
+        }
+      }
+    }
+    tc_fence_before();
+  }
+  __syncthreads();
+  if (threadIdx.x == 0 && *abort_flag) atomicExch(g.error, 1u);
+  if (warp == 1) {
+    tc_fence_after();
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem),
+                 "r"(kTmemCols)
+                 : "memory");
+  }
+}
+
 PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
   static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
   static std::once_flag once;
@@ -722,32 +1084,37 @@ bool encode_slices(CUtensorMap* map, const void* base, int64_t rows, int64_t Kp,
 
 }  // namespace tc
 
-// Engines (tune->algo): 0 the default (the tcgen05 e4m3 engine), 1 mma.sync,
-// 2 tcgen05 with bf16 slices, 3 tcgen05 with e4m3 slices.
-enum Engine { kEngineDefault = 0, kEngineMmaSync = 1, kEngineTcBf16 = 2, kEngineTcE4m3 = 3 };
+// Engines (tune->algo): 0 the default (4), 1 mma.sync, 2 tcgen05 with bf16
+// slices, 3 tcgen05 with e4m3 slices, 4 the same with paired digit weights.
+enum Engine {
+  kEngineDefault = 0, kEngineMmaSync = 1, kEngineTcBf16 = 2, kEngineTcE4m3 = 3,
+  kEngineTcE4m3Paired = 4
+};
 
 int engine_of(const b200_tune* t) {
   const int e = (t && t->algo) ? t->algo : kEngineDefault;
-  return e == kEngineDefault ? kEngineTcE4m3 : e;
+  return e == kEngineDefault ? kEngineTcE4m3Paired : e;
 }
 
 struct SplitLayout {
   int64_t Mp, Np, Kp;
   int esize;  // bytes per stored digit
-  size_t off_err, off_ea, off_eb, off_as, off_bt, total;
+  size_t off_err, off_ea, off_eb, off_bmax, off_as, off_bt, total;
 };
 
 // The slice arrays' K is padded to one 128-byte TMA row (64 bf16 or 128 e4m3).
 SplitLayout split_layout(int64_t m, int64_t n, int64_t k, int S, int engine) {
   SplitLayout L;
-  L.esize = engine == kEngineTcE4m3 ? 1 : 2;
+  const bool f8 = engine == kEngineTcE4m3 || engine == kEngineTcE4m3Paired;
+  L.esize = f8 ? 1 : 2;
   L.Mp = round_up(m > 0 ? m : 1, TM);
   L.Np = round_up(n > 0 ? n : 1, TN);
-  L.Kp = round_up(k > 0 ? k : 1, engine == kEngineTcE4m3 ? 128 : kPadK);
+  L.Kp = round_up(k > 0 ? k : 1, f8 ? 128 : kPadK);
   L.off_err = 16;  // the error word, at the same offset as in the scan workspaces
   L.off_ea = 256;
   L.off_eb = L.off_ea + round_up(L.Mp * 4, 256);
-  L.off_as = L.off_eb + round_up(L.Np * 4, 256);
+  L.off_bmax = L.off_eb + round_up(L.Np * 4, 256);
+  L.off_as = L.off_bmax + round_up(L.Np * 8, 256);
   L.off_bt = L.off_as + round_up(static_cast<int64_t>(S) * L.Mp * L.Kp * L.esize, 256);
   L.total = L.off_bt + round_up(static_cast<int64_t>(S) * L.Np * L.Kp * L.esize, 256);
   return L;
@@ -758,17 +1125,29 @@ int slices_of(const b200_tune* t) {
 }
 
 template <typename T>
-void launch_slicing(const double* A, const double* B, int64_t m, int64_t n, int64_t k,
-                    const SplitLayout& L, int S, int* Ea, int* Eb, T* As, T* Bt,
-                    cudaStream_t st) {
+int launch_slicing(const double* A, const double* B, int64_t m, int64_t n, int64_t k,
+                   const SplitLayout& L, int S, char* w, cudaStream_t st) {
+  int* Ea = reinterpret_cast<int*>(w + L.off_ea);
+  int* Eb = reinterpret_cast<int*>(w + L.off_eb);
+  auto* bmax = reinterpret_cast<unsigned long long*>(w + L.off_bmax);
+  const cudaError_t e = cudaMemsetAsync(bmax, 0, static_cast<size_t>(L.Np) * 8, st);
+  if (e != cudaSuccess) {
+    set_error("b200_gemm_split: %s", cudaGetErrorString(e));
+    return B200_ERR_LAUNCH;
+  }
+  constexpr int kPer = 16 / static_cast<int>(sizeof(T));
   row_scale_kernel<<<static_cast<unsigned>(ceil_div(m, 8)), 256, 0, st>>>(A, m, k, Ea);
-  col_scale_kernel<<<static_cast<unsigned>(ceil_div(n, 256)), 256, 0, st>>>(B, k, n, Eb);
-  slice_a_kernel<T><<<dim3(static_cast<unsigned>(ceil_div(L.Kp, 256)),
+  col_max_kernel<<<dim3(static_cast<unsigned>(ceil_div(n, 32)),
+                        static_cast<unsigned>(k > 0 ? ceil_div(k, kColRows) : 1)),
+                   dim3(32, 8), 0, st>>>(B, k, n, bmax);
+  slice_a_kernel<T><<<dim3(static_cast<unsigned>(ceil_div(L.Kp, 128 * kPer)),
                            static_cast<unsigned>(L.Mp)),
-                      256, 0, st>>>(A, m, k, Ea, S, L.Mp, L.Kp, As);
-  slice_b_kernel<T><<<dim3(static_cast<unsigned>(ceil_div(L.Np, 32)),
-                           static_cast<unsigned>(ceil_div(L.Kp, 32))),
-                      dim3(32, 8), 0, st>>>(B, k, n, Eb, S, L.Np, L.Kp, Bt);
+                      128, 0, st>>>(A, m, k, Ea, S, L.Mp, L.Kp,
+                                    reinterpret_cast<T*>(w + L.off_as));
+  slice_b_kernel<T><<<dim3(static_cast<unsigned>(L.Np / kBtJ), static_cast<unsigned>(L.Kp / kBtK)),
+                      256, 0, st>>>(B, k, n, bmax, Eb, S, L.Np, L.Kp,
+                                    reinterpret_cast<T*>(w + L.off_bt));
+  return B200_OK;
 }
 
 }  // namespace
@@ -786,8 +1165,8 @@ int b200_gemm_split(const double* A, const double* B, double* C, int64_t m, int6
   const int S = slices_of(tune);
   if (S < 2 || S > kMaxSlices) return invalid("b200_gemm_split: slices %d not in [2, %d]", S, kMaxSlices);
   const int engine = engine_of(tune);
-  if (engine < kEngineMmaSync || engine > kEngineTcE4m3)
-    return invalid("b200_gemm_split: engine %d (0 to 3)", engine);
+  if (engine < kEngineMmaSync || engine > kEngineTcE4m3Paired)
+    return invalid("b200_gemm_split: engine %d (0 to 4)", engine);
   if (k > kMaxK)
     return invalid("b200_gemm_split: k = %lld exceeds %lld", static_cast<long long>(k),
                    static_cast<long long>(kMaxK));
@@ -805,15 +1184,11 @@ int b200_gemm_split(const double* A, const double* B, double* C, int64_t m, int6
   int* Ea = reinterpret_cast<int*>(w + L.off_ea);
   int* Eb = reinterpret_cast<int*>(w + L.off_eb);
   cudaStream_t st = as_stream(stream);
-  const bool f8 = engine == kEngineTcE4m3;
+  const bool f8 = engine == kEngineTcE4m3 || engine == kEngineTcE4m3Paired;
   // zero-sized k: C = beta*C through the same epilogue (all digits zero)
-  if (f8)
-    launch_slicing(A, B, m, n, k, L, S, Ea, Eb, reinterpret_cast<uint8_t*>(w + L.off_as),
-                   reinterpret_cast<uint8_t*>(w + L.off_bt), st);
-  else
-    launch_slicing(A, B, m, n, k, L, S, Ea, Eb,
-                   reinterpret_cast<__nv_bfloat16*>(w + L.off_as),
-                   reinterpret_cast<__nv_bfloat16*>(w + L.off_bt), st);
+  const int rc = f8 ? launch_slicing<uint8_t>(A, B, m, n, k, L, S, w, st)
+                    : launch_slicing<__nv_bfloat16>(A, B, m, n, k, L, S, w, st);
+  if (rc != B200_OK) return rc;
   if (engine == kEngineMmaSync) {
     SplitArgs g{reinterpret_cast<const __nv_bfloat16*>(w + L.off_as),
                 reinterpret_cast<const __nv_bfloat16*>(w + L.off_bt),
@@ -826,17 +1201,22 @@ int b200_gemm_split(const double* A, const double* B, double* C, int64_t m, int6
   if (!tc::encode_slices(&tmA, w + L.off_as, S * L.Mp, L.Kp, f8) ||
       !tc::encode_slices(&tmB, w + L.off_bt, S * L.Np, L.Kp, f8))
     return unsupported("b200_gemm_split: cuTensorMapEncodeTiled unavailable or rejected the slices");
-  const void* kern = f8 ? reinterpret_cast<const void*>(tc::ozaki_tc_kernel<true>)
-                        : reinterpret_cast<const void*>(tc::ozaki_tc_kernel<false>);
-  const int attr = allow_dynamic_smem(kern, tc::kSmemBytes, "b200_gemm_split");
+  const bool paired = engine == kEngineTcE4m3Paired;
+  const void* kern = paired ? reinterpret_cast<const void*>(tc::ozaki_tc_paired_kernel<true>)
+                     : f8   ? reinterpret_cast<const void*>(tc::ozaki_tc_kernel<true>)
+                            : reinterpret_cast<const void*>(tc::ozaki_tc_kernel<false>);
+  const size_t smem = paired ? tc::kPSmemBytes : tc::kSmemBytes;
+  const int attr = allow_dynamic_smem(kern, smem, "b200_gemm_split");
   if (attr != B200_OK) return attr;
   tc::TcArgs g{Ea, Eb, C, err, m, n, L.Mp, L.Np, L.Kp, alpha, beta, S,
                wait_limit_ns(tune, tc::kWaitLimitNs)};
   const dim3 grid(static_cast<unsigned>(L.Np / tc::BN), static_cast<unsigned>(L.Mp / tc::BM));
-  if (f8)
-    tc::ozaki_tc_kernel<true><<<grid, tc::kThreads, tc::kSmemBytes, st>>>(tmA, tmB, g);
+  if (paired)
+    tc::ozaki_tc_paired_kernel<true><<<grid, tc::kPThreads, smem, st>>>(tmA, tmB, g);
+  else if (f8)
+    tc::ozaki_tc_kernel<true><<<grid, tc::kThreads, smem, st>>>(tmA, tmB, g);
   else
-    tc::ozaki_tc_kernel<false><<<grid, tc::kThreads, tc::kSmemBytes, st>>>(tmA, tmB, g);
+    tc::ozaki_tc_kernel<false><<<grid, tc::kThreads, smem, st>>>(tmA, tmB, g);
   return after_launch("b200_gemm_split", 5);
 }
 

@@ -33,8 +33,11 @@ POLYBENCH_3MM::POLYBENCH_3MM(const RunParams& params)
                                          getActualProblemSize());
   setComplexity(Complexity::N_to_the_three_halves);
   setUsesFeature(Kernel);
-  addTuning("split_bf16", b200_tune{}, false);
-  addTuning("split_bf16_graph", b200_tune{}, true);
+  addTuning("split_fp8", b200_tune{}, false);  // the e4m3 tensor-core engine (default)
+  addTuning("split_fp8_graph", b200_tune{}, true);
+  b200_tune bf16{};
+  bf16.algo = 2;  // the same digits on bf16 tensor cores
+  addTuning("split_bf16", bf16, false);
   setVariantDefined(Base_GB300);
 }
 
@@ -44,9 +47,10 @@ bool POLYBENCH_3MM::isSplit(size_t tune_idx) const {
 
 void POLYBENCH_3MM::setUp(VariantID vid, size_t tune_idx) {
   if (isSplit(tune_idx)) {
-    m_ws_bytes = std::max(std::max(b200_gemm_split_workspace_bytes(m_ni, m_nj, m_nk, nullptr),
-                                   b200_gemm_split_workspace_bytes(m_nj, m_nl, m_nm, nullptr)),
-                          b200_gemm_split_workspace_bytes(m_ni, m_nl, m_nj, nullptr));
+    const b200_tune tn = getTune(tune_idx);
+    m_ws_bytes = std::max(std::max(b200_gemm_split_workspace_bytes(m_ni, m_nj, m_nk, &tn),
+                                   b200_gemm_split_workspace_bytes(m_nj, m_nl, m_nm, &tn)),
+                          b200_gemm_split_workspace_bytes(m_ni, m_nl, m_nj, &tn));
     m_ws = allocDeviceBytes(m_ws_bytes);
     zeroDeviceBytes(m_ws, m_ws_bytes);
   }

@@ -29,8 +29,11 @@ POLYBENCH_GEMM::POLYBENCH_GEMM(const RunParams& params)
                                    getActualProblemSize());
   setComplexity(Complexity::N_to_the_three_halves);
   setUsesFeature(Kernel);
-  addTuning("split_bf16", b200_tune{}, false);
-  addTuning("split_bf16_graph", b200_tune{}, true);
+  addTuning("split_fp8", b200_tune{}, false);  // the e4m3 tensor-core engine (default)
+  addTuning("split_fp8_graph", b200_tune{}, true);
+  b200_tune bf16{};
+  bf16.algo = 2;  // the same digits on bf16 tensor cores
+  addTuning("split_bf16", bf16, false);
   setVariantDefined(Base_GB300);
 }
 
@@ -43,7 +46,8 @@ void POLYBENCH_GEMM::setUp(VariantID vid, size_t tune_idx) {
   allocAndInitData(m_B, m_nk * m_nj, vid);
   allocAndInitDataConst(m_C, m_ni * m_nj, 0.0, vid);
   if (isSplit(tune_idx)) {
-    m_ws_bytes = b200_gemm_split_workspace_bytes(m_ni, m_nj, m_nk, nullptr);
+    const b200_tune tn = getTune(tune_idx);
+    m_ws_bytes = b200_gemm_split_workspace_bytes(m_ni, m_nj, m_nk, &tn);
     m_ws = allocDeviceBytes(m_ws_bytes);
     zeroDeviceBytes(m_ws, m_ws_bytes);
   }

@@ -30,9 +30,9 @@ RAJAPERF_GB300_KERNEL(POLYBENCH_FDTD_2D,
   size_t m_ws_bytes = 0;)
 
 // GEMM and 3MM tunings: "default"/"graph" run the native FP64 kernel;
-// "split_bf16"/"split_bf16_graph" run the split-precision tensor-core GEMM
-// (b200_gemm_split; inner dimensions up to 524288, summed in exact chunks
-// of 8192).
+// "split_fp8"/"split_fp8_graph" run the split-precision tensor-core GEMM
+// (b200_gemm_split on e4m3 slices; inner dimensions up to 524288, summed in
+// exact chunks of 8192), "split_bf16" the same digits on bf16 tensor cores.
 RAJAPERF_GB300_KERNEL(POLYBENCH_GEMM,
  public:
   void finishRun(size_t tune_idx) override;

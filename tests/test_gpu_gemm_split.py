@@ -16,8 +16,9 @@ pytestmark = pytest.mark.gpu
 REL_FROB = 1e-13
 
 
-# 0 the default, 1 mma.sync, 2 tcgen05 on bf16 slices, 3 tcgen05 on e4m3 slices
-ENGINES = [0, 1, 2, 3]
+# 0 the default, 1 mma.sync, 2 tcgen05 on bf16 slices, 3 tcgen05 on e4m3 slices,
+# 4 tcgen05 on e4m3 slices with paired digit weights (128 x 256 MMAs)
+ENGINES = [0, 1, 2, 3, 4]
 
 
 def run_split(A, B, C, alpha, beta, slices=None, engine=0):
@@ -161,10 +162,25 @@ def test_integer_data_is_exact(engine, k, positive):
     assert np.array_equal(got, want), float(np.max(np.abs(got - want)))
 
 
+@pytest.mark.parametrize("slices", [3, 7, 11, 12])
+def test_slice_counts_agree_across_engines(slices):
+    """Odd slice counts leave the last digit weight without a partner in the
+    paired engine; even and odd counts must give every engine the same
+    result (k <= 8192: one exact chunk, the same FP64 fold order)."""
+    rng = np.random.default_rng(slices)
+    A, B = rng.uniform(-1, 1, (136, 700)), rng.uniform(-1, 1, (700, 264))
+    C = rng.uniform(-1, 1, (136, 264))
+    got = [run_split(A, B, C, 1.25, 0.5, slices=slices, engine=e) for e in (2, 3, 4)]
+    assert np.array_equal(got[0], got[1]) and np.array_equal(got[0], got[2])
+    want = reference(A, B, C, 1.25, 0.5)
+    err = np.linalg.norm(got[0] - want) / np.linalg.norm(want)
+    assert err <= max(REL_FROB, 20 * 32.0 ** -slices), err
+
+
 def test_split_rejects_unknown_engine():
     torch = gu.torch_cuda()
     L = rp.b200()
     x = torch.zeros(16, dtype=torch.float64, device="cuda")
-    t = rp.Tune(algo=7)
+    t = rp.Tune(algo=9)
     assert L.b200_gemm_split(x.data_ptr(), x.data_ptr(), x.data_ptr(), 1, 1, 1, 1.0, 0.0,
                              x.data_ptr(), 128, ctypes.byref(t), None) == rp.B200_ERR_INVALID_ARG

@@ -53,8 +53,9 @@ def test_kernel_matches_suite_base_seq(kernel):
 def test_split_precision_tunings_match_base_seq(kernel):
     for rec in [r for r in RECORDS if r["kernel"] == kernel]:
         res = rp.run_suite(["--size", rec["size"], "--checkrun", rec["reps"], "-k", kernel,
-                            "-t", "split_bf16", "split_bf16_graph", "--disable-warmup"])
-        assert len(res) == 2
+                            "-t", "split_fp8", "split_fp8_graph", "split_bf16",
+                            "--disable-warmup"])
+        assert len(res) == 3
         for r in res:
             _check(kernel, rec, r)
 
