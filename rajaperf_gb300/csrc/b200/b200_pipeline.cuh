@@ -1,11 +1,12 @@
-// The stage ring of the persistent single-pass lookback kernels (SCAN,
-// INDEXLIST): one CTA per SM streams tiles of 4096 items of a 1-D array
-// through seven shared-memory stages.  This header holds what those kernels
-// share: the ring's layout and bounded waits, the producer warp (draws tile
-// ids, issues one bulk copy per tile) and the lookback warps (walk back to
-// the nearest inclusive prefix, publish the tile's own).  Each kernel adds an
-// aggregator warp (publishes a tile's aggregate as soon as it lands), its
-// compute warps, and the role that frees a stage.
+// The stage ring of SCAN's persistent single-pass lookback kernel: one CTA
+// per SM streams tiles of 4096 items of a 1-D array through seven
+// shared-memory stages.  This header holds the ring's layout and bounded
+// waits, the producer warp (draws tile ids, issues one bulk copy per tile)
+// and the lookback warps (walk back to the nearest inclusive prefix, publish
+// the tile's own); the kernel adds an aggregator warp (publishes a tile's
+// aggregate as soon as it lands), its compute warps, and the role that frees
+// a stage.  INDEXLIST's persistent kernel (indexlist.cu) keeps its own slots
+// and roles and shares the bounded wait and the aggregate's publication.
 //
 // Per stage s, mbarriers with one arrival each link the roles:
 //   drawn[s]  producer -> lookback      the stage's tile id is set
@@ -42,6 +43,7 @@ constexpr unsigned int kEnd = 0xffffffffu;   // end marker in ticket[]
 
 template <typename In, typename Acc>
 struct Ring {
+  using AccT = Acc;
   In tile[kStages][kTile];
   Acc agg[kStages];
   Acc excl[kStages];
@@ -74,10 +76,9 @@ __device__ __forceinline__ void init(Ring<In, Acc>& r, uint64_t limit_ns) {
 
 // Bounded wait by a whole warp; the result is the same in every lane (a lane
 // that gave up fails the warp).  On expiry records the error and stops every
-// role of the CTA.
-template <typename In, typename Acc>
-__device__ __forceinline__ bool wait(Ring<In, Acc>& r, uint64_t* bar, uint32_t parity,
-                                     ScanHeader* hdr) {
+// role of the CTA.  R: a Ring, or any struct with its limit_ns and abort.
+template <class R>
+__device__ __forceinline__ bool wait(R& r, uint64_t* bar, uint32_t parity, ScanHeader* hdr) {
   const bool ok = __all_sync(0xffffffffu, mbar_wait_for(bar, parity, r.limit_ns));
   if (!ok && (threadIdx.x & 31) == 0) {
     atomicExch(&hdr->error, 1u);
@@ -176,12 +177,13 @@ __device__ void look_back(Ring<In, Acc>& r, TileDesc* descs, Acc init, ScanHeade
 }
 
 // The aggregator's publish step (lane 0): the tile's aggregate, for tile 0
-// only locally (its inclusive prefix comes from its lookback warp).
-template <typename In, typename Acc>
-__device__ __forceinline__ void publish_aggregate(Ring<In, Acc>& r, TileDesc* descs, int s,
-                                                  unsigned int tile, Acc total) {
+// only locally (its inclusive prefix comes from its lookback warp).  R: a
+// Ring, or any struct with per-slot agg (of R::AccT) and the epoch.
+template <class R>
+__device__ __forceinline__ void publish_aggregate(R& r, TileDesc* descs, int s,
+                                                  unsigned int tile, typename R::AccT total) {
   r.agg[s] = total;
-  if (tile > 0) desc_store(descs + tile, r.epoch * 4 + 1, to_bits<Acc>(total));
+  if (tile > 0) desc_store(descs + tile, r.epoch * 4 + 1, to_bits<typename R::AccT>(total));
 }
 
 // Thread 0 after the CTA's final barrier: after an abort, bulk copies may
