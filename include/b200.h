@@ -460,7 +460,12 @@ size_t b200_indexlist_workspace_bytes(int64_t n);
 
 /* list[count++] = i for every i (in order) with x[i] < 0; *len = count.
  * n <= 2^31 - 1 (the list is int32, the suite's Int_type).  One launch,
- * single-pass compaction on a decoupled lookback
+ * single-pass compaction on a decoupled lookback.  tune->algo 0 (x 16-byte
+ * aligned): one persistent CTA per SM; tiles of 4096 items arrive by bulk
+ * copy, are ranked into 512-byte selection slots (freeing their stage at
+ * once) and wait there for their base counts; runs of 4 consecutive tiles per
+ * ticket need one global lookback each.  tune->algo 1 (and an unaligned x):
+ * one CTA per 8192-item tile.
  *   -- basic/INDEXLIST.hpp:28-34, INDEXLIST-Cuda.cpp:33; also the list and
  *   count of basic/INDEXLIST_3LOOP.hpp:39-45, INDEXLIST_3LOOP-Cuda.cpp:34-56. */
 int b200_basic_indexlist(const double* x, int32_t* list, int64_t n, int64_t* len,

@@ -85,6 +85,35 @@ def test_indexlist(case, algo):
     assert int(gu.host(ws[0:4]).view(np.uint32)[0]) == 0  # ticket count reset
 
 
+@pytest.mark.parametrize("n", [4096, 8193, 4096 * 5, 4096 * 4 * 152 + 4095,
+                               4096 * (4 * 152 * 2 + 1), 4096 * 24 * 152 + 17])
+@pytest.mark.parametrize("offset", [0, 1])
+def test_indexlist_run_and_slot_edges(n, offset):
+    """The persistent kernel draws runs of 4 consecutive tiles: one tile,
+    a run plus one, exactly one run per CTA plus a ragged tile, two runs per
+    CTA plus one, and more tiles than a CTA's 24 slots hold, so slots and
+    stages wrap; offset 1 makes x unaligned (the one-CTA-per-tile kernel)."""
+    torch = gu.torch_cuda()
+    rng = np.random.default_rng(n + offset)
+    x = rng.uniform(-1, 1, n + offset)
+    x[rng.integers(0, n + offset, 64)] = -0.0  # never selected
+    dx = gu.dev(x)
+    lst = torch.full((n,), -5, dtype=torch.int32, device="cuda")
+    ln = zeros(1, torch.int64)
+    wsb = lib().b200_indexlist_workspace_bytes(n)
+    ws = zeros(wsb, torch.uint8)
+    for _ in range(2):
+        rp.check(lib().b200_basic_indexlist(dx.data_ptr() + 8 * offset, lst.data_ptr(), n,
+                                            ln.data_ptr(), ws.data_ptr(), wsb, None,
+                                            gu.stream()))
+        want = np.nonzero(x[offset:] < 0.0)[0]
+        assert int(gu.host(ln)[0]) == want.size
+        got = gu.host(lst)
+        assert np.array_equal(got[:want.size], want.astype(np.int32))
+        assert np.all(got[want.size:] == -5)
+    assert lib().b200_workspace_status(ws.data_ptr(), wsb, gu.stream()) == rp.B200_OK
+
+
 @pytest.mark.parametrize("num_bins", [1, 10, 1000, 20000])
 @pytest.mark.parametrize("layout", ["runs", "random"])
 def test_histogram(num_bins, layout):
