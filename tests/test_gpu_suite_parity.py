@@ -6,6 +6,7 @@ call per rep) and "graph" (rep loop replayed as a CUDA graph) tunings.
 Tolerances: relative 1e-12 for element-wise and stencil kernels; exact for
 FIRST_MIN's location; for the sums (DOT, REDUCE_SUM, SCAN) the reassociation
 bound (n + log2 n + reps) * 2^-53 * sum|terms| relative to the checksum."""
+import csv
 import json
 import math
 import os
@@ -14,6 +15,8 @@ import pytest
 
 import rajaperf_gb300 as rp
 from tests import gpu_util as gu
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 
 pytestmark = pytest.mark.gpu
 
@@ -181,3 +184,24 @@ def test_report_files(tmp_path):
     assert "base_ref" in fom[3]
     with pytest.raises(RuntimeError, match="not available"):
         rp.run_suite(["--size", 100, "-k", "Stream_TRIAD", "--refvar", "Base_Seq"])
+
+
+def test_size_sweep_runs_the_suite(tmp_path):
+    """rajaperf_gb300.sweep with the suite executable: one run per size, each
+    writing its timing report where the sweep gathers it."""
+    import subprocess
+    import sys
+    exe = os.path.join(ROOT, "rajaperf_gb300", "bin", "rajaperf-gb300")
+    r = subprocess.run([sys.executable, "-m", "rajaperf_gb300.sweep", "-x", exe, "-m", "4096",
+                        "-M", "16384", "-r", "4", "--summary", "sum.csv", "--", "-k",
+                        "Stream_TRIAD", "Lcals_FIRST_DIFF", "--checkrun", "2"],
+                       cwd=tmp_path, capture_output=True, text=True,
+                       env=dict(os.environ, PYTHONPATH=ROOT))
+    assert r.returncode == 0, r.stdout + r.stderr
+    for size in (4096, 16384):
+        d = tmp_path / "RAJAPerf_0" / f"SIZE_{size:09d}"
+        assert (d / "RAJAPerf-timing-Average.csv").exists()
+    rows = list(csv.reader(open(tmp_path / "sum.csv")))[1:]
+    kernels = {(int(s), k) for s, _, k, _, _ in rows}
+    assert kernels == {(s, k) for s in (4096, 16384) for k in ("Stream_TRIAD", "Lcals_FIRST_DIFF")}
+    assert all(float(v) > 0 for *_, v in rows)
