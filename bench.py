@@ -293,9 +293,10 @@ def _bandwidth_cases():
             self.div = self.zeros(nn)
             self.bytes_per_rep = 8 * self.nz + 4 * 8 * n_real_nodes + 8 * self.nz
             self.flops_per_rep = 54 * self.nz
-            # 33 per zone (30 DADD, 3 DFMA): halves, divisions, standalone
-            # products and + ptiny off the FP64 pipe
-            self.fp64_instr_per_rep = 33 * self.nz
+            # 27 per zone: of the 30 adds and 3 FMAs, the first add of six
+            # corner sums runs on the integer pipes, as do the halves,
+            # divisions, standalone products and + ptiny
+            self.fp64_instr_per_rep = 27 * self.nz
 
         def run(self, s):
             return self.L.b200_apps_del_dot_vec_2d(
@@ -314,7 +315,9 @@ def _bandwidth_cases():
             self.A, self.B = self.uniform(N * N), self.uniform(N * N)
             self.bytes_per_rep = (8 * (N * N - 4) * 2 + 8 * (N - 2) * (N - 2) * 2) * tsteps
             self.flops_per_rep = tsteps * 10 * (N - 2) * (N - 2)
-            self.fp64_instr_per_rep = tsteps * 8 * (N - 2) * (N - 2)  # 4 adds per point per half-step
+            # per point and half-step: three of the four adds on the FP64 pipe
+            # (the first add and the product by 0.2 run on the integer pipes)
+            self.fp64_instr_per_rep = tsteps * 6 * (N - 2) * (N - 2)
 
         def run(self, s):
             return self.L.b200_polybench_jacobi_2d(self.A.data_ptr(), self.B.data_ptr(), self.N,

@@ -121,8 +121,10 @@ int b200_probe_dfma(double* out, int32_t iters, int64_t* fma_count,
  * integer test; signed zeros, infinities and NaNs added), 8 = a * b on the
  * integer pipe (JACOBI_2D's a * 0.2 for every other pair), 9 = a + b for a b
  * below a's last bit (DEL_DOT_VEC_2D's + ptiny; exponent gaps 50-60 around
- * the fast path's bound of 55, powers of two, special values added); adds to
- * *mismatches (device) the number of
+ * the fast path's bound of 55, powers of two, special values added), 10 =
+ * a + b with close exponents (JACOBI_2D's integer-pipe adds: exponents 0-4
+ * apart, mostly one sign, the top of the exponent range, zeros, subnormals
+ * and non-finite values added); adds to *mismatches (device) the number of
  * results whose bits differ from the FP64 pipe's.  Not in the reference. */
 int b200_f64emu_selftest(int64_t n, uint64_t seed, int32_t op,
                          unsigned long long* mismatches, b200_stream_t stream);
@@ -304,7 +306,12 @@ int b200_apps_vol3d(const double* x, const double* y, const double* z,
                     b200_stream_t stream);
 
 /* Nodal divergence for each real zone i = real_zones[ii], corners i, i+1,
- * i+1+jp, i+jp  -- apps/DEL_DOT_VEC_2D.hpp:65-90, DEL_DOT_VEC_2D-Cuda.cpp:30-60 */
+ * i+1+jp, i+jp  -- apps/DEL_DOT_VEC_2D.hpp:65-90, DEL_DOT_VEC_2D-Cuda.cpp:30-60
+ * With half = 0.5 the halvings are exponent moves, the divisions and five
+ * products integer-pipe arithmetic and the first add of six of the eight
+ * corner sums integer-pipe adds, all bit-identical to the FP64 pipe;
+ * tune->tile_z = 1 + corner sums opened on the integer pipes (0, 2, 4, 6 or 8;
+ * default 6). */
 int b200_apps_del_dot_vec_2d(const double* x, const double* y,
                              const double* xdot, const double* ydot,
                              double* div, const int64_t* real_zones,
@@ -317,8 +324,12 @@ int b200_apps_del_dot_vec_2d(const double* x, const double* y,
 /* tsteps x (B <- 5-point average of A, then A <- of B) on an N x N grid
  *   -- polybench/POLYBENCH_JACOBI_2D.hpp:38-44, -Cuda.cpp:86-114
  * Default: column segments of tune->items rows per thread (2, 4 or 8;
- * default 2), the product by 0.2 on the integer pipe (bit-identical);
- * tune->items 1: one point per thread.  tune->algo > 0 selects the
+ * default 4), the product by 0.2 and the first of each point's four adds on
+ * the integer pipes (bit-identical: f64emu, exact rounding), the other three
+ * adds on the FP64 pipe; tune->tile_z = 1 + integer-pipe adds per four
+ * points (0, 4, 8, 9, 10 or 12; default 4), tune->tile_y 2 puts the product
+ * on the FP64 pipe; tune->items 1: one point per
+ * thread.  tune->algo > 0 selects the
  * mixed-pipe kernel: algo-1 of every 8 warps run bit-identical integer-pipe
  * FP64 (rows per warp: tile_y emulated, tile_z native).                     */
 int b200_polybench_jacobi_2d(double* A, double* B, int64_t N, int64_t tsteps,

@@ -190,7 +190,10 @@ struct Vol3D {
 // pipes (f64emu::div_fast, correctly rounded), which leaves the FP64 pipe the
 // adds and multiplies and every result bit unchanged; a warp with a zero,
 // subnormal or non-finite operand recomputes its zones natively.
-template <bool HALF_POW2>
+// KD: of the eight corner sums, the first KD (x, y, then xdot, ydot) take
+// their first add, of two corner values of one sign and similar size, on the
+// integer pipes (f64emu::add_close_fast, bit-identical).
+template <bool HALF_POW2, int KD = 0>
 struct DelDotVec2D {
   const double* __restrict__ x;
   const double* __restrict__ y;
@@ -214,7 +217,10 @@ struct DelDotVec2D {
     auto s4 = [&](double a, double b, double c, double d) {
       return fform::sub(fform::sub(fform::add(a, b, fr), c, fr), d, fr);
     };
-    if (fast) {
+    // the first add of each sum (fy1 + fy2 and y1 + y2 also open the affine
+    // term's sums); with KD = 0 the sums stay as written (fewer registers)
+    double p[8];
+    if (KD == 0 && fast) {
       xi = f64emu::mul_pow2_fast<-1>(s4(x1, x2, x3, x4), slow);
       xj = f64emu::mul_pow2_fast<-1>(s4(x2, x3, x4, x1), slow);
       yi = f64emu::mul_pow2_fast<-1>(s4(y1, y2, y3, y4), slow);
@@ -223,6 +229,26 @@ struct DelDotVec2D {
       fxj = f64emu::mul_pow2_fast<-1>(s4(fx2, fx3, fx4, fx1), slow);
       fyi = f64emu::mul_pow2_fast<-1>(s4(fy1, fy2, fy3, fy4), slow);
       fyj = f64emu::mul_pow2_fast<-1>(s4(fy2, fy3, fy4, fy1), slow);
+      p[2] = fform::add(y1, y2, fr);
+      p[6] = fform::add(fy1, fy2, fr);
+    } else if (fast) {
+      const double pa[8] = {x1, x2, y1, y2, fx1, fx2, fy1, fy2};
+      const double pb[8] = {x2, x3, y2, y3, fx2, fx3, fy2, fy3};
+#pragma unroll
+      for (int m = 0; m < 8; ++m)
+        p[m] = (m < KD) ? f64emu::add_close_fast(pa[m], pb[m], slow)
+                        : fform::add(pa[m], pb[m], fr);
+      auto t2 = [&](double q, double c, double d) {
+        return f64emu::mul_pow2_fast<-1>(fform::sub(fform::sub(q, c, fr), d, fr), slow);
+      };
+      xi = t2(p[0], x3, x4);
+      xj = t2(p[1], x4, x1);
+      yi = t2(p[2], y3, y4);
+      yj = t2(p[3], y4, y1);
+      fxi = t2(p[4], fx3, fx4);
+      fxj = t2(p[5], fx4, fx1);
+      fyi = t2(p[6], fy3, fy4);
+      fyj = t2(p[7], fy4, fy1);
     } else {  // the same sums as the fast path (shared, not recomputed)
       xi = half * s4(x1, x2, x3, x4);
       xj = half * s4(x2, x3, x4, x1);
@@ -246,9 +272,8 @@ struct DelDotVec2D {
           f64emu::mul_fast(rarea, fma(fxi, yj, -f64emu::mul_fast(fxj, yi, slow)), slow);
       const double dfydy =
           f64emu::mul_fast(rarea, fma(fyj, xi, -f64emu::mul_fast(fyi, xj, slow)), slow);
-      const double affine = f64emu::div_fast(
-          fform::add(fform::add(fform::add(fy1, fy2, fr), fy3, fr), fy4, fr),
-          fform::add(fform::add(fform::add(y1, y2, fr), y3, fr), y4, fr), slow);
+      const double affine = f64emu::div_fast(fform::add(fform::add(p[6], fy3, fr), fy4, fr),
+                                             fform::add(fform::add(p[2], y3, fr), y4, fr), slow);
       return fform::add(fform::add(dfxdx, dfydy, fr), affine, fr);
     }
     // the same FMAs as the fast path, so both give the same bits on its inputs
@@ -323,6 +348,12 @@ int b200_apps_vol3d(const double* x, const double* y, const double* z, double* v
                       iend - ibegin, tune, as_stream(stream));
 }
 
+// DEL_DOT_VEC_2D's corner sums opened on the integer pipes by default.
+// Measured on GB300 (the bench's 4096^2 jittered mesh, 256 x 2): none 0.927
+// ms, 2: 0.908, 4: 0.892, 6: 0.829, all 8: 1.068 (the integer pipes, which
+// also carry the two divisions and five products, become the bound).
+constexpr int kDelDotIntAdds = 6;
+
 int b200_apps_del_dot_vec_2d(const double* x, const double* y, const double* xdot,
                              const double* ydot, double* div,
                              const int64_t* real_zones, int64_t n_real_zones,
@@ -331,11 +362,35 @@ int b200_apps_del_dot_vec_2d(const double* x, const double* y, const double* xdo
   if (n_real_zones < 0 || jp < 0 ||
       (n_real_zones > 0 && (!x || !y || !xdot || !ydot || !div || !real_zones)))
     return invalid("b200_apps_del_dot_vec_2d: bad args");
-  // two zones per thread by default: 1.3% faster than four at 4096^2 zones
-  if (half == 0.5)
-    return launch_map1d("b200_apps_del_dot_vec_2d",
-                        DelDotVec2D<true>{x, y, xdot, ydot, div, real_zones, jp, ptiny, half, 0},
-                        n_real_zones, tune, as_stream(stream), 256, 2);
+  // two zones per thread by default: 1.3% faster than four at 4096^2 zones;
+  // tune->tile_z = 1 + corner sums opened on the integer pipes (0, 2, 4, 6
+  // or 8; 2, 4 and 8 with 256 threads x 2 zones)
+  if (half == 0.5) {
+    const int kd = (tune && tune->tile_z) ? tune->tile_z - 1 : kDelDotIntAdds;
+    // the variants with integer-pipe adds run the default shape (256 x 2)
+    auto go = [&](auto f) -> int {
+      if (n_real_zones <= 0) return B200_OK;
+      const Shape sh = resolve_1d(nullptr, n_real_zones, 256, 2, 1);
+      map_kernel<256, 2, decltype(f)><<<sh.grid, 256, 0, as_stream(stream)>>>(f, n_real_zones);
+      return after_launch("b200_apps_del_dot_vec_2d");
+    };
+    switch (kd) {
+      case 0:
+        return launch_map1d("b200_apps_del_dot_vec_2d",
+                            DelDotVec2D<true, 0>{x, y, xdot, ydot, div, real_zones, jp, ptiny,
+                                                 half, 0},
+                            n_real_zones, tune, as_stream(stream), 256, 2);
+      case 2: return go(DelDotVec2D<true, 2>{x, y, xdot, ydot, div, real_zones, jp, ptiny, half, 0});
+      case 4: return go(DelDotVec2D<true, 4>{x, y, xdot, ydot, div, real_zones, jp, ptiny, half, 0});
+      case 6:
+        return launch_map1d("b200_apps_del_dot_vec_2d",
+                            DelDotVec2D<true, 6>{x, y, xdot, ydot, div, real_zones, jp, ptiny,
+                                                 half, 0},
+                            n_real_zones, tune, as_stream(stream), 256, 2);
+      case 8: return go(DelDotVec2D<true, 8>{x, y, xdot, ydot, div, real_zones, jp, ptiny, half, 0});
+      default: return invalid("b200_apps_del_dot_vec_2d: tile_z %d (1, 3, 5, 7 or 9)", kd + 1);
+    }
+  }
   return launch_map1d("b200_apps_del_dot_vec_2d",
                       DelDotVec2D<false>{x, y, xdot, ydot, div, real_zones, jp, ptiny, half, 0},
                       n_real_zones, tune, as_stream(stream));

@@ -448,6 +448,18 @@ __global__ void f64emu_check_kernel(int64_t n, uint64_t seed, int op,
         default: break;
       }
     }
+    if (op == 10) {  // close exponents (0-4 apart), either sign, near the top of the range
+      const uint64_t e = ((i % 5) == 3) ? 2040u + (ra >> 58) % 7u : ((ra >> 12) % 2000u) + 20u;
+      A = (ra & 0x800FFFFFFFFFFFFFULL) | (e << 52);
+      B = (rb & 0x000FFFFFFFFFFFFFULL) | ((e - (rb >> 60) % 5u) << 52) |
+          (((rb >> 59) & 7u) ? (A & 0x8000000000000000ULL) : (~A & 0x8000000000000000ULL));
+      if ((i % 7) == 6) {  // zeros, subnormals, infinities, NaNs: the slow path
+        const uint64_t sp[6] = {0x0ULL, 0x8000000000000000ULL, 0x7FF0000000000000ULL,
+                                0x0000000000000001ULL, 0x7FF8000000000001ULL,
+                                0x000FFFFFFFFFFFFFULL};
+        A = sp[(ra >> 60) % 6u] | (A & 0x8000000000000000ULL);
+      }
+    }
     if (op == 9 && (i % 5) != 0 && (i % 5) != 3) {  // a + tiny b: gaps 50-60 around 55
       const uint64_t e = ((ra >> 12) % 1900u) + 70u;
       const uint64_t gap = 50u + (rb >> 58) % 11u;
@@ -485,6 +497,11 @@ __global__ void f64emu_check_kernel(int64_t n, uint64_t seed, int op,
     } else if (op == 7) {  // x < 0 as INDEXLIST tests it
       want = a < 0.0 ? 1.0 : 0.0;
       got = b200::f64emu::lt_zero(a) ? 1.0 : 0.0;
+    } else if (op == 10) {  // a + b, close exponents, as JACOBI_2D's integer-pipe adds
+      want = __dadd_rn(a, b);
+      bool slow = false;
+      got = b200::f64emu::add_close_fast(a, b, slow);
+      if (slow) got = __dadd_rn(a, b);
     } else if (op == 9) {  // a + b for b below a's last bit, as DEL_DOT_VEC_2D's + ptiny
       want = __dadd_rn(a, b);
       bool slow = false;
@@ -508,7 +525,7 @@ __global__ void f64emu_check_kernel(int64_t n, uint64_t seed, int op,
 
 extern "C" int b200_f64emu_selftest(int64_t n, uint64_t seed, int32_t op,
                                     unsigned long long* mismatches, b200_stream_t stream) {
-  if (n < 0 || !mismatches || op < 0 || op > 9) return invalid("b200_f64emu_selftest: bad args");
+  if (n < 0 || !mismatches || op < 0 || op > 10) return invalid("b200_f64emu_selftest: bad args");
   const int blocks = device_info().sm_count * 8;
   f64emu_check_kernel<<<blocks, 256, 0, as_stream(stream)>>>(n, seed, op, mismatches);
   return after_launch("b200_f64emu_selftest");

@@ -14,6 +14,8 @@
 #include "b200_fma_form.cuh"
 #include "b200_internal.cuh"
 
+#include <type_traits>
+
 using namespace b200;
 
 namespace {
@@ -59,8 +61,16 @@ jacobi2d_step(const double* __restrict__ src, double* __restrict__ dst, int64_t 
 // per thread with the FP64 multiply: 165 us; with the integer multiply: 158).
 // The four adds are register-operand FMAs (fform::add, bit-identical), which
 // the FP64 pipe issues at its full rate where DADD gets 5/6 of it: 133 ->
-// 115 us.  `zero` is 0 at run time.
-template <int BX, int R>
+// 115 us.  With 4 rows per thread and the first add of each point on the
+// integer pipes (KQ = 4 below): 92 us.  `zero` is 0 at run time.
+// KQ adds in every four consecutive points (the first ones of each point, in
+// the suite's order; row r of a group of four takes (KQ(r+1))/4 - (KQ r)/4)
+// run on the integer pipes (f64emu::add_close_fast, bit-identical; its
+// operands here are sums of one sign and similar size), the rest on the FP64
+// pipe, and the product by 0.2 on the integer pipe (MULINT) or the FP64 pipe
+// (an FMA with -0, bit-identical to the product): the two pipes then share
+// the point's work instead of the FP64 pipe carrying all of it.
+template <int BX, int R, int KQ = 0, bool MULINT = true>
 __global__ void __launch_bounds__(BX)
 jacobi2d_rows(const double* __restrict__ src, double* __restrict__ dst, int64_t N, int zero) {
   const int64_t j = 1 + static_cast<int64_t>(blockIdx.x) * BX + threadIdx.x;
@@ -80,11 +90,17 @@ jacobi2d_rows(const double* __restrict__ src, double* __restrict__ dst, int64_t 
       rgt[r] = ld(p + (r + 1) * N + 1);
     }
     const fform::Regs fr = fform::regs(zero);
+    const double fifth = fform::reg(0.2, zero);  // a per-thread register
 #pragma unroll
-    for (int r = 0; r < R; ++r)
-      q[r * N] = f64emu::mul_fast(
-          fform::add(fform::add(fform::add(fform::add(col[r + 1], lft[r], fr), rgt[r], fr),
-                                col[r + 2], fr), col[r], fr), 0.2, slow);
+    for (int r = 0; r < R; ++r) {
+      const int ki = (KQ * (r % 4 + 1)) / 4 - (KQ * (r % 4)) / 4;
+      auto add = [&](int k, double a, double b) {
+        return (k < ki) ? f64emu::add_close_fast(a, b, slow) : fform::add(a, b, fr);
+      };
+      const double sum =
+          add(3, add(2, add(1, add(0, col[r + 1], lft[r]), rgt[r]), col[r + 2]), col[r]);
+      q[r * N] = MULINT ? f64emu::mul_fast(sum, 0.2, slow) : fform::mul(sum, fifth, fr);
+    }
   } else {
     for (int64_t r = 0; r < rows; ++r) {
       const double* c = p + (r + 1) * N;
@@ -607,6 +623,16 @@ dim3 grid2(int64_t nxthreads, int64_t nrows, int bx, int by) {
 
 extern "C" {
 
+// JACOBI_2D's split between the pipes by default: integer-pipe adds per
+// four points and where the product by 0.2 runs.  Measured on GB300 (4 rows
+// per thread, us per half-step at 4096^2): FP64 adds only 114.7; one add per
+// point on the integer pipe 92.3; two 125.1; with the product on the FP64
+// pipe, two adds per point 94.2, one 114.8.  One integer-pipe add costs
+// about 33 us of the integer pipes' time per half-step here (some 40
+// instructions), the integer product about 59.
+constexpr int kJacobiIntAdds4 = 4;
+constexpr bool kJacobiMulInt = true;
+
 int b200_polybench_jacobi_2d(double* A, double* B, int64_t N, int64_t tsteps,
                              const b200_tune* tune, b200_stream_t stream) {
   if (!A || !B || N < 0 || tsteps < 0) return invalid("b200_polybench_jacobi_2d: bad args");
@@ -624,9 +650,9 @@ int b200_polybench_jacobi_2d(double* A, double* B, int64_t N, int64_t tsteps,
     }
     return after_launch("b200_polybench_jacobi_2d", static_cast<int>(2 * tsteps));
   }
-  // default: column segments of 2 rows per thread (tune->items 2, 4 or 8);
+  // default: column segments of 4 rows per thread (tune->items 2, 4 or 8);
   // tune->items 1: one point per thread with rows strided over the grid
-  const int rows = (tune && tune->items) ? tune->items : 2;
+  const int rows = (tune && tune->items) ? tune->items : 4;
   if (rows != 1 && rows != 2 && rows != 4 && rows != 8)
     return invalid("b200_polybench_jacobi_2d: items %d (1, 2, 4 or 8)", rows);
   if (rows != 1) {
@@ -640,9 +666,35 @@ int b200_polybench_jacobi_2d(double* A, double* B, int64_t N, int64_t tsteps,
         kernel<<<g, BX, 0, st>>>(B, A, N, 0);
       }
     };
-    if (rows == 2) run(jacobi2d_rows<BX, 2>);
-    else if (rows == 4) run(jacobi2d_rows<BX, 4>);
-    else run(jacobi2d_rows<BX, 8>);
+    // tune->tile_z = 1 + integer-pipe adds per four points (0, 4, 8, 9, 10,
+    // 12); tune->tile_y 2: the product by 0.2 on the FP64 pipe
+    const int kq = (tune && tune->tile_z) ? tune->tile_z - 1 : kJacobiIntAdds4;
+    const bool mulint = (tune && tune->tile_y) ? tune->tile_y != 2 : kJacobiMulInt;
+    auto pick = [&](auto r_tag) -> int {
+      constexpr int R = decltype(r_tag)::value;
+      switch (kq * 2 + (mulint ? 1 : 0)) {
+        case 1: run(jacobi2d_rows<BX, R, 0, true>); break;
+        case 0: run(jacobi2d_rows<BX, R, 0, false>); break;
+        case 9: run(jacobi2d_rows<BX, R, 4, true>); break;
+        case 8: run(jacobi2d_rows<BX, R, 4, false>); break;
+        case 17: run(jacobi2d_rows<BX, R, 8, true>); break;
+        case 16: run(jacobi2d_rows<BX, R, 8, false>); break;
+        case 19: run(jacobi2d_rows<BX, R, 9, true>); break;
+        case 18: run(jacobi2d_rows<BX, R, 9, false>); break;
+        case 21: run(jacobi2d_rows<BX, R, 10, true>); break;
+        case 20: run(jacobi2d_rows<BX, R, 10, false>); break;
+        case 25: run(jacobi2d_rows<BX, R, 12, true>); break;
+        case 24: run(jacobi2d_rows<BX, R, 12, false>); break;
+        default:
+          return invalid("b200_polybench_jacobi_2d: tile_z %d (1, 5, 9, 10, 11 or 13)", kq + 1);
+      }
+      return B200_OK;
+    };
+    int rc;
+    if (rows == 2) rc = pick(std::integral_constant<int, 2>{});
+    else if (rows == 4) rc = pick(std::integral_constant<int, 4>{});
+    else rc = pick(std::integral_constant<int, 8>{});
+    if (rc != B200_OK) return rc;
     return after_launch("b200_polybench_jacobi_2d", static_cast<int>(2 * tsteps));
   }
   constexpr int BX = 64, BY = 4;

@@ -70,6 +70,36 @@ def test_del_dot_vec_2d_irregular_zones():
     close(gu.host(dd), div)
 
 
+@pytest.mark.parametrize("int_adds", [2, 4, 6, 8])
+def test_del_dot_vec_2d_integer_pipe_adds_bit_identical(int_adds):
+    """Corner sums opened on the integer pipes (tile_z = 1 + count): the same
+    bits as the FP64-pipe form on a mesh of positive coordinates and fields
+    (the fast path) and on signed fields with zeros (the fallback)."""
+    rng = np.random.default_rng(17 + int_adds)
+    jp, rows = 301, 120
+    nn = jp * rows
+    ii, jj = np.meshgrid(np.arange(jp), np.arange(rows))
+    for signed in (False, True):
+        x = (ii.ravel() * 0.2 + rng.uniform(-0.02, 0.02, nn))
+        y = (jj.ravel() * 0.1 + rng.uniform(-0.01, 0.01, nn))
+        lo = -1.5 if signed else 0.5
+        xd, yd = rng.uniform(lo, 1.5, nn), rng.uniform(lo, 1.5, nn)
+        if signed:
+            xd[rng.integers(0, nn, 30)] = 0.0
+        zones = np.arange(0, nn - jp - 1, dtype=np.int64)
+        zones = zones[(zones % jp) != jp - 1]
+        out = []
+        for tz in (1, 1 + int_adds):
+            div = np.zeros(nn)
+            dd, dx, dy, dxd, dyd, dz = dev(div), dev(x), dev(y), dev(xd), dev(yd), dev(zones)
+            rp.check(lib().b200_apps_del_dot_vec_2d(
+                dx.data_ptr(), dy.data_ptr(), dxd.data_ptr(), dyd.data_ptr(), dd.data_ptr(),
+                dz.data_ptr(), zones.size, jp, 1e-20, 0.5, ctypes.byref(rp.Tune(tile_z=tz)),
+                gu.stream()))
+            out.append(gu.host(dd))
+        assert np.array_equal(out[0], out[1])
+
+
 def test_vol3d_random_mesh():
     rng = np.random.default_rng(4)
     jp, kp = 11, 11 * 13
@@ -399,19 +429,43 @@ def test_null_pointer_rejected(fn, args):
     assert f(*argv) == rp.B200_ERR_INVALID_ARG
 
 
-@pytest.mark.parametrize("op", [0, 1, 2, 3, 4, 5, 6, 7, 8, 9])
+@pytest.mark.parametrize("op", [0, 1, 2, 3, 4, 5, 6, 7, 8, 9, 10])
 def test_integer_pipe_fp64_is_bit_exact(op):
     """The integer-pipe add/sub/mul used by the mixed-pipe stencils, the
     exponent-shift products by 0.5, 0.125 and 2 of DEL_DOT_VEC_2D and HEAT_3D,
     the FP64-free division of HYDRO_2D and DEL_DOT_VEC_2D, INDEXLIST's integer
     x < 0 test, the integer-pipe multiply of JACOBI_2D, HYDRO_2D and
-    DEL_DOT_VEC_2D and DEL_DOT_VEC_2D's + ptiny, against the FP64 pipe on 16M
-    operands (every class of double; 64M for the division)."""
+    DEL_DOT_VEC_2D, DEL_DOT_VEC_2D's + ptiny and JACOBI_2D's close-exponent
+    integer add, against the FP64 pipe on 16M operands (every class of
+    double; 64M for the division)."""
     torch = gu.torch_cuda()
     bad = torch.zeros(1, dtype=torch.int64, device="cuda")
     n = (1 << 26) if op == 6 else (1 << 24)
     rp.check(lib().b200_f64emu_selftest(n, 12345 + op, op, bad.data_ptr(), gu.stream()))
     assert int(gu.host(bad)[0]) == 0
+
+
+@pytest.mark.parametrize("N,ts", [(3, 1), (37, 2), (300, 3), (1031, 2)])
+@pytest.mark.parametrize("int_adds", [0, 4, 8, 9, 10, 12])
+@pytest.mark.parametrize("mul_fp64", [False, True])
+@pytest.mark.parametrize("rows", [2, 4])
+def test_jacobi_integer_pipe_adds_bit_identical(N, ts, int_adds, mul_fp64, rows):
+    """Integer-pipe adds per four points (tile_z = 1 + count) and the product
+    by 0.2 on either pipe (tile_y 2: FP64): bit-identical to the suite's loop
+    in the oracle, on data of one sign (the fast path) and on signed data
+    with zeros (the native fallback)."""
+    rng = np.random.default_rng(N + 11 * int_adds + rows + 3 * mul_fp64)
+    for signed in (False, True):
+        lo = -1.5 if signed else 0.5
+        A, B = rng.uniform(lo, 1.5, N * N), rng.uniform(lo, 1.5, N * N)
+        if signed:
+            A[rng.integers(0, N * N, 20)] = 0.0
+        dA, dB = dev(A), dev(B)
+        t = rp.Tune(items=rows, tile_z=1 + int_adds, tile_y=2 if mul_fp64 else 1)
+        rp.check(lib().b200_polybench_jacobi_2d(dA.data_ptr(), dB.data_ptr(), N, ts,
+                                                ctypes.byref(t), gu.stream()))
+        oracle.call("oracle_jacobi_2d", A, B, N, ts)
+        assert np.array_equal(gu.host(dA), A) and np.array_equal(gu.host(dB), B)
 
 
 @pytest.mark.parametrize("N,ts", [(3, 1), (37, 2), (300, 3)])
