@@ -335,7 +335,9 @@ def _bandwidth_cases():
             inner = (N - 2) ** 3
             self.bytes_per_rep = (8 * (N ** 3 - 12 * (N - 2) - 8) * 2 + 8 * inner * 2) * tsteps
             self.flops_per_rep = tsteps * 30 * inner
-            self.fp64_instr_per_rep = tsteps * 18 * inner  # 9 adds per point per half-step
+            # per point and half-step: 9 adds, 2.5 of them (5 of the 6
+            # differences b(+1) - 2a of two planes) on the integer pipes
+            self.fp64_instr_per_rep = tsteps * 13 * inner
 
         def run(self, s):
             return self.L.b200_polybench_heat_3d(self.A.data_ptr(), self.B.data_ptr(), self.N,

@@ -124,7 +124,10 @@ int b200_probe_dfma(double* out, int32_t iters, int64_t* fma_count,
  * the fast path's bound of 55, powers of two, special values added), 10 =
  * a + b with close exponents (JACOBI_2D's integer-pipe adds: exponents 0-4
  * apart, mostly one sign, the top of the exponent range, zeros, subnormals
- * and non-finite values added); adds to *mismatches (device) the number of
+ * and non-finite values added), 11 = a + b of either sign with close
+ * exponents (HEAT_3D's integer-pipe b(+1) - 2a: exponents 0-4 apart, b near
+ * -a with differences of 0 to 53 bits, results below the normal range, the
+ * top of the range, special values added); adds to *mismatches (device) the number of
  * results whose bits differ from the FP64 pipe's.  Not in the reference. */
 int b200_f64emu_selftest(int64_t n, uint64_t seed, int32_t op,
                          unsigned long long* mismatches, b200_stream_t stream);
@@ -337,8 +340,13 @@ int b200_polybench_jacobi_2d(double* A, double* B, int64_t N, int64_t tsteps,
 
 /* tsteps x (B <- 7-point heat update of A, then A <- of B) on N^3
  *   -- polybench/POLYBENCH_HEAT_3D.hpp:47-82, -Cuda.cpp:97-113
- * tune->algo > 0 selects the mixed-pipe kernel as for JACOBI_2D (tile_x =
- * planes per CTA).                                                          */
+ * Default: each thread walks tune->tile_x consecutive planes (2 or 4;
+ * default 4) with the plane neighbours in registers; 2.0 * a and the three
+ * 0.125 * (...) are exponent moves, and tune->tile_z - 1 of the six
+ * differences b(+1) - 2a of every two planes (0..6; default 5) run on the
+ * integer pipes (f64emu::sub_near_fast: exact rounding, bit-identical); the
+ * remaining adds are FP64 FMAs.  tune->algo > 0 selects the mixed-pipe
+ * kernel as for JACOBI_2D (tile_x = planes per CTA).                        */
 int b200_polybench_heat_3d(double* A, double* B, int64_t N, int64_t tsteps,
                            const b200_tune* tune, b200_stream_t stream);
 

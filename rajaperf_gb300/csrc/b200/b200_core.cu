@@ -460,6 +460,27 @@ __global__ void f64emu_check_kernel(int64_t n, uint64_t seed, int op,
         A = sp[(ra >> 60) % 6u] | (A & 0x8000000000000000ULL);
       }
     }
+    if (op == 11) {  // either sign, exponents 0-4 apart, cancellations of every depth
+      const uint64_t e = ((i % 5) == 3)   ? 2040u + (ra >> 58) % 7u
+                         : ((i % 5) == 4) ? 1u + (ra >> 12) % 60u  // results below the normal range
+                                          : ((ra >> 12) % 2000u) + 20u;
+      A = (ra & 0x800FFFFFFFFFFFFFULL) | (e << 52);
+      const uint64_t r = (rb >> 60) % 5u;
+      B = (rb & 0x000FFFFFFFFFFFFFULL) | ((e > r ? e - r : 0u) << 52) |
+          (((rb >> 59) & 1u) ? (A & 0x8000000000000000ULL) : (~A & 0x8000000000000000ULL));
+      if ((i % 3) == 1) {  // b = -(a +- delta): delta of 0 to 53 bits, exact zero included
+        const uint64_t mag = A & ~0x8000000000000000ULL;
+        const uint64_t delta = (rb >> 2) & ((1ULL << ((rb >> 56) % 54u)) - 1u);
+        const uint64_t bm = (((rb >> 1) & 1u) || delta > mag) ? mag + delta : mag - delta;
+        B = bm | (~A & 0x8000000000000000ULL);
+      }
+      if ((i % 7) == 6) {  // zeros, subnormals, infinities, NaNs: the slow path
+        const uint64_t sp[6] = {0x0ULL, 0x8000000000000000ULL, 0x7FF0000000000000ULL,
+                                0x0000000000000001ULL, 0x7FF8000000000001ULL,
+                                0x000FFFFFFFFFFFFFULL};
+        A = sp[(ra >> 60) % 6u] | (A & 0x8000000000000000ULL);
+      }
+    }
     if (op == 9 && (i % 5) != 0 && (i % 5) != 3) {  // a + tiny b: gaps 50-60 around 55
       const uint64_t e = ((ra >> 12) % 1900u) + 70u;
       const uint64_t gap = 50u + (rb >> 58) % 11u;
@@ -502,6 +523,11 @@ __global__ void f64emu_check_kernel(int64_t n, uint64_t seed, int op,
       bool slow = false;
       got = b200::f64emu::add_close_fast(a, b, slow);
       if (slow) got = __dadd_rn(a, b);
+    } else if (op == 11) {  // a + b, either sign, close exponents, as HEAT_3D's b(+1) - 2a
+      want = __dadd_rn(a, b);
+      bool slow = false;
+      got = b200::f64emu::add_near_fast(a, b, slow);
+      if (slow) got = __dadd_rn(a, b);
     } else if (op == 9) {  // a + b for b below a's last bit, as DEL_DOT_VEC_2D's + ptiny
       want = __dadd_rn(a, b);
       bool slow = false;
@@ -525,7 +551,7 @@ __global__ void f64emu_check_kernel(int64_t n, uint64_t seed, int op,
 
 extern "C" int b200_f64emu_selftest(int64_t n, uint64_t seed, int32_t op,
                                     unsigned long long* mismatches, b200_stream_t stream) {
-  if (n < 0 || !mismatches || op < 0 || op > 10) return invalid("b200_f64emu_selftest: bad args");
+  if (n < 0 || !mismatches || op < 0 || op > 11) return invalid("b200_f64emu_selftest: bad args");
   const int blocks = device_info().sm_count * 8;
   f64emu_check_kernel<<<blocks, 256, 0, as_stream(stream)>>>(n, seed, op, mismatches);
   return after_launch("b200_f64emu_selftest");

@@ -34,6 +34,14 @@ __device__ __forceinline__ uint64_t bits(double x) {
 __device__ __forceinline__ double from_bits(uint64_t u) {
   return __longlong_as_double(static_cast<long long>(u));
 }
+// The bits of x through a move the compiler cannot see into: integer masks
+// on them (|x| as x & ~sign, -x as x ^ sign) stay integer instructions
+// instead of being recognised as fabs / fneg and issued on the FP64 pipe.
+__device__ __forceinline__ uint64_t bits_opaque(double x) {
+  uint64_t u;
+  asm("mov.b64 %0, %1;" : "=l"(u) : "d"(x));
+  return u;
+}
 
 // a + b, correctly rounded (RN-even), integer pipe on the fast path.
 __device__ __forceinline__ double add(double a, double b) {
@@ -148,6 +156,57 @@ __device__ __forceinline__ double add_close_fast(double a, double b, bool& slow)
   const uint32_t half = 4u << c;
   const uint64_t up = (rem > half || (rem == half && (mant & 1u))) ? 1u : 0u;
   return from_bits((X & kSign) | ((static_cast<uint64_t>(emax + c - 1u) << 52) + mant + up));
+}
+
+// a + b (bit patterns A and B) for normal operands of either sign with biased
+// exponents at most 3 apart and below 2046.  The operand of larger magnitude
+// is X; aligned to its exponent with 3 guard bits both significands are
+// exact, so S = |X| +- |Y| (never negative) is the exact result's magnitude
+// in units of 2^(ex - 1078).  A difference may cancel any number of leading
+// bits: S is shifted up until its leading one is bit 63 (a leading-zero
+// count), which keeps every bit, and the 11 bits below the 53 kept ones
+// decide round to nearest even (at most 4 of them can be set).  An exact
+// zero is +0 (round to nearest).  `slow` is set when an operand is zero,
+// subnormal, infinite or NaN, the exponents are further apart, or the result
+// falls below the normal range; the caller then adds natively.  About 50
+// integer instructions against one FP64 add (HEAT_3D's b(+1) - 2a, whose
+// operands are within a binade or two of each other).  SUB gives a - b: b's
+// sign is flipped in the sign logic.  The callers pass bits_opaque() bits, so
+// the masks below stay on the integer pipes.
+template <bool SUB>
+__device__ __forceinline__ double add_near_bits(uint64_t A, uint64_t B, bool& slow) {
+  const uint64_t ma = A & ~kSign, mb = B & ~kSign;
+  const bool a_big = ma >= mb;
+  const uint64_t X = a_big ? ma : mb, Y = a_big ? mb : ma;
+  const uint32_t ex = static_cast<uint32_t>(X >> 52), ey = static_cast<uint32_t>(Y >> 52);
+  const uint32_t d = ex - ey;
+  if (ey == 0u || ex > 2045u || d > 3u) {
+    slow = true;
+    return 0.0;
+  }
+  const uint64_t mx = ((X & kFrac) | kHidden) << 3;
+  const uint64_t my = ((Y & kFrac) | kHidden) << (3u - d);
+  const bool opp = (((A ^ B) >> 63) != 0u) != SUB;
+  const uint64_t S = opp ? mx - my : mx + my;            // < 2^57, exact
+  if (S == 0u) return 0.0;
+  const uint32_t lz = static_cast<uint32_t>(__clzll(static_cast<long long>(S)));  // 7..63
+  const int e = static_cast<int>(ex) + 8 - static_cast<int>(lz);  // the result's biased exponent
+  if (e <= 0) {
+    slow = true;
+    return 0.0;
+  }
+  const uint64_t V = S << lz;                             // leading one at bit 63
+  const uint64_t mant = V >> 11;                          // 53 bits with the hidden one
+  const uint32_t rem = static_cast<uint32_t>(V) & 0x7ffu;
+  const uint64_t up = (rem > 0x400u || (rem == 0x400u && (mant & 1u))) ? 1u : 0u;
+  const uint64_t sign = a_big ? (A & kSign) : (SUB ? (~B & kSign) : (B & kSign));
+  return from_bits(sign | ((static_cast<uint64_t>(e - 1) << 52) + mant + up));
+}
+__device__ __forceinline__ double add_near_fast(double a, double b, bool& slow) {
+  return add_near_bits<false>(bits_opaque(a), bits_opaque(b), slow);
+}
+__device__ __forceinline__ double sub_near_fast(double a, double b, bool& slow) {
+  return add_near_bits<true>(bits_opaque(a), bits_opaque(b), slow);
 }
 
 // x * 2^k for a small |k|: exact exponent arithmetic; native when the result

@@ -116,41 +116,62 @@ jacobi2d_rows(const double* __restrict__ src, double* __restrict__ dst, int64_t 
 }
 
 // ---- HEAT_3D: polybench/POLYBENCH_HEAT_3D.hpp:47-82 -------------------------
-// Index k + N*(j + N*i); threads run along k (contiguous).
-template <int BX, int BY>
+// Index k + N*(j + N*i); threads run along k (contiguous), and each thread
+// walks PL consecutive planes i, keeping b(i-1), a and b(i+1) in registers
+// (five loads a point instead of seven, one index step).  KS2 of the six
+// differences b(+1) - 2a of two consecutive planes (directions i, j, k in that
+// order; an odd KS2 gives the second plane the larger share) run on the
+// integer pipes (f64emu::sub_near_fast, bit-identical); the rest stay on the
+// FP64 pipe.
+template <int BX, int BY, int PL, int KS2>
 __global__ void __launch_bounds__(BX * BY)
 heat3d_step(const double* __restrict__ S, double* __restrict__ D, int64_t N, int zero) {
+  static_assert(PL % 2 == 0 && KS2 >= 0 && KS2 <= 6, "planes in pairs, 0..6 integer differences");
   const int64_t k = 1 + static_cast<int64_t>(blockIdx.x) * BX + threadIdx.x;
   const int64_t j = 1 + static_cast<int64_t>(blockIdx.y) * BY + threadIdx.y;
   if (k >= N - 1 || j >= N - 1) return;
+  const unsigned live = __activemask();
   const int64_t NN = N * N;
+  const int64_t i0 = 1 + static_cast<int64_t>(blockIdx.z) * PL;
+  const int np = static_cast<int>((N - 1 - i0) < PL ? (N - 1 - i0) : PL);
   // 2.0 * a and 0.125 * v are exact: exponent moves on the integer pipe, so
-  // the FP64 pipe keeps only the 9 adds of a point, issued as register-operand
-  // FMAs (fform, bit-identical; full rate where DADD gets 5/6 of it).  A
-  // thread that met a zero, subnormal or non-finite value rewrites its points
+  // the FP64 pipe keeps at most the 9 adds of a point, issued as
+  // register-operand FMAs (fform, bit-identical; full rate where DADD gets 5/6
+  // of it).  A thread that met a zero, subnormal or non-finite value (or
+  // differences too far apart for the integer-pipe form) rewrites its points
   // with the FP64 products after the loop (the same results, bit for bit).
   // `zero` is 0 at run time.
   const fform::Regs fr = fform::regs(zero);
   bool slow = false;
-  for (int64_t i = 1 + blockIdx.z; i < N - 1; i += gridDim.z) {
-    const int64_t c = k + N * (j + N * i);
-    const double a = ld(S + c);
+  const double* p = S + k + N * (j + N * i0);
+  double* q = D + k + N * (j + N * i0);
+  double im = ld(p - NN), a = ld(p);
+#pragma unroll
+  for (int r = 0; r < PL; ++r) {
+    if (r >= np) break;
+    const int ks = (KS2 * (r % 2 + 1)) / 2 - (KS2 * (r % 2)) / 2;  // this plane's share
+    const double ip = ld(p + NN);
     const double a2 = f64emu::mul_pow2_fast<1>(a, slow);
-    const double ti = f64emu::mul_pow2_fast<-3>(
-        fform::add(fform::sub(ld(S + c + NN), a2, fr), ld(S + c - NN), fr), slow);
-    const double tj = f64emu::mul_pow2_fast<-3>(
-        fform::add(fform::sub(ld(S + c + N), a2, fr), ld(S + c - N), fr), slow);
-    const double tk = f64emu::mul_pow2_fast<-3>(
-        fform::add(fform::sub(ld(S + c + 1), a2, fr), ld(S + c - 1), fr), slow);
-    D[c] = fform::add(fform::add(fform::add(ti, tj, fr), tk, fr), a, fr);
+    auto dir = [&](int m, double hi, double lo) {
+      const double d = (m < ks) ? f64emu::sub_near_fast(hi, a2, slow) : fform::sub(hi, a2, fr);
+      return f64emu::mul_pow2_fast<-3>(fform::add(d, lo, fr), slow);
+    };
+    const double ti = dir(0, ip, im);
+    const double tj = dir(1, ld(p + N), ld(p - N));
+    const double tk = dir(2, ld(p + 1), ld(p - 1));
+    *q = fform::add(fform::add(fform::add(ti, tj, fr), tk, fr), a, fr);
+    im = a;
+    a = ip;
+    p += NN;
+    q += NN;
   }
-  if (__any_sync(__activemask(), slow) && slow) {
-    for (int64_t i = 1 + blockIdx.z; i < N - 1; i += gridDim.z) {
-      const int64_t c = k + N * (j + N * i);
-      const double a = ld(S + c);
-      D[c] = 0.125 * (ld(S + c + NN) - 2.0 * a + ld(S + c - NN)) +
-             0.125 * (ld(S + c + N) - 2.0 * a + ld(S + c - N)) +
-             0.125 * (ld(S + c + 1) - 2.0 * a + ld(S + c - 1)) + a;
+  if (__any_sync(live, slow) && slow) {
+    for (int r = 0; r < np; ++r) {
+      const int64_t c = k + N * (j + N * (i0 + r));
+      const double a0 = ld(S + c);
+      D[c] = 0.125 * (ld(S + c + NN) - 2.0 * a0 + ld(S + c - NN)) +
+             0.125 * (ld(S + c + N) - 2.0 * a0 + ld(S + c - N)) +
+             0.125 * (ld(S + c + 1) - 2.0 * a0 + ld(S + c - 1)) + a0;
     }
   }
 }
@@ -633,6 +654,17 @@ extern "C" {
 constexpr int kJacobiIntAdds4 = 4;
 constexpr bool kJacobiMulInt = true;
 
+// HEAT_3D by default: planes per thread and integer-pipe differences
+// b(+1) - 2a per two planes.  Measured on GB300 (us per half-step at 256^3,
+// 4 planes): 0 of 6 on the integer pipes 243.9, 2: 219.2, 4: 194.7,
+// 5: 184.8, 6: 217.2 (the integer ALU 88% busy: each such difference costs
+// some 65 integer instructions); 2 planes per thread, 5 of 6: 192.6.  Sums
+// (b(+1) - 2a) + b(-1) on the integer pipes measured slower at every count
+// (the ALU is already the co-bound, and a second difference that nearly
+// cancels leaves the close-exponent form).
+constexpr int kHeatPlanes = 4;
+constexpr int kHeatIntSubs2 = 5;
+
 int b200_polybench_jacobi_2d(double* A, double* B, int64_t N, int64_t tsteps,
                              const b200_tune* tune, b200_stream_t stream) {
   if (!A || !B || N < 0 || tsteps < 0) return invalid("b200_polybench_jacobi_2d: bad args");
@@ -725,15 +757,36 @@ int b200_polybench_heat_3d(double* A, double* B, int64_t N, int64_t tsteps,
     return after_launch("b200_polybench_heat_3d", static_cast<int>(2 * tsteps));
   }
   constexpr int BX = 32, BY = 8;
-  int64_t gz = N - 2;
-  if (gz > 65535) gz = 65535;
+  // tile_x = planes per thread (2 or 4), tile_z = 1 + differences on the
+  // integer pipes per two planes (0..6); 0 keeps the defaults
+  const int pl = (tune && tune->tile_x > 0) ? tune->tile_x : kHeatPlanes;
+  const int ks2 = (tune && tune->tile_z > 0) ? tune->tile_z - 1 : kHeatIntSubs2;
+  if ((pl != 2 && pl != 4) || ks2 < 0 || ks2 > 6)
+    return invalid("b200_polybench_heat_3d: bad tile_x/tile_z");
+  const int64_t gz = ceil_div(N - 2, pl);
+  if (ceil_div(N - 2, BY) > 65535 || gz > 65535) return invalid("b200_polybench_heat_3d: N too large");
   dim3 g(static_cast<unsigned>(ceil_div(N - 2, BX)), static_cast<unsigned>(ceil_div(N - 2, BY)),
          static_cast<unsigned>(gz));
-  if (ceil_div(N - 2, BY) > 65535) return invalid("b200_polybench_heat_3d: N too large");
-  for (int64_t t = 0; t < tsteps; ++t) {
-    heat3d_step<BX, BY><<<g, dim3(BX, BY), 0, st>>>(A, B, N, 0);
-    heat3d_step<BX, BY><<<g, dim3(BX, BY), 0, st>>>(B, A, N, 0);
-  }
+  auto run = [&](auto kernel) {
+    for (int64_t t = 0; t < tsteps; ++t) {
+      kernel<<<g, dim3(BX, BY), 0, st>>>(A, B, N, 0);
+      kernel<<<g, dim3(BX, BY), 0, st>>>(B, A, N, 0);
+    }
+  };
+  auto by_ks = [&](auto P) {
+    constexpr int kP = decltype(P)::value;
+    switch (ks2) {
+      case 0: run(heat3d_step<BX, BY, kP, 0>); break;
+      case 1: run(heat3d_step<BX, BY, kP, 1>); break;
+      case 2: run(heat3d_step<BX, BY, kP, 2>); break;
+      case 3: run(heat3d_step<BX, BY, kP, 3>); break;
+      case 4: run(heat3d_step<BX, BY, kP, 4>); break;
+      case 5: run(heat3d_step<BX, BY, kP, 5>); break;
+      default: run(heat3d_step<BX, BY, kP, 6>); break;
+    }
+  };
+  if (pl == 2) by_ks(std::integral_constant<int, 2>{});
+  else by_ks(std::integral_constant<int, 4>{});
   return after_launch("b200_polybench_heat_3d", static_cast<int>(2 * tsteps));
 }
 

@@ -429,14 +429,14 @@ def test_null_pointer_rejected(fn, args):
     assert f(*argv) == rp.B200_ERR_INVALID_ARG
 
 
-@pytest.mark.parametrize("op", [0, 1, 2, 3, 4, 5, 6, 7, 8, 9, 10])
+@pytest.mark.parametrize("op", [0, 1, 2, 3, 4, 5, 6, 7, 8, 9, 10, 11])
 def test_integer_pipe_fp64_is_bit_exact(op):
     """The integer-pipe add/sub/mul used by the mixed-pipe stencils, the
     exponent-shift products by 0.5, 0.125 and 2 of DEL_DOT_VEC_2D and HEAT_3D,
     the FP64-free division of HYDRO_2D and DEL_DOT_VEC_2D, INDEXLIST's integer
     x < 0 test, the integer-pipe multiply of JACOBI_2D, HYDRO_2D and
-    DEL_DOT_VEC_2D, DEL_DOT_VEC_2D's + ptiny and JACOBI_2D's close-exponent
-    integer add, against the FP64 pipe on 16M operands (every class of
+    DEL_DOT_VEC_2D, DEL_DOT_VEC_2D's + ptiny, JACOBI_2D's close-exponent
+    integer add and HEAT_3D's signed one, against the FP64 pipe on 16M operands (every class of
     double; 64M for the division)."""
     torch = gu.torch_cuda()
     bad = torch.zeros(1, dtype=torch.int64, device="cuda")
@@ -466,6 +466,42 @@ def test_jacobi_integer_pipe_adds_bit_identical(N, ts, int_adds, mul_fp64, rows)
                                                 ctypes.byref(t), gu.stream()))
         oracle.call("oracle_jacobi_2d", A, B, N, ts)
         assert np.array_equal(gu.host(dA), A) and np.array_equal(gu.host(dB), B)
+
+
+@pytest.mark.parametrize("N,ts", [(3, 1), (4, 1), (19, 2), (66, 3)])
+@pytest.mark.parametrize("subs2", [0, 1, 2, 3, 4, 5, 6])
+@pytest.mark.parametrize("planes", [2, 4])
+def test_heat_integer_pipe_differences_bit_identical(N, ts, subs2, planes):
+    """HEAT_3D with each thread walking `planes` planes (tile_x) and `subs2`
+    of the six differences b(+1) - 2a of two planes on the integer pipes
+    (tile_z = 1 + subs2): bit-identical to the suite's loop in the oracle on
+    positive data (the fast path, cancellations of any depth), on signed data
+    with zeros (the thread fallback) and on a plateau (exact zeros)."""
+    rng = np.random.default_rng(N + 5 * subs2 + 31 * planes)
+    for data in ("positive", "signed", "plateau"):
+        if data == "plateau":
+            A, B = np.full(N ** 3, 1.0), np.full(N ** 3, 1.0)
+            A[rng.integers(0, N ** 3, 30)] = 1.5
+        else:
+            lo = -1.5 if data == "signed" else 0.5
+            A, B = rng.uniform(lo, 1.5, N ** 3), rng.uniform(lo, 1.5, N ** 3)
+            if data == "signed":
+                A[rng.integers(0, N ** 3, 20)] = 0.0
+        dA, dB = dev(A), dev(B)
+        t = rp.Tune(tile_x=planes, tile_z=1 + subs2)
+        rp.check(lib().b200_polybench_heat_3d(dA.data_ptr(), dB.data_ptr(), N, ts,
+                                              ctypes.byref(t), gu.stream()))
+        oracle.call("oracle_heat_3d", A, B, N, ts)
+        assert np.array_equal(gu.host(dA), A) and np.array_equal(gu.host(dB), B), data
+
+
+def test_heat_integer_pipe_bad_counts_rejected():
+    torch = gu.torch_cuda()
+    d = torch.zeros(27, dtype=torch.float64, device="cuda")
+    for tx, tz in ((2, 8), (1, 1), (3, 1), (8, 1)):
+        t = rp.Tune(tile_x=tx, tile_z=tz)
+        assert lib().b200_polybench_heat_3d(d.data_ptr(), d.data_ptr(), 3, 1, ctypes.byref(t),
+                                            gu.stream()) == rp.B200_ERR_INVALID_ARG
 
 
 @pytest.mark.parametrize("N,ts", [(3, 1), (37, 2), (300, 3)])
