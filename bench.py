@@ -216,8 +216,9 @@ def _bandwidth_cases():
                                   8 * 6 * (kn - 2) * (jn - 2))
             self.flops_per_rep = 44 * (kn - 2) * (jn - 2)
             # ncu: BODY1 10 per point (its divisions and products run on the
-            # integer and FP32 pipes), BODY2+BODY3 20 per point
-            self.fp64_instr_per_rep = 30 * (kn - 2) * (jn - 2)
+            # integer and FP32 pipes), BODY2+BODY3 14 per point (6 of its 8
+            # differences on the integer pipes)
+            self.fp64_instr_per_rep = 24 * (kn - 2) * (jn - 2)
 
         def run(self, s):
             a = [t.data_ptr() for t in self.arr]
@@ -233,7 +234,8 @@ def _bandwidth_cases():
             self.y, self.z, self.u = (self.uniform(n + 7) for _ in range(3))
             self.bytes_per_rep = 16 * n + 8 * (n + 7) + 8 * n
             self.flops_per_rep = 16 * n
-            self.fp64_instr_per_rep = 8 * n
+            # two of the eight FMAs per element on the integer pipes
+            self.fp64_instr_per_rep = 6 * n
 
         def run(self, s):
             return self.L.b200_lcals_eos(self.x.data_ptr(), self.y.data_ptr(), self.z.data_ptr(),
@@ -414,7 +416,7 @@ BW27 = {
     "Stream_COPY": (16, 0), "Stream_MUL": (16, 1), "Stream_ADD": (24, 1),
     "Stream_TRIAD": (24, 1), "Stream_DOT": (16, 1), "Basic_DAXPY": (24, 1),
     "Basic_INIT3": (40, 1), "Basic_MULADDSUB": (40, 3), "Lcals_HYDRO_1D": (24, 3),
-    "Lcals_EOS": (32, 8), "Lcals_FIRST_DIFF": (16, 1), "Lcals_INT_PREDICT": (88, 9),
+    "Lcals_EOS": (32, 6), "Lcals_FIRST_DIFF": (16, 1), "Lcals_INT_PREDICT": (88, 9),
     "Lcals_FIRST_MIN": (8, 0), "Lcals_DIFF_PREDICT": (160, 9), "Lcals_PLANCKIAN": (40, 16),
     "Apps_PRESSURE": (48, 6), "Apps_ENERGY": (216, 18), "Algorithm_SCAN": (16, 0),
     "Algorithm_REDUCE_SUM": (8, 1), "Algorithm_MEMSET": (8, 0), "Algorithm_MEMCPY": (16, 0),

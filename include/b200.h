@@ -127,7 +127,11 @@ int b200_probe_dfma(double* out, int32_t iters, int64_t* fma_count,
  * and non-finite values added), 11 = a + b of either sign with close
  * exponents (HEAT_3D's integer-pipe b(+1) - 2a: exponents 0-4 apart, b near
  * -a with differences of 0 to 53 bits, results below the normal range, the
- * top of the range, special values added); adds to *mismatches (device) the number of
+ * top of the range, special values added), 12 = a * b + c on the integer
+ * pipes (EOS's FMAs: positive operands, c 0 to 74 bits above the product's
+ * last bit and a little past that window, products with low bits cleared for
+ * near-ties, the top and bottom of the range, zeros, subnormals, negatives
+ * and non-finite values added); adds to *mismatches (device) the number of
  * results whose bits differ from the FP64 pipe's.  Not in the reference. */
 int b200_f64emu_selftest(int64_t n, uint64_t seed, int32_t op,
                          unsigned long long* mismatches, b200_stream_t stream);
@@ -237,7 +241,9 @@ int b200_lcals_hydro_1d(double* x, const double* y, const double* z, double q,
 
 /* One rep of HYDRO_2D on a kn x jn row-major grid (index j + k*jn): BODY1
  * (za, zb) then BODY2 (zu, zv +=) and BODY3 (zrout, zzout) over the interior
- *   -- lcals/HYDRO_2D.hpp:66-90, HYDRO_2D-Cuda.cpp:104-140.  Two launches.   */
+ *   -- lcals/HYDRO_2D.hpp:66-90, HYDRO_2D-Cuda.cpp:104-140.  Two launches.
+ * tune->tile_z - 1 of BODY2's eight differences (0, 2, 4, 6, 8; default 6)
+ * run on the integer pipes (exact, bit-identical).                          */
 int b200_lcals_hydro_2d(double* za, double* zb, const double* zm,
                         const double* zp, const double* zq, const double* zr,
                         double* zu, double* zv, const double* zz, double* zrout,
@@ -245,7 +251,13 @@ int b200_lcals_hydro_2d(double* za, double* zb, const double* zm,
                         int64_t jn, const b200_tune* tune, b200_stream_t stream);
 
 /* x[i] = EOS polynomial; y, z, u hold >= n+7 values
- *   -- lcals/EOS.hpp:33, EOS-Cuda.cpp:26                                    */
+ *   -- lcals/EOS.hpp:33, EOS-Cuda.cpp:26
+ * Default: tune->tile_z - 1 of each element's eight FMAs (1..3; default 2)
+ * run on the integer pipes (exact a * b + c for positive operands,
+ * bit-identical; other operands take the FP64 pipe), tune->items elements
+ * per thread (1, 2, 4, 8; default 2), tune->block_size threads (128, 256,
+ * 512; default 128).  tune->tile_z = 1, or another block size: the
+ * element-map kernel, all eight FMAs on the FP64 pipe.                      */
 int b200_lcals_eos(double* x, const double* y, const double* z, const double* u,
                    double q, double r, double t, int64_t n,
                    const b200_tune* tune, b200_stream_t stream);

@@ -391,7 +391,7 @@ __global__ void f64emu_check_kernel(int64_t n, uint64_t seed, int op,
   for (int64_t i = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; i < n;
        i += stride) {
     uint64_t ra = rnd64(seed, 2 * i), rb = rnd64(seed, 2 * i + 1);
-    uint64_t A = ra, B = rb;
+    uint64_t A = ra, B = rb, C = 0;  // C: op 12's addend
     switch (i % 5) {
       case 0: break;
       case 1: {  // exponents within 2 of each other
@@ -481,6 +481,31 @@ __global__ void f64emu_check_kernel(int64_t n, uint64_t seed, int op,
         A = sp[(ra >> 60) % 6u] | (A & 0x8000000000000000ULL);
       }
     }
+    if (op == 12) {  // a * b + c: positive, c a few binades above the product (EOS), the
+                     // window edges, near-ties, the top and bottom of the range, specials
+      const uint64_t ea = (i % 5) == 3 ? 1000u + (ra >> 58) % 40u : 900u + (ra >> 12) % 200u;
+      const uint64_t eb = (i % 5) == 4 ? 2u + (rb >> 58) % 30u : 1000u + (rb >> 12) % 46u;
+      A = (ra & 0x000FFFFFFFFFFFFFULL) | (ea << 52);
+      B = (rb & 0x000FFFFFFFFFFFFFULL) | (eb << 52);
+      // c's exponent from D = ec + 1075 - ea - eb in [-3, 78]: the window [0, 74] and past it
+      const int64_t D = static_cast<int64_t>((ra >> 40) % 82u) - 3;
+      int64_t ec = D + static_cast<int64_t>(ea + eb) - 1075;
+      if ((i % 5) == 3) ec = 2040 + static_cast<int64_t>((rb >> 40) % 8u);  // the top of the range
+      if (ec < 0) ec = 0;
+      if (ec > 2047) ec = 2047;
+      const uint64_t mc = (rb >> 5) & 0x000FFFFFFFFFFFFFULL;
+      C = mc | (static_cast<uint64_t>(ec) << 52);
+      if ((i % 3) == 1) {  // low bits of a and b cleared: exact products, sums near ties
+        A &= ~0x3FFFFFFULL;
+        B &= ~0x3FFFFFFULL;
+      }
+      if ((i % 7) == 6) {  // zeros, subnormals, negatives, infinities, NaNs: the slow path
+        const uint64_t sp[6] = {0x0ULL, 0x8000000000000000ULL, 0x7FF0000000000000ULL,
+                                0x0000000000000001ULL, 0x7FF8000000000001ULL,
+                                0xBFF0000000000000ULL};
+        if ((ra >> 61) & 1u) A = sp[(ra >> 58) % 6u]; else C = sp[(rb >> 58) % 6u];
+      }
+    }
     if (op == 9 && (i % 5) != 0 && (i % 5) != 3) {  // a + tiny b: gaps 50-60 around 55
       const uint64_t e = ((ra >> 12) % 1900u) + 70u;
       const uint64_t gap = 50u + (rb >> 58) % 11u;
@@ -523,6 +548,12 @@ __global__ void f64emu_check_kernel(int64_t n, uint64_t seed, int op,
       bool slow = false;
       got = b200::f64emu::add_close_fast(a, b, slow);
       if (slow) got = __dadd_rn(a, b);
+    } else if (op == 12) {  // a * b + c on the integer pipes, as EOS's FMAs
+      const double c = __longlong_as_double(static_cast<long long>(C));
+      want = __fma_rn(a, b, c);
+      bool slow = false;
+      got = b200::f64emu::fma_pos_fast(a, b, c, slow);
+      if (slow) got = __fma_rn(a, b, c);
     } else if (op == 11) {  // a + b, either sign, close exponents, as HEAT_3D's b(+1) - 2a
       want = __dadd_rn(a, b);
       bool slow = false;
@@ -551,7 +582,7 @@ __global__ void f64emu_check_kernel(int64_t n, uint64_t seed, int op,
 
 extern "C" int b200_f64emu_selftest(int64_t n, uint64_t seed, int32_t op,
                                     unsigned long long* mismatches, b200_stream_t stream) {
-  if (n < 0 || !mismatches || op < 0 || op > 11) return invalid("b200_f64emu_selftest: bad args");
+  if (n < 0 || !mismatches || op < 0 || op > 12) return invalid("b200_f64emu_selftest: bad args");
   const int blocks = device_info().sm_count * 8;
   f64emu_check_kernel<<<blocks, 256, 0, as_stream(stream)>>>(n, seed, op, mismatches);
   return after_launch("b200_f64emu_selftest");

@@ -209,6 +209,48 @@ __device__ __forceinline__ double sub_near_fast(double a, double b, bool& slow) 
   return add_near_bits<true>(bits_opaque(a), bits_opaque(b), slow);
 }
 
+// a * b + c with one rounding (the FP64 pipe's fma) on the integer pipes, for
+// positive normal operands with c's last bit at or above the product's
+// (D = ec + 1075 - ea - eb, the shift of c's significand to the product's
+// scale, in [0, 74]).  The 106-bit product of the significands and c's
+// shifted significand add exactly in 128 bits (their sum stays below 2^128);
+// the sum is shifted up until its leading one is bit 127 (the product alone
+// is at least 2^104, so the high word is never zero), the top 53 bits are
+// kept, and bit 74 with the OR of the bits below decides round to nearest
+// even.  `slow` is set for every other input (a zero, subnormal, negative,
+// infinite or NaN operand; c too far below the product or too far above
+// it; a result leaving the normal range), for which the caller uses the FP64
+// pipe.  About 60 integer instructions against one DFMA (EOS's r * y + z,
+// whose addends exceed their products by a few binades).
+__device__ __forceinline__ double fma_pos_fast(double a, double b, double c, bool& slow) {
+  const uint64_t A = bits_opaque(a), B = bits_opaque(b), C = bits_opaque(c);
+  // biased exponents with the sign bit above them: a negative operand gives
+  // a value of 2048 or more and fails the range test
+  const uint32_t ea = static_cast<uint32_t>(A >> 52), eb = static_cast<uint32_t>(B >> 52);
+  const uint32_t ec = static_cast<uint32_t>(C >> 52);
+  const int D = static_cast<int>(ec) + 1075 - static_cast<int>(ea) - static_cast<int>(eb);
+  if (ea - 1u > 2045u || eb - 1u > 2045u || ec - 1u > 2045u ||
+      static_cast<unsigned>(D) > 74u) {
+    slow = true;
+    return 0.0;
+  }
+  const uint64_t ma = (A & kFrac) | kHidden, mb = (B & kFrac) | kHidden, mc = (C & kFrac) | kHidden;
+  using u128 = unsigned __int128;
+  const u128 S = static_cast<u128>(ma) * mb + (static_cast<u128>(mc) << D);  // exact, < 2^128
+  const uint32_t lz = static_cast<uint32_t>(__clzll(static_cast<long long>(S >> 64)));  // 0..23
+  const u128 V = S << lz;                                    // leading one at bit 127
+  const uint64_t vh = static_cast<uint64_t>(V >> 64), vl = static_cast<uint64_t>(V);
+  const uint64_t mant = vh >> 11;                            // 53 bits with the hidden one
+  const uint32_t rest = static_cast<uint32_t>(vh) & 0x7ffu;  // round bit 0x400, sticky below
+  const uint64_t up = (rest > 0x400u || (rest == 0x400u && (vl != 0u || (mant & 1u)))) ? 1u : 0u;
+  const int e = static_cast<int>(ea + eb) - 1000 - static_cast<int>(lz);  // the result's biased exponent
+  if (e <= 0 || e >= 2046) {
+    slow = true;
+    return 0.0;
+  }
+  return from_bits((static_cast<uint64_t>(e - 1) << 52) + mant + up);
+}
+
 // x * 2^k for a small |k|: exact exponent arithmetic; native when the result
 // would leave the normal range (or x is not a normal number).
 __device__ __forceinline__ double scale2(double x, int k) {

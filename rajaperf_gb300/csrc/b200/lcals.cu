@@ -8,6 +8,8 @@
 #include "b200_map.cuh"
 #include "b200_reduce.cuh"
 
+#include <type_traits>
+
 using namespace b200;
 
 namespace {
@@ -48,6 +50,63 @@ struct Eos {
     x[i] = fma(tr, fma(tr, c, b), a);
   }
 };
+
+// EOS with KF of each element's eight FMAs on the integer pipes
+// (f64emu::fma_pos_fast, bit-identical), in the order r*y+z, r*u1+u2,
+// q*u4+u5, then the three outer ones of each group, then the two in t.  A
+// CTA covers PT * BS consecutive elements, a thread every BS-th of them
+// (coalesced).  An element whose operands leave the integer form's range
+// stores nothing in the loop and is redone on the FP64 pipe after it (one
+// bit per element); an FP64 redo inside the loop would be compiled as
+// predicated FMAs, which occupy the FP64 pipe in every warp.
+template <int BS, int PT, int KF>
+__global__ void __launch_bounds__(BS)
+eos_split_kernel(double* __restrict__ x, const double* __restrict__ y,
+                 const double* __restrict__ z, const double* __restrict__ u, double q,
+                 double r, double t, int64_t n, int zero) {
+  static_assert(KF >= 0 && KF <= 8 && PT >= 1 && PT <= 64, "0..8 integer FMAs, one bit each");
+  const double rr = fform::reg(r, zero), tr = fform::reg(t, zero), qr = fform::reg(q, zero);
+  const int64_t base = static_cast<int64_t>(blockIdx.x) * BS * PT + threadIdx.x;
+  auto f = [&](int m, double a, double b, double c, bool& slow) {
+    return (m < KF) ? f64emu::fma_pos_fast(a, b, c, slow) : fma(a, b, c);
+  };
+  uint64_t redo = 0;
+  auto element = [&](int p) {
+    const int64_t i = base + static_cast<int64_t>(p) * BS;
+    bool slow = false;
+    const double a1 = f(0, rr, ld(y + i), ld(z + i), slow);
+    const double b1 = f(1, rr, ld(u + i + 1), ld(u + i + 2), slow);
+    const double c1 = f(2, qr, ld(u + i + 4), ld(u + i + 5), slow);
+    const double a = f(3, rr, a1, ld(u + i), slow);
+    const double b = f(4, rr, b1, ld(u + i + 3), slow);
+    const double c = f(5, qr, c1, ld(u + i + 6), slow);
+    const double v = f(7, tr, f(6, tr, c, b, slow), a, slow);
+    if (!slow) x[i] = v;
+    else redo |= 1ull << p;
+  };
+  if (static_cast<int64_t>(blockIdx.x + 1) * BS * PT <= n) {
+    // a whole CTA in range: no bounds test, so the unrolled elements' loads
+    // issue together
+#pragma unroll
+    for (int p = 0; p < PT; ++p) element(p);
+  } else {
+    for (int p = 0; p < PT; ++p) {
+      if (base + static_cast<int64_t>(p) * BS >= n) break;
+      element(p);
+    }
+  }
+  if (KF > 0 && __any_sync(__activemask(), redo != 0)) {
+    for (int p = 0; p < PT; ++p) {
+      const int64_t i = base + static_cast<int64_t>(p) * BS;
+      if (i < n && ((redo >> p) & 1u)) {
+        const double a = fma(rr, fma(rr, ld(y + i), ld(z + i)), ld(u + i));
+        const double b = fma(rr, fma(rr, ld(u + i + 1), ld(u + i + 2)), ld(u + i + 3));
+        const double c = fma(qr, fma(qr, ld(u + i + 4), ld(u + i + 5)), ld(u + i + 6));
+        x[i] = fma(tr, fma(tr, c, b), a);
+      }
+    }
+  }
+}
 
 // lcals/FIRST_DIFF.hpp:25
 struct FirstDiff {
@@ -202,15 +261,24 @@ hydro2d_body1(double* __restrict__ za, double* __restrict__ zb,
   }
 }
 
-template <int BS>
+// KH of the eight differences (du1..du4, dv1..dv4 in that order) run on the
+// integer pipes (f64emu::sub_near_fast, bit-identical).  A point whose
+// operands are outside that form's range stores nothing in the loop (zu and
+// zv are updated in place, so its inputs stay intact) and is redone on the
+// FP64 pipe after the loop; a thread holds at most 64 points (the launcher
+// checks), one bit each.  An FP64 redo inside the loop would be compiled as
+// predicated FP64 instructions, which occupy the FP64 pipe in every warp.
+template <int BS, int KH>
 __global__ void __launch_bounds__(BS)
 hydro2d_body23(const double* __restrict__ za, const double* __restrict__ zb,
                const double* __restrict__ zr, double* __restrict__ zu,
                double* __restrict__ zv, const double* __restrict__ zz,
                double* __restrict__ zrout, double* __restrict__ zzout, double s,
                double t, int64_t kn, int64_t jn, int zero) {
+  static_assert(KH >= 0 && KH <= 8, "0..8 integer-pipe differences");
   const int64_t j = 1 + static_cast<int64_t>(blockIdx.x) * BS + threadIdx.x;
   if (j >= jn - 1) return;
+  const unsigned live = __activemask();
   // Every FP64 instruction a register-operand FMA (fform: the differences and
   // the leading products, s and t in per-thread registers), which the FP64
   // pipe issues at its full rate; `zero` is 0 at run time.  (The leading
@@ -219,25 +287,45 @@ hydro2d_body23(const double* __restrict__ za, const double* __restrict__ zb,
   // like executed ones.)
   const fform::Regs fr = fform::regs(zero);
   const double sr = fform::reg(s, zero), tr = fform::reg(t, zero);
-  for (int64_t k = 1 + blockIdx.y; k < kn - 1; k += gridDim.y) {
-    const int64_t c = j + k * jn;
+  auto point = [&](int64_t c, bool use_int, bool& slow) {
     const double za0 = ld(za + c), za1 = ld(za + c - 1);
     const double zb0 = ld(zb + c), zb1 = ld(zb + c + jn);
     const double zz0 = ld(zz + c), zr0 = ld(zr + c);
-    const double du1 = fform::sub(zz0, ld(zz + c + 1), fr), du2 = fform::sub(zz0, ld(zz + c - 1), fr);
-    const double du3 = fform::sub(zz0, ld(zz + c - jn), fr), du4 = fform::sub(zz0, ld(zz + c + jn), fr);
-    const double dv1 = fform::sub(zr0, ld(zr + c + 1), fr), dv2 = fform::sub(zr0, ld(zr + c - 1), fr);
-    const double dv3 = fform::sub(zr0, ld(zr + c - jn), fr), dv4 = fform::sub(zr0, ld(zr + c + jn), fr);
+    const int64_t off[4] = {1, -1, -jn, jn};
+    double du[4], dv[4];
+#pragma unroll
+    for (int m = 0; m < 4; ++m) {
+      const double zn = ld(zz + c + off[m]), rn = ld(zr + c + off[m]);
+      du[m] = (use_int && m < KH) ? f64emu::sub_near_fast(zz0, zn, slow) : fform::sub(zz0, zn, fr);
+      dv[m] = (use_int && m + 4 < KH) ? f64emu::sub_near_fast(zr0, rn, slow)
+                                      : fform::sub(zr0, rn, fr);
+    }
     // zu + s * (((za0 du1 - za1 du2) - zb0 du3) + zb1 du4), left to right as
     // the suite writes it, the products after the first and s * (...) as FMAs
-    const double u = fma(sr, fma(zb1, du4, fma(-zb0, du3, fma(-za1, du2, fform::mul(za0, du1, fr)))),
+    const double u = fma(sr, fma(zb1, du[3], fma(-zb0, du[2], fma(-za1, du[1], fform::mul(za0, du[0], fr)))),
                          zu[c]);
-    const double v = fma(sr, fma(zb1, dv4, fma(-zb0, dv3, fma(-za1, dv2, fform::mul(za0, dv1, fr)))),
+    const double v = fma(sr, fma(zb1, dv[3], fma(-zb0, dv[2], fma(-za1, dv[1], fform::mul(za0, dv[0], fr)))),
                          zv[c]);
-    zu[c] = u;
-    zv[c] = v;
-    zrout[c] = fma(tr, u, zr0);
-    zzout[c] = fma(tr, v, zz0);
+    if (!slow) {
+      zu[c] = u;
+      zv[c] = v;
+      zrout[c] = fma(tr, u, zr0);
+      zzout[c] = fma(tr, v, zz0);
+    }
+  };
+  uint64_t redo = 0;
+  int it = 0;
+  for (int64_t k = 1 + blockIdx.y; k < kn - 1; k += gridDim.y, ++it) {
+    bool slow = false;
+    point(j + k * jn, KH > 0, slow);
+    if (slow) redo |= 1ull << it;
+  }
+  if (KH > 0 && __any_sync(live, redo != 0)) {
+    it = 0;
+    for (int64_t k = 1 + blockIdx.y; k < kn - 1; k += gridDim.y, ++it) {
+      bool slow = false;
+      if ((redo >> it) & 1u) point(j + k * jn, false, slow);
+    }
   }
 }
 
@@ -358,12 +446,57 @@ int b200_lcals_hydro_1d(double* x, const double* y, const double* z, double q,
                       as_stream(stream));
 }
 
+// EOS FMAs per element on the integer pipes by default (0: the map kernel).
+// Measured on GB300 (us at 2^24 / 2^27): 0 (map kernel, 256 x 2): 223.2 /
+// 1729.5; with 128 threads and 2 elements per thread 2: 176.1 / 1374.2, 3:
+// 188.4 / 1473.1; with 16 elements per thread 1: 206.8, 2: 194.6, 3: 223.2,
+// 4: 258.0 at 2^24 (each integer FMA some 80 integer instructions: from 3
+// on, the integer pipes are the bound).
+constexpr int kEosIntFmas = 2;
+constexpr int kEosPerThread = 2;
+
 int b200_lcals_eos(double* x, const double* y, const double* z, const double* u,
                    double q, double r, double t, int64_t n, const b200_tune* tune,
                    b200_stream_t stream) {
   if (n < 0 || (n > 0 && (!x || !y || !z || !u))) return invalid("b200_lcals_eos: bad args");
-  return launch_map1d("b200_lcals_eos", Eos{x, y, z, u, q, r, t, 0}, n, tune,
-                      as_stream(stream));
+  // tune->tile_z = 1 + FMAs per element on the integer pipes (0..3), items =
+  // elements per thread (1, 2, 4 or 8), block_size 128, 256 or 512; 0 keeps
+  // the defaults.  No integer FMAs, or another block size: the element-map
+  // kernel (tune->block_size, items), all eight FMAs on the FP64 pipe.
+  const int kf = (tune && tune->tile_z > 0) ? tune->tile_z - 1 : kEosIntFmas;
+  if (kf < 0 || kf > 3) return invalid("b200_lcals_eos: bad tile_z");
+  const int bs = (tune && tune->block_size) ? tune->block_size : 128;
+  if (kf == 0 || n == 0 || (bs != 128 && bs != 256 && bs != 512))
+    return launch_map1d("b200_lcals_eos", Eos{x, y, z, u, q, r, t, 0}, n, tune,
+                        as_stream(stream));
+  const int pt = (tune && tune->items) ? tune->items : kEosPerThread;
+  if (pt != 1 && pt != 2 && pt != 4 && pt != 8) return invalid("b200_lcals_eos: bad items %d", pt);
+  const int64_t grid = ceil_div(n, static_cast<int64_t>(bs) * pt);
+  if (grid > 0x7fffffff) return invalid("b200_lcals_eos: n too large");
+  cudaStream_t st = as_stream(stream);
+  auto go = [&](auto B, auto P, auto K) {
+    eos_split_kernel<decltype(B)::value, decltype(P)::value, decltype(K)::value>
+        <<<static_cast<unsigned>(grid), decltype(B)::value, 0, st>>>(x, y, z, u, q, r, t, n, 0);
+  };
+  auto by_kf = [&](auto B, auto P) {
+    switch (kf) {
+      case 1: go(B, P, std::integral_constant<int, 1>{}); break;
+      case 2: go(B, P, std::integral_constant<int, 2>{}); break;
+      default: go(B, P, std::integral_constant<int, 3>{}); break;
+    }
+  };
+  auto by_pt = [&](auto B) {
+    switch (pt) {
+      case 1: by_kf(B, std::integral_constant<int, 1>{}); break;
+      case 2: by_kf(B, std::integral_constant<int, 2>{}); break;
+      case 4: by_kf(B, std::integral_constant<int, 4>{}); break;
+      default: by_kf(B, std::integral_constant<int, 8>{}); break;
+    }
+  };
+  if (bs == 128) by_pt(std::integral_constant<int, 128>{});
+  else if (bs == 256) by_pt(std::integral_constant<int, 256>{});
+  else by_pt(std::integral_constant<int, 512>{});
+  return after_launch("b200_lcals_eos");
 }
 
 int b200_lcals_first_diff(double* x, const double* y, int64_t n, const b200_tune* tune,
@@ -401,6 +534,13 @@ int b200_lcals_planckian(const double* x, double* y, const double* u, const doub
                       as_stream(stream));
 }
 
+// HYDRO_2D's BODY2 differences on the integer pipes by default (of 8).
+// Measured on GB300 (us per rep at 4096^2, BODY1 + BODY2/3, 64 threads):
+// 0: 864.9, 2: 815.1, 4: 764.5, 6: 756.4, 8: 832.1 (BODY2/3 alone: 546 us
+// at 0, 447 at 4 with the FP64 pipe 97% and the integer ALU 55% busy, 516
+// at 8 with the ALU 90% busy and the FP64 pipe 63%).
+constexpr int kHydroIntSubs = 6;
+
 int b200_lcals_hydro_2d(double* za, double* zb, const double* zm, const double* zp,
                         const double* zq, const double* zr, double* zu, double* zv,
                         const double* zz, double* zrout, double* zzout, double s,
@@ -414,10 +554,24 @@ int b200_lcals_hydro_2d(double* za, double* zb, const double* zm, const double* 
   if (!valid_block(bs)) return invalid("b200_lcals_hydro_2d: bad block size %d", bs);
   cudaStream_t st = as_stream(stream);
   dim3 grid = rows_grid(jn, kn, bs);
+  // tune->tile_z = 1 + differences of BODY2 on the integer pipes (0, 2, 4,
+  // 6 or 8); 0 keeps the default
+  int kh = (tune && tune->tile_z > 0) ? tune->tile_z - 1 : kHydroIntSubs;
+  if (kh < 0 || kh > 8 || (kh & 1)) return invalid("b200_lcals_hydro_2d: bad tile_z");
+  if (ceil_div(kn - 2, static_cast<int64_t>(grid.y)) > 64) kh = 0;  // one redo bit per point
   B200_DISPATCH_BLOCK(bs, BS,
     hydro2d_body1<BS><<<grid, BS, 0, st>>>(za, zb, zm, zp, zq, zr, kn, jn, 0);
-    hydro2d_body23<BS><<<grid, BS, 0, st>>>(za, zb, zr, zu, zv, zz, zrout, zzout, s, t,
-                                            kn, jn, 0));
+    auto body23 = [&](auto K) {
+      hydro2d_body23<BS, decltype(K)::value><<<grid, BS, 0, st>>>(za, zb, zr, zu, zv, zz, zrout,
+                                                                  zzout, s, t, kn, jn, 0);
+    };
+    switch (kh) {
+      case 0: body23(std::integral_constant<int, 0>{}); break;
+      case 2: body23(std::integral_constant<int, 2>{}); break;
+      case 4: body23(std::integral_constant<int, 4>{}); break;
+      case 6: body23(std::integral_constant<int, 6>{}); break;
+      default: body23(std::integral_constant<int, 8>{}); break;
+    });
   return after_launch("b200_lcals_hydro_2d", 2);
 }
 

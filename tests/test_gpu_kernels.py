@@ -429,14 +429,14 @@ def test_null_pointer_rejected(fn, args):
     assert f(*argv) == rp.B200_ERR_INVALID_ARG
 
 
-@pytest.mark.parametrize("op", [0, 1, 2, 3, 4, 5, 6, 7, 8, 9, 10, 11])
+@pytest.mark.parametrize("op", [0, 1, 2, 3, 4, 5, 6, 7, 8, 9, 10, 11, 12])
 def test_integer_pipe_fp64_is_bit_exact(op):
     """The integer-pipe add/sub/mul used by the mixed-pipe stencils, the
     exponent-shift products by 0.5, 0.125 and 2 of DEL_DOT_VEC_2D and HEAT_3D,
     the FP64-free division of HYDRO_2D and DEL_DOT_VEC_2D, INDEXLIST's integer
     x < 0 test, the integer-pipe multiply of JACOBI_2D, HYDRO_2D and
     DEL_DOT_VEC_2D, DEL_DOT_VEC_2D's + ptiny, JACOBI_2D's close-exponent
-    integer add and HEAT_3D's signed one, against the FP64 pipe on 16M operands (every class of
+    integer add, HEAT_3D's signed one and EOS's integer-pipe FMA, against the FP64 pipe on 16M operands (every class of
     double; 64M for the division)."""
     torch = gu.torch_cuda()
     bad = torch.zeros(1, dtype=torch.int64, device="cuda")
@@ -602,6 +602,68 @@ def close_special(got, want, rtol=1e-12):
     fin = np.isfinite(want)
     if fin.any():
         close(got[fin], want[fin], rtol)
+
+
+@pytest.mark.parametrize("kh", [2, 4, 6, 8])
+@pytest.mark.parametrize("kn,jn", [(3, 3), (9, 70), (131, 257)])
+def test_hydro_2d_integer_pipe_differences_bit_identical(kh, kn, jn):
+    """BODY2 with `kh` of its eight differences on the integer pipes
+    (tile_z = 1 + kh): every output bit-identical to the FP64-pipe kernel
+    (tile_z = 1), on positive data (the fast path) and on signed data with
+    zeros, subnormals and equal neighbours (the voted FP64 redo)."""
+    rng = np.random.default_rng(kh * 7 + kn + jn)
+    for data in ("positive", "special"):
+        arrs = [rng.uniform(0.5 if data == "positive" else -1.5, 1.5, kn * jn) for _ in range(11)]
+        if data == "special":
+            zz, zr = arrs[8], arrs[5]
+            zz[rng.integers(0, kn * jn, 40)] = 0.0
+            zr[rng.integers(0, kn * jn, 40)] = 3e-310
+            zz[1::7] = zz[0::7][: len(zz[1::7])]              # equal neighbours: exact zeros
+        outs = []
+        for tz in (1, 1 + kh):
+            d = [dev(a) for a in arrs]
+            t = rp.Tune(tile_z=tz)
+            rp.check(lib().b200_lcals_hydro_2d(*[x.data_ptr() for x in d], 0.0041, 0.0037, kn, jn,
+                                               ctypes.byref(t), gu.stream()))
+            outs.append([gu.host(x) for x in d])
+        for g, w in zip(outs[1], outs[0]):
+            assert np.array_equal(g.view(np.int64), w.view(np.int64)), data
+
+
+def test_hydro_2d_bad_difference_count_rejected():
+    torch = gu.torch_cuda()
+    d = torch.zeros(9, dtype=torch.float64, device="cuda")
+    for tz in (2, 10):
+        t = rp.Tune(tile_z=tz)
+        assert lib().b200_lcals_hydro_2d(*([d.data_ptr()] * 11), 0.1, 0.1, 3, 3, ctypes.byref(t),
+                                         gu.stream()) == rp.B200_ERR_INVALID_ARG
+
+
+@pytest.mark.parametrize("kf,items,block", [(1, 2, 128), (2, 2, 128), (3, 2, 128), (2, 1, 256),
+                                             (2, 4, 512), (2, 8, 128), (3, 8, 256)])
+@pytest.mark.parametrize("n", [1, 7, 4097, 100003])
+def test_eos_integer_pipe_fmas_bit_identical(kf, items, block, n):
+    """EOS with `kf` of each element's eight FMAs on the integer pipes
+    (tile_z = 1 + kf): bit-identical to the FP64-pipe kernel (tile_z = 1) on
+    the suite's kind of data (positive; the fast path), on signed data with
+    zeros and subnormals (the redo after the loop) and with coefficients
+    that put some addends below their products."""
+    rng = np.random.default_rng(kf * 31 + items * 7 + block + n)
+    for data, coef in (("positive", (0.0979, 0.1958, 0.0979)), ("special", (0.0979, 0.1958, 0.0979)),
+                       ("positive", (3.5e9, 2.1e-3, 7.0))):
+        lo = 0.5 if data == "positive" else -1.5
+        y, z, u = (rng.uniform(lo, 1.5, n + 7) for _ in range(3))
+        if data == "special":
+            z[rng.integers(0, n + 7, max(1, n // 50))] = 0.0
+            u[rng.integers(0, n + 7, max(1, n // 50))] = 2e-310
+        outs = []
+        for tz in (1, 1 + kf):
+            dx, dy, dz, du = dev(np.zeros(n + 7)), dev(y), dev(z), dev(u)
+            t = rp.Tune(tile_z=tz, items=items if tz > 1 else 0, block_size=block if tz > 1 else 0)
+            rp.check(lib().b200_lcals_eos(dx.data_ptr(), dy.data_ptr(), dz.data_ptr(), du.data_ptr(),
+                                          *coef, n, ctypes.byref(t), gu.stream()))
+            outs.append(gu.host(dx))
+        assert np.array_equal(outs[0].view(np.int64), outs[1].view(np.int64)), (data, coef)
 
 
 def test_hydro_2d_division_special_values():
