@@ -51,37 +51,26 @@ struct Eos {
   }
 };
 
-// EOS with KF of each element's eight FMAs on the integer pipes
-// (f64emu::fma_pos_fast, bit-identical), in the order r*y+z, r*u1+u2,
-// q*u4+u5, then the three outer ones of each group, then the two in t.  A
-// CTA covers PT * BS consecutive elements, a thread every BS-th of them
-// (coalesced).  An element whose operands leave the integer form's range
-// stores nothing in the loop and is redone on the FP64 pipe after it (one
-// bit per element); an FP64 redo inside the loop would be compiled as
-// predicated FMAs, which occupy the FP64 pipe in every warp.
-template <int BS, int PT, int KF>
-__global__ void __launch_bounds__(BS)
-eos_split_kernel(double* __restrict__ x, const double* __restrict__ y,
-                 const double* __restrict__ z, const double* __restrict__ u, double q,
-                 double r, double t, int64_t n, int zero) {
-  static_assert(KF >= 0 && KF <= 8 && PT >= 1 && PT <= 64, "0..8 integer FMAs, one bit each");
-  const double rr = fform::reg(r, zero), tr = fform::reg(t, zero), qr = fform::reg(q, zero);
+// Element map with part of each element's FP64 work on the integer pipes.
+// F::split(i, regs, slow) computes element i with some operations in an
+// exact integer form (bit-identical to the FP64 pipe's) and sets `slow` when
+// an operand leaves that form's range; F::exact(i, regs) is the all-FP64
+// form.  A CTA covers PT * BS consecutive elements, a thread every BS-th of
+// them (coalesced).  An element that met `slow` stores nothing in the loop
+// and is redone with F::exact after it (one bit per element): an FP64 redo
+// inside the loop would be compiled as predicated FP64 instructions, which
+// occupy the FP64 pipe in every warp.
+template <int BS, int PT, class F>
+__global__ void __launch_bounds__(BS) split_map_kernel(F f, int64_t n) {
+  static_assert(PT >= 1 && PT <= 64, "one redo bit per element");
+  const auto rg = f.regs();
   const int64_t base = static_cast<int64_t>(blockIdx.x) * BS * PT + threadIdx.x;
-  auto f = [&](int m, double a, double b, double c, bool& slow) {
-    return (m < KF) ? f64emu::fma_pos_fast(a, b, c, slow) : fma(a, b, c);
-  };
   uint64_t redo = 0;
   auto element = [&](int p) {
     const int64_t i = base + static_cast<int64_t>(p) * BS;
     bool slow = false;
-    const double a1 = f(0, rr, ld(y + i), ld(z + i), slow);
-    const double b1 = f(1, rr, ld(u + i + 1), ld(u + i + 2), slow);
-    const double c1 = f(2, qr, ld(u + i + 4), ld(u + i + 5), slow);
-    const double a = f(3, rr, a1, ld(u + i), slow);
-    const double b = f(4, rr, b1, ld(u + i + 3), slow);
-    const double c = f(5, qr, c1, ld(u + i + 6), slow);
-    const double v = f(7, tr, f(6, tr, c, b, slow), a, slow);
-    if (!slow) x[i] = v;
+    const double v = f.split(i, rg, slow);
+    if (!slow) f.store(i, v);
     else redo |= 1ull << p;
   };
   if (static_cast<int64_t>(blockIdx.x + 1) * BS * PT <= n) {
@@ -95,17 +84,72 @@ eos_split_kernel(double* __restrict__ x, const double* __restrict__ y,
       element(p);
     }
   }
-  if (KF > 0 && __any_sync(__activemask(), redo != 0)) {
+  if (__any_sync(__activemask(), redo != 0)) {
     for (int p = 0; p < PT; ++p) {
       const int64_t i = base + static_cast<int64_t>(p) * BS;
-      if (i < n && ((redo >> p) & 1u)) {
-        const double a = fma(rr, fma(rr, ld(y + i), ld(z + i)), ld(u + i));
-        const double b = fma(rr, fma(rr, ld(u + i + 1), ld(u + i + 2)), ld(u + i + 3));
-        const double c = fma(qr, fma(qr, ld(u + i + 4), ld(u + i + 5)), ld(u + i + 6));
-        x[i] = fma(tr, fma(tr, c, b), a);
-      }
+      if (i < n && ((redo >> p) & 1u)) f.store(i, f.exact(i, rg));
     }
   }
+}
+
+// EOS with KF of each element's eight FMAs on the integer pipes
+// (f64emu::fma_pos_fast), in the order r*y+z, r*u1+u2, q*u4+u5, then the
+// three outer ones of each group, then the two in t.
+template <int KF>
+struct EosSplit {
+  double* __restrict__ x;
+  const double* __restrict__ y;
+  const double* __restrict__ z;
+  const double* __restrict__ u;
+  double q, r, t;
+  int zero;
+  struct Regs { double q, r, t; };
+  __device__ Regs regs() const {
+    return {fform::reg(q, zero), fform::reg(r, zero), fform::reg(t, zero)};
+  }
+  __device__ double split(int64_t i, const Regs& g, bool& slow) const {
+    auto f = [&](int m, double a, double b, double c) {
+      return (m < KF) ? f64emu::fma_pos_fast(a, b, c, slow) : fma(a, b, c);
+    };
+    const double a1 = f(0, g.r, ld(y + i), ld(z + i));
+    const double b1 = f(1, g.r, ld(u + i + 1), ld(u + i + 2));
+    const double c1 = f(2, g.q, ld(u + i + 4), ld(u + i + 5));
+    const double a = f(3, g.r, a1, ld(u + i));
+    const double b = f(4, g.r, b1, ld(u + i + 3));
+    const double c = f(5, g.q, c1, ld(u + i + 6));
+    return f(7, g.t, f(6, g.t, c, b), a);
+  }
+  __device__ double exact(int64_t i, const Regs& g) const {
+    const double a = fma(g.r, fma(g.r, ld(y + i), ld(z + i)), ld(u + i));
+    const double b = fma(g.r, fma(g.r, ld(u + i + 1), ld(u + i + 2)), ld(u + i + 3));
+    const double c = fma(g.q, fma(g.q, ld(u + i + 4), ld(u + i + 5)), ld(u + i + 6));
+    return fma(g.t, fma(g.t, c, b), a);
+  }
+  __device__ void store(int64_t i, double v) const { x[i] = v; }
+};
+
+// Launches split_map_kernel<bs, pt, F> for bs in {128, 256, 512} and pt in
+// {1, 2, 4, 8} (the caller checks both).
+template <class F>
+int launch_split_map(const char* name, const F& f, int64_t n, int bs, int pt, cudaStream_t st) {
+  const int64_t grid = ceil_div(n, static_cast<int64_t>(bs) * pt);
+  if (grid > 0x7fffffff) return invalid("%s: n too large", name);
+  auto go = [&](auto B, auto P) {
+    split_map_kernel<decltype(B)::value, decltype(P)::value, F>
+        <<<static_cast<unsigned>(grid), decltype(B)::value, 0, st>>>(f, n);
+  };
+  auto by_pt = [&](auto B) {
+    switch (pt) {
+      case 1: go(B, std::integral_constant<int, 1>{}); break;
+      case 2: go(B, std::integral_constant<int, 2>{}); break;
+      case 4: go(B, std::integral_constant<int, 4>{}); break;
+      default: go(B, std::integral_constant<int, 8>{}); break;
+    }
+  };
+  if (bs == 128) by_pt(std::integral_constant<int, 128>{});
+  else if (bs == 256) by_pt(std::integral_constant<int, 256>{});
+  else by_pt(std::integral_constant<int, 512>{});
+  return after_launch(name);
 }
 
 // lcals/FIRST_DIFF.hpp:25
@@ -442,6 +486,10 @@ int b200_lcals_hydro_1d(double* x, const double* y, const double* z, double q,
                         double r, double t, int64_t n, const b200_tune* tune,
                         b200_stream_t stream) {
   if (n < 0 || (n > 0 && (!x || !y || !z))) return invalid("b200_lcals_hydro_1d: bad args");
+  // Its inner FMA on the integer pipes (f64emu::fma_pos_fast) measured no
+  // faster at 2^27 (655-680 us against 660): at 24 bytes an element the
+  // integer pipes have about 70 instructions per element to spare, and that
+  // FMA takes some 80.
   return launch_map1d("b200_lcals_hydro_1d", Hydro1D{x, y, z, q, r, t, 0}, n, tune,
                       as_stream(stream));
 }
@@ -471,32 +519,12 @@ int b200_lcals_eos(double* x, const double* y, const double* z, const double* u,
                         as_stream(stream));
   const int pt = (tune && tune->items) ? tune->items : kEosPerThread;
   if (pt != 1 && pt != 2 && pt != 4 && pt != 8) return invalid("b200_lcals_eos: bad items %d", pt);
-  const int64_t grid = ceil_div(n, static_cast<int64_t>(bs) * pt);
-  if (grid > 0x7fffffff) return invalid("b200_lcals_eos: n too large");
   cudaStream_t st = as_stream(stream);
-  auto go = [&](auto B, auto P, auto K) {
-    eos_split_kernel<decltype(B)::value, decltype(P)::value, decltype(K)::value>
-        <<<static_cast<unsigned>(grid), decltype(B)::value, 0, st>>>(x, y, z, u, q, r, t, n, 0);
-  };
-  auto by_kf = [&](auto B, auto P) {
-    switch (kf) {
-      case 1: go(B, P, std::integral_constant<int, 1>{}); break;
-      case 2: go(B, P, std::integral_constant<int, 2>{}); break;
-      default: go(B, P, std::integral_constant<int, 3>{}); break;
-    }
-  };
-  auto by_pt = [&](auto B) {
-    switch (pt) {
-      case 1: by_kf(B, std::integral_constant<int, 1>{}); break;
-      case 2: by_kf(B, std::integral_constant<int, 2>{}); break;
-      case 4: by_kf(B, std::integral_constant<int, 4>{}); break;
-      default: by_kf(B, std::integral_constant<int, 8>{}); break;
-    }
-  };
-  if (bs == 128) by_pt(std::integral_constant<int, 128>{});
-  else if (bs == 256) by_pt(std::integral_constant<int, 256>{});
-  else by_pt(std::integral_constant<int, 512>{});
-  return after_launch("b200_lcals_eos");
+  switch (kf) {
+    case 1: return launch_split_map("b200_lcals_eos", EosSplit<1>{x, y, z, u, q, r, t, 0}, n, bs, pt, st);
+    case 2: return launch_split_map("b200_lcals_eos", EosSplit<2>{x, y, z, u, q, r, t, 0}, n, bs, pt, st);
+    default: return launch_split_map("b200_lcals_eos", EosSplit<3>{x, y, z, u, q, r, t, 0}, n, bs, pt, st);
+  }
 }
 
 int b200_lcals_first_diff(double* x, const double* y, int64_t n, const b200_tune* tune,

@@ -630,6 +630,25 @@ def test_hydro_2d_integer_pipe_differences_bit_identical(kh, kn, jn):
             assert np.array_equal(g.view(np.int64), w.view(np.int64)), data
 
 
+def test_hydro_2d_integer_pipe_long_columns():
+    """More than 64 interior rows per thread (kn - 2 > 64 x 65535 with jn = 3):
+    the launcher falls back to the FP64-pipe differences (one redo bit per
+    point would not fit), and the results equal the FP64-pipe kernel's."""
+    kn, jn = 64 * 65535 + 2 + 700, 3
+    rng = np.random.default_rng(99)
+    arrs = [rng.uniform(0.5, 1.5, kn * jn) for _ in range(11)]
+    outs = []
+    for tz in (1, 7):
+        d = [dev(a) for a in arrs]
+        t = rp.Tune(tile_z=tz)
+        rp.check(lib().b200_lcals_hydro_2d(*[x.data_ptr() for x in d], 0.0041, 0.0037, kn, jn,
+                                           ctypes.byref(t), gu.stream()))
+        outs.append([gu.host(x) for x in d])
+        del d
+    for g, w in zip(outs[1], outs[0]):
+        assert np.array_equal(g.view(np.int64), w.view(np.int64))
+
+
 def test_hydro_2d_bad_difference_count_rejected():
     torch = gu.torch_cuda()
     d = torch.zeros(9, dtype=torch.float64, device="cuda")
