@@ -48,7 +48,10 @@ typedef enum b200_status {
 /* Launch-shape tuning.  Zero fields take the library default.
  * block_size: threads per CTA.  items: elements per thread per tile.
  * vec: elements per vector memory access (1, 2).  grid_blocks: CTA count
- * cap (0 = one tile per CTA).  tile_*: stencil tile shape.  time_block:
+ * cap (0 = one tile per CTA).  tile_*: stencil tile shape, or, where an
+ * entry point documents it, how many of a point's FP64 operations run in an
+ * exact integer-pipe form (JACOBI_2D, HEAT_3D, HYDRO_2D, EOS,
+ * DEL_DOT_VEC_2D: tile_z = 1 + count).  time_block:
  * stencil time steps fused per launch.  algo: kernel-specific algorithm
  * selector (documented per entry point).  wait_limit_us: limit of every
  * bounded device-side wait of the call (scan and index-list lookback and
