@@ -151,11 +151,12 @@ __device__ __forceinline__ double add_close_fast(double a, double b, bool& slow)
   const uint64_t my = ((Y & kFrac) | kHidden) << (3u - d);
   const uint64_t S = mx + my;                         // < 2^57, exact
   const uint32_t c = static_cast<uint32_t>(S >> 56);  // carried into the next binade
-  const uint64_t mant = S >> (3u + c);                // 53 bits with the hidden one
-  const uint32_t rem = static_cast<uint32_t>(S) & ((8u << c) - 1u);
-  const uint32_t half = 4u << c;
-  const uint64_t up = (rem > half || (rem == half && (mant & 1u))) ? 1u : 0u;
-  return from_bits((X & kSign) | ((static_cast<uint64_t>(emax + c - 1u) << 52) + mant + up));
+  const uint32_t k = 3u + c;                          // bits dropped
+  // round to nearest even in one add: with q = S >> k, S + (half an ulp - 1)
+  // + (q & 1) carries into q exactly when the dropped bits exceed half an ulp,
+  // or equal it and q is odd
+  const uint64_t mant = (S + ((4ull << c) - 1u) + ((S >> k) & 1u)) >> k;  // 53 bits (54 on a carry)
+  return from_bits((X & kSign) | ((static_cast<uint64_t>(emax + c - 1u) << 52) + mant));
 }
 
 // a + b (bit patterns A and B) for normal operands of either sign with biased
