@@ -274,17 +274,16 @@ __device__ __forceinline__ double mul_fast(double a, double b, bool& slow) {
   const uint64_t mA = (A & kFrac) | kHidden, mB = (B & kFrac) | kHidden;
   const uint64_t lo = mA * mB;
   const uint64_t hi = __umul64hi(mA, mB);  // product < 2^106: hi < 2^42
-  int e = static_cast<int>(eA) + static_cast<int>(eB) - 1023;
-  const bool top = (hi >> 41) != 0u;  // product in [2^105, 2^106)
-  uint64_t mant = top ? ((hi << 11) | (lo >> 53)) : ((hi << 12) | (lo >> 52));
-  const uint64_t rem = top ? (lo & ((1ULL << 53) - 1u)) : (lo & ((1ULL << 52) - 1u));
-  const uint64_t half = top ? (1ULL << 52) : (1ULL << 51);
-  e += top ? 1 : 0;
-  if (rem > half || (rem == half && (mant & 1u))) mant += 1u;
-  if (mant >> 53) {
-    mant >>= 1;
-    e += 1;
-  }
+  const uint32_t top = static_cast<uint32_t>(hi >> 41);  // 1: product in [2^105, 2^106)
+  const int e = static_cast<int>(eA) + static_cast<int>(eB) - 1023 + static_cast<int>(top);
+  const uint32_t s = 52u + top;  // bits dropped
+  // round to nearest even in one 128-bit add: half an ulp - 1, plus the kept
+  // part's low bit, carries into the kept part exactly when it should; a
+  // carry to 2^53 runs into the exponent field when packed below
+  const uint64_t bias = ((1ULL << (s - 1u)) - 1u) + ((lo >> s) & 1u);
+  const uint64_t lo2 = lo + bias;
+  const uint64_t hi2 = hi + (lo2 < lo ? 1u : 0u);
+  const uint64_t mant = (hi2 << (64u - s)) | (lo2 >> s);  // 53 bits (54 on a carry)
   slow |= (eA - 1u >= 2046u) || (eB - 1u >= 2046u) || e <= 0 || e >= 2047;
   return from_bits(((A ^ B) & kSign) | ((static_cast<uint64_t>(e & 0x7ff) - 1u) << 52) + mant);
 }
