@@ -650,7 +650,9 @@ extern "C" {
 // point on the integer pipe 92.3; two 125.1; with the product on the FP64
 // pipe, two adds per point 94.2, one 114.8.  One integer-pipe add costs
 // about 33 us of the integer pipes' time per half-step here (some 40
-// instructions), the integer product about 59.
+// instructions), the integer product about 59.  With both integer forms rounding in
+// one add (90.1 us at one add per point), five and six adds per four points
+// measured 94.4 and 102.5 us.
 constexpr int kJacobiIntAdds4 = 4;
 constexpr bool kJacobiMulInt = true;
 
