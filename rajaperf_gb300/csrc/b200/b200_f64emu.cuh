@@ -164,8 +164,8 @@ __device__ __forceinline__ double add_close_fast(double a, double b, bool& slow)
 // is X; aligned to its exponent with 3 guard bits both significands are
 // exact, so S = |X| +- |Y| (never negative) is the exact result's magnitude
 // in units of 2^(ex - 1078).  A difference may cancel any number of leading
-// bits: S is shifted up until its leading one is bit 63 (a leading-zero
-// count), which keeps every bit, and the 11 bits below the 53 kept ones
+// bits: S is shifted up until its leading one is bit 62 (a leading-zero
+// count), which keeps every bit, and the 10 bits below the 53 kept ones
 // decide round to nearest even (at most 4 of them can be set).  An exact
 // zero is +0 (round to nearest).  `slow` is set when an operand is zero,
 // subnormal, infinite or NaN, the exponents are further apart, or the result
@@ -196,12 +196,14 @@ __device__ __forceinline__ double add_near_bits(uint64_t A, uint64_t B, bool& sl
     slow = true;
     return 0.0;
   }
-  const uint64_t V = S << lz;                             // leading one at bit 63
-  const uint64_t mant = V >> 11;                          // 53 bits with the hidden one
-  const uint32_t rem = static_cast<uint32_t>(V) & 0x7ffu;
-  const uint64_t up = (rem > 0x400u || (rem == 0x400u && (mant & 1u))) ? 1u : 0u;
+  // leading one at bit 62 (lz >= 7, so no bit is lost); the 53 bits from there
+  // down are kept, and adding (half an ulp - 1) plus the kept part's last bit
+  // before the shift rounds to nearest even (a carry to 2^53 runs into the
+  // exponent field when packed)
+  const uint64_t W = S << (lz - 1u);
+  const uint64_t mant = (W + 0x1ffu + ((W >> 10) & 1u)) >> 10;
   const uint64_t sign = a_big ? (A & kSign) : (SUB ? (~B & kSign) : (B & kSign));
-  return from_bits(sign | ((static_cast<uint64_t>(e - 1) << 52) + mant + up));
+  return from_bits(sign | ((static_cast<uint64_t>(e - 1) << 52) + mant));
 }
 __device__ __forceinline__ double add_near_fast(double a, double b, bool& slow) {
   return add_near_bits<false>(bits_opaque(a), bits_opaque(b), slow);
